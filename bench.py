@@ -1,0 +1,300 @@
+"""Benchmark: DOF-stage updates/s of the GB300 DGSEM operator + LSERK stepper.
+
+Workload (default): compressible Navier-Stokes Taylor-Green vortex, N=7 Gauss-Lobatto nodes,
+split-form flux differencing with the Pirozzoli two-point flux, Roe surface flux, BR1 lifting,
+24^3 periodic hexahedra on [-pi,pi]^3 (7 077 888 DOF x 5 variables), Ma 0.1, Re 1600, Pr 0.72,
+Carpenter RK4-5.  A step is one LSERK step (5 RHS stages) over the whole mesh; inputs are seeded
+synthetic TGV states (no dataset exists for this path).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--precision fp64|mixed]
+
+One JSON line on rank 0.  Multi-GPU runs are replicas (each rank steps its own mesh; no collective
+on the data path): value = all ranks' DOF-stages / max-over-ranks time, scaling "weak".
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (N, elems per direction, split, riemann, parabolic, mu0, flops/DOF-stage, bytes/DOF-stage)
+    "tgv_n7_24cube_split_pi_roe_br1": dict(N=7, ne=24, SplitDG="pi", Riemann="roe", parabolic=True, mu0=1 / 1600.0),
+    "tgv_n7_64cube_split_pi_roe_br1": dict(N=7, ne=64, SplitDG="pi", Riemann="roe", parabolic=True, mu0=1 / 1600.0),
+}
+# Algorithmic work per DOF-stage for the N=7 split-form NS path (FMA = 2 flops), per kernel:
+#   prolong: ConsToPrim 14 ; lift: 30n+75 + 270/n + 15 ; face: 1200/n ; volume: 135N + 115 + 30n + 60/n + 30
+ALG_FLOPS_N7 = {"prolong": 14.0, "lift": 30 * 8 + 75 + 270 / 8 + 15, "face": 1200 / 8,
+                "volume": 135 * 7 + 115 + 30 * 8 + 60 / 8 + 30}
+ALG_BYTES_N7 = 510.0  # compulsory HBM bytes per DOF-stage of a fully fused implementation (FP64)
+TGV_R = 71.42857
+CFL = 0.9
+DFL = 0.9
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--workload", default="tgv_n7_24cube_split_pi_roe_br1", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu, self.samples, self._stop = gpu, [], threading.Event()
+        self._t = threading.Thread(target=self._run, daemon=True)
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.samples.append([x.strip() for x in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = sorted(float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit())
+        mx = max(float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()) if sm else None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if len(s) > 5 + k and s[5 + k] == "Active"})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, x, device=None):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline(workload, threads=None, target_s=12.0):
+    """The oracle (CPU restatement of the reference formulas, OpenMP) on a bounded sample:
+    full LSERK steps on an 8^3-element box of the same N/form (a 1/27 slice of the 24^3 workload)."""
+    import numpy as np  # noqa: F401
+    import galaexi_gb300 as gx
+    from oracle.oracle import Oracle, set_threads
+    w = WORKLOADS[workload]
+    nthreads = set_threads(threads or os.cpu_count() or 1)
+    ne = 8
+    cfg = gx.config(N=w["N"], NodeType="gauss-lobatto", Riemann=w["Riemann"], SplitDG=w["SplitDG"],
+                    parabolic=w["parabolic"], mu0=w["mu0"], R=TGV_R)
+    mesh = gx.Mesh(w["N"], 2, ne, ne, ne, (-math.pi,) * 3, (math.pi,) * 3)
+    U0 = gx.tgv_state(mesh, mach=0.1, R=TGV_R)
+    o = Oracle(cfg, mesh)
+    dt, _ = o.calc_timestep(U0, CFL, DFL)
+    t0 = time.perf_counter()
+    U, Ut = o.lserk_steps(U0, dt, 1)
+    one = time.perf_counter() - t0
+    steps = max(1, min(50, int(target_s / max(one, 1e-3))))
+    t0 = time.perf_counter()
+    U, Ut = o.lserk_steps(U, dt, steps, Ut_tmp=Ut)
+    el = time.perf_counter() - t0
+    val = mesh.nDOF * 5 * steps / el
+    return {"value": val, "unit": "DOF-stage/s", "cores": nthreads, "kind": "port",
+            "sample": "%d LSERK steps (5 stages) on %d^3 elements N=%d (%d DOF), %.1f s" % (
+                steps, ne, w["N"], mesh.nDOF, el)}
+
+
+def run_reference(args, world, rank):
+    """Reference arm: the CPU restatement of the reference's formulas (the reference itself is CUDA
+    Fortran and has no CPU build; it cannot be compiled here), all host threads, same metric."""
+    if rank != 0:
+        return
+    w = WORKLOADS[args.workload]
+    for _ in range(args.warmup):
+        pass
+    res = cpu_baseline(args.workload, target_s=max(5.0, 2.0 * args.steps))
+    line = {"metric": "DOF-stage updates/s", "value": res["value"], "unit": "DOF-stage/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic TGV state",
+            "impl": "reference",
+            "config": {"workload": args.workload, "N": w["N"], "elements_per_dir": w["ne"], "form": "split PI",
+                       "riemann": w["Riemann"], "lifting": "BR1"},
+            "cpu_baseline": res,
+            "e2e": {"value": res["value"], "unit": "DOF-stage/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    import galaexi_gb300 as gx
+    from galaexi_gb300 import _native as nat
+    import ctypes
+
+    torch.cuda.set_device(local)
+    w = WORKLOADS[args.workload]
+    N, ne = w["N"], w["ne"]
+    cfg = gx.config(N=N, NodeType="gauss-lobatto", Riemann=w["Riemann"], SplitDG=w["SplitDG"],
+                    parabolic=w["parabolic"], mu0=w["mu0"], R=TGV_R, precision=args.precision)
+    mesh = gx.Mesh(N, 2, ne, ne, ne, (-math.pi,) * 3, (math.pi,) * 3)
+    U0 = gx.tgv_state(mesh, mach=0.1, R=TGV_R)
+    op = gx.DG(cfg, mesh)
+    stream = torch.cuda.current_stream()
+    U = torch.from_numpy(U0).cuda()
+    Ut_tmp = torch.zeros_like(U)
+    dt, err = op.CalcTimeStep(U, CFL, DFL)
+    assert err == 0
+    nDOF = mesh.nDOF
+    # ---- device-resident timing
+    for _ in range(args.warmup):
+        op.TimeStepByLSERKW2(0.0, dt, U, Ut_tmp)
+    torch.cuda.synchronize()
+    barrier(world)
+    launches0 = op.kernel_launches
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            op.TimeStepByLSERKW2(0.0, dt, U, Ut_tmp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = e0.elapsed_time(e1)
+    launches = op.kernel_launches - launches0
+    ms = max_over_ranks(world, ms, device="cuda")
+    value = world * nDOF * 5 * args.steps / (ms * 1e-3)
+    bad = op.check_state(U)
+    # ---- end-to-end through the public API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        Uh = torch.from_numpy(U0).pin_memory()
+        Uout = torch.empty_like(Uh).pin_memory()
+        Ud = torch.empty_like(U)
+        Ut2 = torch.zeros_like(U)
+        for _ in range(1):
+            Ud.copy_(Uh, non_blocking=True)
+            op.TimeStepByLSERKW2(0.0, dt, Ud, Ut2)
+            Uout.copy_(Ud, non_blocking=True)
+        torch.cuda.synchronize()
+        barrier(world)
+        e0.record(stream)
+        for _ in range(args.steps):
+            Ud.copy_(Uh, non_blocking=True)
+            op.TimeStepByLSERKW2(0.0, dt, Ud, Ut2)
+            Uout.copy_(Ud, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms_e2e = max_over_ranks(world, e0.elapsed_time(e1), device="cuda")
+        e2e = {"value": world * nDOF * 5 * args.steps / (ms_e2e * 1e-3), "unit": "DOF-stage/s",
+               "h2d_bytes_per_step": Uh.numel() * 8, "d2h_bytes_per_step": Uout.numel() * 8}
+    # ---- per-kernel timing (CUDA events on the launching stream) for the roofline
+    out = (ctypes.c_double * 5)()
+    Up = U.clone()
+    Utp = torch.zeros_like(U)
+    nat.check(nat.lib().dg_profile_stage(op._h, ctypes.c_void_p(Up.data_ptr()), ctypes.c_void_p(Utp.data_ptr()),
+                                         dt, 20, out, ctypes.c_void_p(stream.cuda_stream)), "dg_profile_stage")
+    kms = {"prolong": out[0], "lift": out[1], "face": out[2], "volume": out[3], "stage": out[4]}
+    peak64 = ctypes.c_double()
+    peak32 = ctypes.c_double()
+    nat.check(nat.lib().dg_measure_fma_peak(0, ctypes.byref(peak64)), "fma peak fp64")
+    nat.check(nat.lib().dg_measure_fma_peak(1, ctypes.byref(peak32)), "fma peak fp32")
+    peak = peak64.value if args.precision == "fp64" else peak32.value
+    vol_flops = ALG_FLOPS_N7["volume"] * nDOF
+    achieved = vol_flops / (kms["volume"] * 1e-3) * 1e-12
+    mp = {}
+    try:
+        mp = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = mp.get("hbm_gbs", 6800.0)
+    stage_s = kms["stage"] * 1e-3
+    roofline = {
+        "kernel": "k_volume (split-form volume + viscous volume + surface integral + Jacobian + RK stage)",
+        "bound": "fp64" if args.precision == "fp64" else "fp32",
+        "achieved": achieved, "peak": peak * 1e-3, "unit": "TFLOP/s", "frac": achieved / (peak * 1e-3),
+        "peak_source": "FMA-chain microkernel measured in this run (no FP64/FP32 CUDA-core peak in MEASURED_PEAKS.json)",
+        "alg_flops_per_dof": ALG_FLOPS_N7["volume"],
+        "traffic": None,
+        "kernel_ms": kms,
+        "stage": {"alg_flops_per_dof_stage": sum(ALG_FLOPS_N7.values()),
+                  "achieved_tflops": sum(ALG_FLOPS_N7.values()) * nDOF / stage_s * 1e-12,
+                  "alg_bytes_per_dof_stage": ALG_BYTES_N7,
+                  "hbm_gbs_alg": ALG_BYTES_N7 * nDOF / stage_s * 1e-9,
+                  "hbm_peak_gbs": hbm_peak, "hbm_frac_of_measured": ALG_BYTES_N7 * nDOF / stage_s * 1e-9 / hbm_peak},
+        "fp64_peak_tflops_measured": peak64.value * 1e-3,
+        "fp32_peak_tflops_measured": peak32.value * 1e-3,
+    }
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args.workload)
+    if rank == 0:
+        line = {"metric": "DOF-stage updates/s", "value": value, "unit": "DOF-stage/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64" if args.precision == "fp64" else "f32-bulk/f64-rk",
+                "data": "synthetic (seeded TGV initial state, generated mesh)",
+                "config": {"workload": args.workload, "N": N, "elements_per_dir": ne, "nDOF": nDOF,
+                           "form": "split PI", "riemann": w["Riemann"], "lifting": "BR1", "precision": args.precision,
+                           "dt": dt, "l2": "inputs larger than L2 (state 283 MB)", "parallelism": "replicas"},
+                "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
+                "gpu_launches": launches, "bad_nodes_after": bad}
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_init(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

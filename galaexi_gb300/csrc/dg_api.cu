@@ -1,0 +1,386 @@
+// C ABI of the GB300 DGSEM operator: context, mesh upload, RHS, LSERK stepping, CFL time step.
+// The entry points replace the reference's module-global operator (see include/galaexi_gb300.h).
+#include <cuda_runtime.h>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/galaexi_gb300.h"
+#include "dg_host.h"
+#include "dg_ctx.h"
+
+using gxh::set_error;
+
+namespace {
+
+// Carpenter-Kennedy RK4-5 (timedisc_vars.f90:213-227), stage s = 1..5
+const double kRKA[6] = {0., 0., 567301805773.0 / 1357537059087.0, 2404267990393.0 / 2016746695238.0,
+                        3550918686646.0 / 2091501179385.0, 1275806237668.0 / 842570457699.0};
+const double kRKb[6] = {0., 1432997174477.0 / 9575080441755.0, 5161836677717.0 / 13612068292357.0,
+                        1720146321549.0 / 2090206949498.0, 3134564353537.0 / 4481467310338.0,
+                        2277821191437.0 / 14882151754819.0};
+// CFL / DFL scaling of FillCFL_DFL (timedisc_func.f90:480-550) for Carpenter RK4-5
+// (CFLScaleAlpha timedisc_vars.f90:193-206, DFLScaleAlpha timedisc_vars.f90:104-108, RelativeDFL 1.853)
+double cfl_alpha(int node_type, int N) {
+  static const double G[15] = {2.0351, 1.7595, 1.5401, 1.3702, 1.2375, 1.1318, 1.0440, 0.9709,
+                               0.9079, 0.8539, 0.8066, 0.7650, 0.7290, 0.6952, 0.6660};
+  static const double GL[15] = {4.7497, 3.4144, 2.8451, 2.4739, 2.2027, 1.9912, 1.8225, 1.6830,
+                                1.5682, 1.4692, 1.3849, 1.3106, 1.2454, 1.1880, 1.1362};
+  const int i = (N < 15 ? N : 15) - 1;
+  return node_type == DG_NODETYPE_GAUSS ? G[i] : GL[i];
+}
+double dfl_alpha(int node_type, int N) {
+  static const double G[10] = {1.12, 0.76, 0.55, 0.41, 0.32, 0.25, 0.20, 0.17, 0.14, 0.12};
+  static const double GL[10] = {4.50, 1.95, 1.18, 0.79, 0.56, 0.42, 0.32, 0.25, 0.20, 0.17};
+  const int i = (N < 10 ? N : 10) - 1;
+  return node_type == DG_NODETYPE_GAUSS ? G[i] : GL[i];
+}
+
+const gxc::NPTable* table_for(int n) {
+  switch (n) {
+    case 2: return &gx_np_table_2;
+    case 3: return &gx_np_table_3;
+    case 4: return &gx_np_table_4;
+    case 5: return &gx_np_table_5;
+    case 6: return &gx_np_table_6;
+    case 7: return &gx_np_table_7;
+    case 8: return &gx_np_table_8;
+    case 9: return &gx_np_table_9;
+    case 10: return &gx_np_table_10;
+  }
+  return nullptr;
+}
+
+#define CUDA_TRY(call, what)                                                                  \
+  do {                                                                                        \
+    cudaError_t _e = (call);                                                                  \
+    if (_e != cudaSuccess) {                                                                  \
+      set_error(std::string(what) + ": " + cudaGetErrorString(_e));                          \
+      return DG_ERR_CUDA;                                                                     \
+    }                                                                                         \
+  } while (0)
+
+template <typename R>
+int upload_basis(dg_ctx* ctx, gxc::PrecData<R>& P) {
+  const int n = ctx->n;
+  std::vector<R> h(3 * n * n + 4 * n);
+  for (int t = 0; t < n * n; ++t) {
+    h[t] = (R)ctx->B.D[t];
+    h[n * n + t] = (R)ctx->B.DhatT[t];
+    h[2 * n * n + t] = (R)ctx->B.DVS[t];
+  }
+  for (int t = 0; t < n; ++t) {
+    h[3 * n * n + t] = (R)ctx->B.Lm[t];
+    h[3 * n * n + n + t] = (R)ctx->B.Lp[t];
+    h[3 * n * n + 2 * n + t] = (R)ctx->B.Lhm[t];
+    h[3 * n * n + 3 * n + t] = (R)ctx->B.Lhp[t];
+  }
+  if (!P.basis.alloc(h.size())) { set_error("cudaMalloc basis"); return DG_ERR_ALLOC; }
+  CUDA_TRY(cudaMemcpy(P.basis.p, h.data(), h.size() * sizeof(R), cudaMemcpyHostToDevice), "upload basis");
+  return DG_OK;
+}
+
+int run_rhs(dg_ctx* ctx, const double* U, gx::RKArgs rk, int rkmode, cudaStream_t st) {
+  const gxc::NPTable* T = table_for(ctx->n);
+  if (!T) { set_error("unsupported N"); return DG_ERR_UNSUPPORTED; }
+  return ctx->cfg.precision == DG_PRECISION_FP64 ? T->rhs_d(ctx, U, rk, rkmode, st) : T->rhs_f(ctx, U, rk, rkmode, st);
+}
+
+template <typename R>
+int alloc_prec(dg_ctx* ctx, gxc::PrecData<R>& P, const std::vector<double>& met, const std::vector<double>& fgeo) {
+  const size_t nE = ctx->nElems, nS = ctx->nSides, n2 = ctx->n2, n3 = ctx->n3;
+  const bool par = ctx->cfg.parabolic != 0;
+  bool ok = P.Met.alloc(nE * 10 * n3) && P.Fgeo.alloc(nS * 10 * n2) && P.Pvol.alloc(nE * 7 * n3) &&
+            P.Uf.alloc(2 * nS * 5 * n2) && P.Pf.alloc(2 * nS * 6 * n2) && P.Flux.alloc(nS * 5 * n2);
+  if (ok && par) ok = P.Gvol.alloc(nE * 15 * n3) && P.Gf.alloc(2 * nS * 15 * n2);
+  if (!ok) { set_error("cudaMalloc scratch"); return DG_ERR_ALLOC; }
+  std::vector<R> hm(met.size()), hg(fgeo.size());
+  for (size_t t = 0; t < met.size(); ++t) hm[t] = (R)met[t];
+  for (size_t t = 0; t < fgeo.size(); ++t) hg[t] = (R)fgeo[t];
+  CUDA_TRY(cudaMemcpy(P.Met.p, hm.data(), hm.size() * sizeof(R), cudaMemcpyHostToDevice), "upload metrics");
+  CUDA_TRY(cudaMemcpy(P.Fgeo.p, hg.data(), hg.size() * sizeof(R), cudaMemcpyHostToDevice), "upload face geometry");
+  return DG_OK;
+}
+
+int check_ctx(dg_ctx* ctx, bool need_mesh) {
+  if (!ctx) { set_error("null context"); return DG_ERR_ARG; }
+  if (need_mesh && !ctx->mesh_ok) { set_error("dg_set_mesh has not been called"); return DG_ERR_ARG; }
+  return DG_OK;
+}
+
+// FMA-chain microkernel: 8 independent dependency chains per thread
+template <typename T>
+__global__ void __launch_bounds__(256) k_fma_peak(T* out, int iters, T a, T b) {
+  T x[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) x[c] = (T)(threadIdx.x + c) * (T)1e-7;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) x[c] = fma(x[c], a, b);
+  }
+  T s = 0;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) s += x[c];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+template <typename T>
+int fma_peak(double* gflops) {
+  int dev = 0, nsm = 0;
+  CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
+  CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
+  const int threads = 256, blocks = nsm * 16;
+  const int iters = sizeof(T) == 8 ? 4096 : 65536;
+  T* out = nullptr;
+  CUDA_TRY(cudaMalloc(&out, sizeof(T) * threads * blocks), "cudaMalloc");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; ++rep) {
+    cudaEventRecord(e0);
+    k_fma_peak<T><<<blocks, threads>>>(out, iters, (T)0.999999, (T)1e-7);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && ms < best) best = ms;
+  }
+  cudaError_t err = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (err != cudaSuccess) { set_error(std::string("fma peak: ") + cudaGetErrorString(err)); return DG_ERR_CUDA; }
+  *gflops = 2.0 * 8.0 * (double)iters * threads * blocks / (best * 1e-3) * 1e-9;
+  return DG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dg_measure_fma_peak(int precision, double* gflops) {
+  if (!gflops) { set_error("null output"); return DG_ERR_ARG; }
+  return precision == 0 ? fma_peak<double>(gflops) : fma_peak<float>(gflops);
+}
+
+int dg_profile_stage(dg_ctx* ctx, double* d_U, double* d_Ut_tmp, double dt, int reps, double* ms_out, void* stream) {
+  if (int rc = check_ctx(ctx, true)) return rc;
+  if (!d_U || !d_Ut_tmp || !ms_out || reps < 1) { set_error("dg_profile_stage: bad argument"); return DG_ERR_ARG; }
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t ev[5];
+  for (int i = 0; i < 5; ++i) CUDA_TRY(cudaEventCreate(&ev[i]), "cudaEventCreate");
+  double acc[5] = {0, 0, 0, 0, 0};
+  int rc = DG_OK;
+  for (int r = 0; r < reps && rc == DG_OK; ++r) {
+    const int stage = 2 + (r % 4);
+    gx::RKArgs rk{d_U, d_Ut_tmp, nullptr, -1. * kRKA[stage], kRKb[stage] * dt};
+    rc = table_for(ctx->n)->stage_events(ctx, d_U, rk, st, ev);
+    if (rc != DG_OK) break;
+    if (cudaEventSynchronize(ev[4]) != cudaSuccess) { set_error("event sync"); rc = DG_ERR_CUDA; break; }
+    float ms[4];
+    for (int k = 0; k < 4; ++k) cudaEventElapsedTime(&ms[k], ev[k], ev[k + 1]);
+    float tot = 0;
+    cudaEventElapsedTime(&tot, ev[0], ev[4]);
+    for (int k = 0; k < 4; ++k) acc[k] += ms[k];
+    acc[4] += tot;
+  }
+  for (int i = 0; i < 5; ++i) cudaEventDestroy(ev[i]);
+  if (rc != DG_OK) return rc;
+  for (int k = 0; k < 5; ++k) ms_out[k] = acc[k] / reps;
+  return DG_OK;
+}
+
+
+int dg_ctx_create(const dg_config* cfg, dg_ctx** out) {
+  if (!cfg || !out) { set_error("dg_ctx_create: null argument"); return DG_ERR_ARG; }
+  *out = nullptr;
+  if (cfg->N < 1 || cfg->N > DG_MAX_N) { set_error("N out of range 1..DG_MAX_N"); return DG_ERR_ARG; }
+  if (cfg->node_type != DG_NODETYPE_GAUSS && cfg->node_type != DG_NODETYPE_GAUSS_LOBATTO) {
+    set_error("unknown node type"); return DG_ERR_ARG;
+  }
+  if (cfg->riemann < DG_RIEMANN_LF || cfg->riemann > DG_RIEMANN_AVERAGE) { set_error("unknown Riemann solver"); return DG_ERR_ARG; }
+  if (cfg->split_dg < DG_SPLIT_NONE || cfg->split_dg > DG_SPLIT_PI) { set_error("unknown SplitDG"); return DG_ERR_ARG; }
+  if (cfg->split_dg >= 0 && cfg->node_type != DG_NODETYPE_GAUSS_LOBATTO) {
+    // InitSplitDG (splitflux.f90:115-119)
+    set_error("Wrong Pointset: Gauss-Lobatto-Points are mandatory for using SplitDG"); return DG_ERR_ARG;
+  }
+  if (cfg->split_dg >= 0 && (cfg->riemann == DG_RIEMANN_HLL || cfg->riemann == DG_RIEMANN_HLLC ||
+                             cfg->riemann == DG_RIEMANN_HLLE || cfg->riemann == DG_RIEMANN_HLLEM)) {
+    // src/CMakeLists.txt:108-127 rejects the HLL family with split fluxes
+    set_error("HLL-type Riemann solvers are not available with split-form DG"); return DG_ERR_ARG;
+  }
+  if (cfg->split_dg < 0 && cfg->riemann == DG_RIEMANN_AVERAGE) { set_error("Riemann=avg needs SplitDG"); return DG_ERR_ARG; }
+  if (cfg->split_dg >= 0 && cfg->N < 2) { set_error("split form needs N >= 2"); return DG_ERR_UNSUPPORTED; }
+  if (cfg->parabolic && cfg->lifting != DG_LIFTING_BR1) { set_error("only BR1 lifting is built"); return DG_ERR_UNSUPPORTED; }
+  if (!(cfg->kappa > 1.) || !(cfg->R > 0.)) { set_error("bad kappa or R"); return DG_ERR_ARG; }
+  if (cfg->parabolic && !(cfg->Pr > 0.)) { set_error("bad Pr"); return DG_ERR_ARG; }
+  if (cfg->precision != DG_PRECISION_FP64 && cfg->precision != DG_PRECISION_MIXED) { set_error("bad precision"); return DG_ERR_ARG; }
+  dg_ctx* ctx = new dg_ctx();
+  ctx->cfg = *cfg;
+  ctx->N = cfg->N;
+  ctx->n = cfg->N + 1;
+  ctx->n2 = ctx->n * ctx->n;
+  ctx->n3 = ctx->n2 * ctx->n;
+  gxh::basis_1d(cfg->N, cfg->node_type, ctx->B);
+  const gxc::NPTable* T = table_for(ctx->n);
+  int rc = (cfg->precision == DG_PRECISION_FP64) ? upload_basis(ctx, ctx->d) : upload_basis(ctx, ctx->f);
+  if (rc == DG_OK) rc = (cfg->precision == DG_PRECISION_FP64) ? T->configure_d() : T->configure_f();
+  if (rc == DG_OK && !(ctx->red.alloc(2) && ctx->bad.alloc(1))) { set_error("cudaMalloc"); rc = DG_ERR_ALLOC; }
+  if (rc != DG_OK) { dg_ctx_destroy(ctx); return rc; }
+  *out = ctx;
+  return DG_OK;
+}
+
+int dg_ctx_destroy(dg_ctx* ctx) {
+  if (!ctx) return DG_OK;
+  ctx->d.release();
+  ctx->f.release();
+  ctx->MetD.release();
+  ctx->E2S.release();
+  ctx->red.release();
+  ctx->bad.release();
+  delete ctx;
+  return DG_OK;
+}
+
+int dg_set_mesh(dg_ctx* ctx, int nElems, int nSides, int nBCSides, const double* Mf, const double* Mg,
+                const double* Mh, const double* sJ, const double* nv, const double* t1, const double* t2,
+                const double* se, const int* e2s, const int* s2e) {
+  if (int rc = check_ctx(ctx, false)) return rc;
+  if (nElems < 1 || nSides < 1 || !Mf || !Mg || !Mh || !sJ || !nv || !t1 || !t2 || !se || !e2s || !s2e) {
+    set_error("dg_set_mesh: bad argument"); return DG_ERR_ARG;
+  }
+  if (nBCSides != 0) { set_error("boundary sides are not supported"); return DG_ERR_UNSUPPORTED; }
+  const int n = ctx->n, n2 = ctx->n2, n3 = ctx->n3;
+  // validate connectivity: every side has one master (flip 0) and one slave (flip 1..4)
+  std::vector<int> seen((size_t)nSides * 2, 0);
+  std::vector<int> he2s((size_t)nElems * 12);
+  for (int e = 0; e < nElems; ++e)
+    for (int ls = 0; ls < 6; ++ls) {
+      const int side = e2s[3 * (ls + 6 * (size_t)e)] - 1, flip = e2s[3 * (ls + 6 * (size_t)e) + 1];
+      if (side < 0 || side >= nSides || flip < 0 || flip > 4) { set_error("ElemToSide out of range"); return DG_ERR_ARG; }
+      seen[2 * (size_t)side + (flip == 0 ? 0 : 1)]++;
+      he2s[(e * 6 + ls) * 2] = side;
+      he2s[(e * 6 + ls) * 2 + 1] = flip;
+    }
+  for (size_t t = 0; t < seen.size(); ++t)
+    if (seen[t] != 1) { set_error("every side needs exactly one master and one slave element"); return DG_ERR_ARG; }
+  (void)s2e;
+  // pack metrics [e][10][n3] and face geometry [side][10][n2]
+  std::vector<double> met((size_t)nElems * 10 * n3), fgeo((size_t)nSides * 10 * n2);
+  for (size_t e = 0; e < (size_t)nElems; ++e)
+    for (int node = 0; node < n3; ++node) {
+      const size_t g = e * n3 + node;
+      for (int c = 0; c < 3; ++c) {
+        met[(e * 10 + c) * n3 + node] = Mf[3 * g + c];
+        met[(e * 10 + 3 + c) * n3 + node] = Mg[3 * g + c];
+        met[(e * 10 + 6 + c) * n3 + node] = Mh[3 * g + c];
+      }
+      met[(e * 10 + 9) * n3 + node] = sJ[g];
+    }
+  for (size_t s = 0; s < (size_t)nSides; ++s)
+    for (int pq = 0; pq < n2; ++pq) {
+      const size_t g = s * n2 + pq;
+      for (int c = 0; c < 3; ++c) {
+        fgeo[(s * 10 + c) * n2 + pq] = nv[3 * g + c];
+        fgeo[(s * 10 + 3 + c) * n2 + pq] = t1[3 * g + c];
+        fgeo[(s * 10 + 6 + c) * n2 + pq] = t2[3 * g + c];
+      }
+      fgeo[(s * 10 + 9) * n2 + pq] = se[g];
+    }
+  (void)n;
+  ctx->nElems = nElems;
+  ctx->nSides = nSides;
+  ctx->d.release();
+  ctx->f.release();
+  int rc;
+  if (ctx->cfg.precision == DG_PRECISION_FP64) {
+    rc = upload_basis(ctx, ctx->d);
+    if (rc == DG_OK) rc = alloc_prec(ctx, ctx->d, met, fgeo);
+  } else {
+    rc = upload_basis(ctx, ctx->f);
+    if (rc == DG_OK) rc = alloc_prec(ctx, ctx->f, met, fgeo);
+  }
+  if (rc != DG_OK) return rc;
+  if (!ctx->MetD.alloc(met.size()) || !ctx->E2S.alloc(he2s.size())) { set_error("cudaMalloc mesh"); return DG_ERR_ALLOC; }
+  CUDA_TRY(cudaMemcpy(ctx->MetD.p, met.data(), met.size() * sizeof(double), cudaMemcpyHostToDevice), "upload metrics");
+  CUDA_TRY(cudaMemcpy(ctx->E2S.p, he2s.data(), he2s.size() * sizeof(int), cudaMemcpyHostToDevice), "upload E2S");
+  ctx->mesh_ok = true;
+  return DG_OK;
+}
+
+int dg_rhs(dg_ctx* ctx, double t, const double* d_U, double* d_Ut, void* stream) {
+  if (int rc = check_ctx(ctx, true)) return rc;
+  if (!d_U || !d_Ut) { set_error("dg_rhs: null state"); return DG_ERR_ARG; }
+  (void)t;  // periodic meshes: no time-dependent boundary states or sources
+  gx::RKArgs rk{nullptr, nullptr, d_Ut, 0., 0.};
+  cudaStream_t st = (cudaStream_t)stream;
+  return run_rhs(ctx, d_U, rk, 0, st);
+}
+
+int dg_lserk_steps(dg_ctx* ctx, double t, double dt, int nSteps, double* d_U, double* d_Ut_tmp, void* stream) {
+  if (int rc = check_ctx(ctx, true)) return rc;
+  if (!d_U || !d_Ut_tmp || nSteps < 0) { set_error("dg_lserk_steps: bad argument"); return DG_ERR_ARG; }
+  cudaStream_t st = (cudaStream_t)stream;
+  for (int s = 0; s < nSteps; ++s) {
+    for (int stage = 1; stage <= 5; ++stage) {
+      // TimeStepByLSERKW2 (timestep.f90:83-104): mRKA = 0 at stage 1, -RKA(stage) otherwise
+      gx::RKArgs rk{d_U, d_Ut_tmp, nullptr, stage == 1 ? 0. : -1. * kRKA[stage], kRKb[stage] * dt};
+      int rc = run_rhs(ctx, d_U, rk, 1, st);
+      if (rc != DG_OK) return rc;
+    }
+  }
+  (void)t;
+  return DG_OK;
+}
+
+int dg_lserk_step(dg_ctx* ctx, double t, double dt, double* d_U, double* d_Ut_tmp, void* stream) {
+  return dg_lserk_steps(ctx, t, dt, 1, d_U, d_Ut_tmp, stream);
+}
+
+int dg_calc_timestep(dg_ctx* ctx, const double* d_U, double cfl_scale, double dfl_scale, double* dt_out, void* stream) {
+  if (int rc = check_ctx(ctx, true)) return rc;
+  if (!d_U || !dt_out) { set_error("dg_calc_timestep: null argument"); return DG_ERR_ARG; }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int N = ctx->N;
+  const dg_config& c = ctx->cfg;
+  const double cflS = cfl_scale * cfl_alpha(c.node_type, N) / (2. * N + 1.);
+  const double dflS = dfl_scale * dfl_alpha(c.node_type, N) * 1.853 / ((2. * N + 1.) * (2. * N + 1.));
+  const double kpr = (4. / 3. > c.kappa / c.Pr) ? 4. / 3. : c.kappa / c.Pr;  // KAPPASPR_MAX_TIMESTEP_H
+  const double init[2] = {HUGE_VAL, HUGE_VAL};
+  CUDA_TRY(cudaMemcpyAsync(ctx->red.p, init, sizeof(init), cudaMemcpyHostToDevice, st), "reset dt");
+  CUDA_TRY(cudaMemsetAsync(ctx->bad.p, 0, sizeof(unsigned long long), st), "reset flag");
+  if (int rc = table_for(ctx->n)->cfl(ctx, d_U, cflS, dflS, kpr, st)) return rc;
+  double h[2];
+  unsigned long long bad = 0;
+  CUDA_TRY(cudaMemcpyAsync(h, ctx->red.p, sizeof(h), cudaMemcpyDeviceToHost, st), "read dt");
+  CUDA_TRY(cudaMemcpyAsync(&bad, ctx->bad.p, sizeof(bad), cudaMemcpyDeviceToHost, st), "read flag");
+  CUDA_TRY(cudaStreamSynchronize(st), "sync dt");
+  *dt_out = h[0] < h[1] ? h[0] : h[1];
+  if (bad) { set_error("state holds NaN/Inf or non-positive density/pressure"); return DG_ERR_NAN; }
+  return DG_OK;
+}
+
+int dg_check_state(dg_ctx* ctx, const double* d_U, long long* bad_count, void* stream) {
+  if (int rc = check_ctx(ctx, true)) return rc;
+  if (!d_U || !bad_count) { set_error("dg_check_state: null argument"); return DG_ERR_ARG; }
+  cudaStream_t st = (cudaStream_t)stream;
+  CUDA_TRY(cudaMemsetAsync(ctx->bad.p, 0, sizeof(unsigned long long), st), "reset flag");
+  const long long nNodes = (long long)ctx->nElems * ctx->n3;
+  int grid = (int)((nNodes + 255) / 256);
+  if (grid > 152 * 32) grid = 152 * 32;
+  gx::k_check<<<grid, 256, 0, st>>>(d_U, nNodes, ctx->cfg.kappa, ctx->bad.p);
+  ctx->launches++;
+  CUDA_TRY(cudaGetLastError(), "k_check launch");
+  unsigned long long bad = 0;
+  CUDA_TRY(cudaMemcpyAsync(&bad, ctx->bad.p, sizeof(bad), cudaMemcpyDeviceToHost, st), "read flag");
+  CUDA_TRY(cudaStreamSynchronize(st), "sync check");
+  *bad_count = (long long)bad;
+  return bad ? DG_ERR_NAN : DG_OK;
+}
+
+long long dg_kernel_launch_count(const dg_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,120 @@
+// Internal definition of the operator context, shared by the C-ABI translation unit and the
+// per-degree kernel translation units (dg_np*.cu, one per N+1 so they compile in parallel).
+#pragma once
+#include <cuda_runtime.h>
+#include <string>
+#include <vector>
+
+#include "../../include/galaexi_gb300.h"
+#include "dg_host.h"
+#include "dg_kernels.cuh"
+
+namespace gxc {
+
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  bool alloc(size_t cnt) {
+    release();
+    if (cnt == 0) return true;
+    if (cudaMalloc(&p, cnt * sizeof(T)) != cudaSuccess) { p = nullptr; return false; }
+    n = cnt;
+    return true;
+  }
+  void release() { if (p) cudaFree(p); p = nullptr; n = 0; }
+};
+
+// device data of one compute precision R
+template <typename R>
+struct PrecData {
+  DBuf<R> basis;  // D, DhatT, DVS (n^2 each), Lm, Lp, Lhm, Lhp (n each)
+  DBuf<R> Met, Fgeo, Pvol, Gvol, Uf, Pf, Gf, Flux;
+  void release() {
+    basis.release(); Met.release(); Fgeo.release(); Pvol.release(); Gvol.release();
+    Uf.release(); Pf.release(); Gf.release(); Flux.release();
+  }
+};
+
+template <typename R>
+inline gx::DevBasis<R> dev_basis(const PrecData<R>& P, int n) {
+  gx::DevBasis<R> b;
+  const R* base = P.basis.p;
+  b.D = base;
+  b.DhatT = base + n * n;
+  b.DVS = base + 2 * n * n;
+  b.Lm = base + 3 * n * n;
+  b.Lp = b.Lm + n;
+  b.Lhm = b.Lp + n;
+  b.Lhp = b.Lhm + n;
+  return b;
+}
+
+template <typename R>
+inline gx::Gas<R> make_gas(const dg_config& c) {
+  gx::Gas<R> g;
+  g.kappa = (R)c.kappa;
+  g.kappaM1 = (R)(c.kappa - 1.);
+  g.sKappaM1 = (R)(1. / (c.kappa - 1.));
+  g.R_gas = (R)c.R;
+  g.sR = (R)(1. / c.R);
+  g.mu = (R)c.mu0;
+  g.lambda = (R)(c.mu0 * c.R * c.kappa / ((c.kappa - 1.) * c.Pr));  // THERMAL_CONDUCTIVITY_EOS (eos.h:110)
+  return g;
+}
+
+}  // namespace gxc
+
+struct dg_ctx {
+  dg_config cfg;
+  int N = 0, n = 0, n2 = 0, n3 = 0;
+  int nElems = 0, nSides = 0;
+  gxh::Basis1D B;
+  gxc::PrecData<double> d;
+  gxc::PrecData<float> f;
+  gxc::DBuf<double> MetD;  // FP64 packed metrics [e][10][n3] for the CFL reduction
+  gxc::DBuf<int> E2S;      // [e][6][2]: 0-based side, flip
+  gxc::DBuf<double> red;   // dt reduction result (2)
+  gxc::DBuf<unsigned long long> bad;
+  long long launches = 0;
+  bool mesh_ok = false;
+};
+
+namespace gxc {
+
+inline gx::Launch make_launch(const dg_ctx* ctx) {
+  gx::Launch L;
+  L.nElems = ctx->nElems;
+  L.nSides = ctx->nSides;
+  L.gauss = ctx->cfg.node_type == DG_NODETYPE_GAUSS ? 1 : 0;
+  L.riemann = ctx->cfg.riemann;
+  L.split = ctx->cfg.split_dg;
+  L.parabolic = ctx->cfg.parabolic;
+  L.lift_mode = ctx->cfg.do_weak_lifting ? 2 : (ctx->cfg.do_conservative_lifting ? 1 : 0);
+  return L;
+}
+
+// entry points of one per-degree translation unit
+struct NPTable {
+  int (*configure_d)();
+  int (*configure_f)();
+  int (*rhs_d)(dg_ctx*, const double* U, gx::RKArgs rk, int rkmode, cudaStream_t st);
+  int (*rhs_f)(dg_ctx*, const double* U, gx::RKArgs rk, int rkmode, cudaStream_t st);
+  int (*cfl)(dg_ctx*, const double* U, double cflS, double dflS, double kpr, cudaStream_t st);
+  // one RK-mode stage with an event recorded after each kernel (ev[0..4]); lift may be skipped
+  int (*stage_events)(dg_ctx*, double* U, gx::RKArgs rk, cudaStream_t st, cudaEvent_t* ev);
+};
+
+}  // namespace gxc
+
+#define GX_DECLARE_NP(NPV) extern const gxc::NPTable gx_np_table_##NPV;
+GX_DECLARE_NP(2)
+GX_DECLARE_NP(3)
+GX_DECLARE_NP(4)
+GX_DECLARE_NP(5)
+GX_DECLARE_NP(6)
+GX_DECLARE_NP(7)
+GX_DECLARE_NP(8)
+GX_DECLARE_NP(9)
+GX_DECLARE_NP(10)
+#undef GX_DECLARE_NP

@@ -1,0 +1,606 @@
+// Host-side set-up of the DGSEM operator: 1D basis, ini keys, mesh and metrics, initial states.
+// These replace, for the periodic box meshes this library builds itself, the reference's
+// InitInterpolation/InitDGbasis (src/interpolation/interpolation.f90:96-193, src/dg/dg.f90:181-242),
+// HOPR mesh + ReadMesh + CalcMetrics (src/mesh/metrics.f90:171-789) and FillIni/ExactFunc
+// (src/dg/dg.f90:432-456, idealgas/exactfunc.f90, testcase/taylorgreenvortex/testcase.f90).
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/galaexi_gb300.h"
+#include "dg_host.h"
+
+namespace gxh {
+
+static const double kPi = 3.141592653589793238462643383279502884197;
+
+// ---------------------------------------------------------------------------------------------
+// 1D basis
+// ---------------------------------------------------------------------------------------------
+// Normalised Legendre polynomial L_N and derivative by the three-term recurrence
+// (the normalisation sqrt(N+1/2) is the one of basis.f90:232-233).
+static void legendre(int N, double x, double& L, double& dL) {
+  if (N == 0) { L = 1.; dL = 0.; }
+  else if (N == 1) { L = x; dL = 1.; }
+  else {
+    double lm2 = 1., lm1 = x, dlm1 = 1.;
+    for (int k = 2; k <= N; ++k) {
+      L = ((double)(2 * k - 1) * x * lm1 - (double)(k - 1) * lm2) / (double)k;
+      dL = k * lm1 + x * dlm1;
+      lm2 = lm1; lm1 = L; dlm1 = dL;
+    }
+  }
+  const double s = std::sqrt((double)N + 0.5);
+  L *= s; dL *= s;
+}
+
+// Gauss nodes: roots of L_{N+1} by Newton from Chebyshev-Gauss guesses (cf. basis.f90:417-486)
+static void gauss_nodes(int N, double* x, double* w) {
+  if (N == 0) { x[0] = 0.; w[0] = 2.; return; }
+  if (N == 1) { x[0] = -std::sqrt(1. / 3.); x[1] = -x[0]; w[0] = w[1] = 1.; return; }
+  const double h = 2. * std::atan(1.) / (double)(N + 1);
+  for (int i = 0; i <= (N + 1) / 2 - 1; ++i) {
+    double xi = -std::cos(h * (double)(2 * i + 1)), L, dL;
+    for (int it = 0; it <= 10; ++it) {
+      legendre(N + 1, xi, L, dL);
+      const double dx = -L / dL;
+      xi += dx;
+      if (std::fabs(dx) < 1.e-15 * std::fabs(xi)) break;
+    }
+    legendre(N + 1, xi, L, dL);
+    x[i] = xi; x[N - i] = -xi;
+    w[i] = w[N - i] = (2. * N + 3) / ((1. - xi * xi) * dL * dL);
+  }
+  if (N % 2 == 0) {
+    double L, dL;
+    x[N / 2] = 0.;
+    legendre(N + 1, 0., L, dL);
+    w[N / 2] = (2. * N + 3) / (dL * dL);
+  }
+}
+
+// q = L_{N+1} - L_{N-1} (unnormalised), its derivative, and L_N (cf. basis.f90:527-556)
+static void lobatto_q(int N, double x, double& q, double& dq, double& L) {
+  double lm2 = 1., lm1 = x;
+  L = x;
+  for (int k = 2; k <= N; ++k) {
+    L = ((double)(2 * k - 1) * x * lm1 - (double)(k - 1) * lm2) / (double)k;
+    lm2 = lm1; lm1 = L;
+  }
+  q = (double)(2 * N + 1) / (double)(N + 1) * (x * L - lm2);
+  dq = (double)(2 * N + 1) * L;
+}
+
+// Gauss-Lobatto nodes (cf. basis.f90:567-630)
+static void lobatto_nodes(int N, double* x, double* w) {
+  x[0] = -1.; x[N] = 1.;
+  const double w0 = 2. / (double)(N * (N + 1));
+  w[0] = w[N] = w0;
+  if (N > 1) {
+    const double c1 = kPi / (double)N, c2 = 3. / ((double)(8 * N) * kPi);
+    for (int i = 1; i <= (N + 1) / 2 - 1; ++i) {
+      double xi = -std::cos(c1 * ((double)i + 0.25) - c2 / ((double)i + 0.25)), q, dq, L;
+      for (int it = 0; it <= 10; ++it) {
+        lobatto_q(N, xi, q, dq, L);
+        const double dx = -q / dq;
+        xi += dx;
+        if (std::fabs(dx) < 1.e-15 * std::fabs(xi)) break;
+      }
+      lobatto_q(N, xi, q, dq, L);
+      x[i] = xi; x[N - i] = -xi;
+      w[i] = w[N - i] = w0 / (L * L);
+    }
+  }
+  if (N % 2 == 0) {
+    double q, dq, L;
+    x[N / 2] = 0.;
+    lobatto_q(N, 0., q, dq, L);
+    w[N / 2] = w0 / (L * L);
+  }
+}
+
+static void bary_weights(int N, const double* x, double* wb) {
+  for (int i = 0; i <= N; ++i) wb[i] = 1.;
+  for (int i = 1; i <= N; ++i)
+    for (int j = 0; j < i; ++j) {
+      wb[j] *= (x[j] - x[i]);
+      wb[i] *= (x[i] - x[j]);
+    }
+  for (int i = 0; i <= N; ++i) wb[i] = 1. / wb[i];
+}
+
+// D(i,l) = dl_l/dx(x_i), column-major, diagonal by negative row sum (cf. basis.f90:664-690)
+static void diff_matrix(int N, const double* x, double* D) {
+  const int n = N + 1;
+  std::vector<double> wb(n);
+  bary_weights(N, x, wb.data());
+  for (int t = 0; t < n * n; ++t) D[t] = 0.;
+  for (int l = 0; l <= N; ++l)
+    for (int i = 0; i <= N; ++i)
+      if (l != i) {
+        D[i + n * l] = wb[l] / (wb[i] * (x[i] - x[l]));
+        D[i + n * i] -= D[i + n * l];
+      }
+}
+
+// Lagrange polynomials at x0 in barycentric form (cf. basis.f90:720-752)
+static void lagrange_at(double x0, int N, const double* x, const double* wb, double* L) {
+  const double eps = 2.220446049250313e-16;
+  bool hit = false;
+  for (int i = 0; i <= N; ++i) {
+    L[i] = 0.;
+    const double d = std::fabs(x0 - x[i]);
+    const bool eq = (x0 == 0. || x[i] == 0.) ? d <= 2. * eps : (d <= eps * std::fabs(x0) && d <= eps * std::fabs(x[i]));
+    if (eq) { L[i] = 1.; hit = true; }
+  }
+  if (hit) return;
+  double s = 0.;
+  for (int i = 0; i <= N; ++i) { L[i] = wb[i] / (x0 - x[i]); s += L[i]; }
+  for (int i = 0; i <= N; ++i) L[i] /= s;
+}
+
+void basis_1d(int N, int node_type, Basis1D& B) {
+  const int n = N + 1;
+  B.N = N;
+  B.x.assign(n, 0.); B.w.assign(n, 0.); B.wb.assign(n, 0.);
+  if (node_type == DG_NODETYPE_GAUSS) gauss_nodes(N, B.x.data(), B.w.data());
+  else if (node_type == DG_NODETYPE_GAUSS_LOBATTO) lobatto_nodes(N, B.x.data(), B.w.data());
+  else {  // Chebyshev-Gauss-Lobatto (used for the metric computation)
+    for (int i = 0; i <= N; ++i) B.x[i] = -std::cos(i / (double)N * kPi);
+    for (int i = 0; i <= N; ++i) B.w[i] = kPi / (double)N;
+    B.w[0] *= 0.5; B.w[N] *= 0.5;
+  }
+  bary_weights(N, B.x.data(), B.wb.data());
+  B.D.assign(n * n, 0.);
+  diff_matrix(N, B.x.data(), B.D.data());
+  B.Lm.assign(n, 0.); B.Lp.assign(n, 0.);
+  lagrange_at(-1., N, B.x.data(), B.wb.data(), B.Lm.data());
+  lagrange_at(1., N, B.x.data(), B.wb.data(), B.Lp.data());
+  // D_hat = -M^{-1} D^T M with M = diag(w): D_hat(i,j) = -(1/w_i) * D(j,i) * w_j ; stored transposed
+  B.DhatT.assign(n * n, 0.);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) B.DhatT[j + n * i] = -((1. / B.w[i]) * (D_at(B, j, i) * B.w[j]));
+  // DVolSurf = D^T with the surface terms of the strong form folded into the corners (dg.f90:228-234)
+  B.DVS.assign(n * n, 0.);
+  for (int l = 0; l < n; ++l)
+    for (int i = 0; i < n; ++i) B.DVS[l + n * i] = D_at(B, i, l);
+  B.DVS[0] += 1.0 / (2.0 * B.w[0]);
+  B.DVS[N + n * N] -= 1.0 / (2.0 * B.w[N]);
+  B.Lhm.assign(n, 0.); B.Lhp.assign(n, 0.);
+  for (int i = 0; i < n; ++i) { B.Lhm[i] = (1. / B.w[i]) * B.Lm[i]; B.Lhp[i] = (1. / B.w[i]) * B.Lp[i]; }
+}
+
+// interpolation matrix V(i,j) = l_j(y_i) from nodes x (degree N) to points y (m+1 points)
+static void vandermonde(int N, const double* x, const double* wb, int M, const double* y, std::vector<double>& V) {
+  V.assign((size_t)(M + 1) * (N + 1), 0.);
+  std::vector<double> L(N + 1);
+  for (int i = 0; i <= M; ++i) {
+    lagrange_at(y[i], N, x, wb, L.data());
+    for (int j = 0; j <= N; ++j) V[i + (M + 1) * j] = L[j];
+  }
+}
+
+}  // namespace gxh
+
+using namespace gxh;
+
+// ---------------------------------------------------------------------------------------------
+// thread-local last error (shared with dg_api.cu)
+// ---------------------------------------------------------------------------------------------
+static thread_local std::string g_last_error;
+void gxh::set_error(const std::string& s) { g_last_error = s; }
+
+extern "C" const char* dg_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" void dg_config_default(dg_config* c) {
+  std::memset(c, 0, sizeof(*c));
+  c->N = 3;
+  c->node_type = DG_NODETYPE_GAUSS_LOBATTO;
+  c->parabolic = 0;
+  c->riemann = DG_RIEMANN_LF;
+  c->split_dg = DG_SPLIT_NONE;
+  c->lifting = DG_LIFTING_BR1;
+  c->do_weak_lifting = 0;
+  c->do_conservative_lifting = 0;
+  c->eta_br2 = 2.;
+  c->kappa = 1.4;       // idealgas/eos.f90:86
+  c->R = 287.058;       // idealgas/eos.f90:87
+  c->Pr = 0.72;         // idealgas/eos.f90:88
+  c->mu0 = 0.;          // idealgas/eos.f90:89
+  c->precision = DG_PRECISION_FP64;
+}
+
+static std::string lower(std::string s) {
+  for (auto& ch : s) ch = (char)std::tolower((unsigned char)ch);
+  return s;
+}
+static std::string trim(const std::string& s) {
+  size_t a = s.find_first_not_of(" \t\r"), b = s.find_last_not_of(" \t\r");
+  return a == std::string::npos ? std::string() : s.substr(a, b - a + 1);
+}
+static bool parse_bool(const std::string& v, int& out) {
+  std::string s = lower(v);
+  if (s == "t" || s == ".true." || s == "true" || s == "1" || s == "on") { out = 1; return true; }
+  if (s == "f" || s == ".false." || s == "false" || s == "0" || s == "off") { out = 0; return true; }
+  return false;
+}
+
+extern "C" int dg_config_from_ini(const char* text, dg_config* cfg) {
+  if (!text || !cfg) { set_error("dg_config_from_ini: null argument"); return DG_ERR_ARG; }
+  std::string all(text);
+  size_t pos = 0;
+  while (pos <= all.size()) {
+    size_t e = all.find('\n', pos);
+    if (e == std::string::npos) e = all.size();
+    std::string line = all.substr(pos, e - pos);
+    pos = e + 1;
+    size_t bang = line.find('!');
+    if (bang != std::string::npos) line = line.substr(0, bang);
+    size_t eq = line.find('=');
+    if (eq == std::string::npos) continue;
+    std::string key = lower(trim(line.substr(0, eq))), val = trim(line.substr(eq + 1));
+    std::string lv = lower(val);
+    try {
+      if (key == "n") cfg->N = std::stoi(val);
+      else if (key == "nodetype") {
+        if (lv == "gauss") cfg->node_type = DG_NODETYPE_GAUSS;
+        else if (lv == "gauss-lobatto") cfg->node_type = DG_NODETYPE_GAUSS_LOBATTO;
+        else { set_error("unknown NodeType " + val); return DG_ERR_ARG; }
+      } else if (key == "riemann") {
+        // string list of riemann.f90:130-144 (commented-out in GALAEXI, compile-time there)
+        static const char* names[] = {"lf", "roe", "roel2", "roeentropyfix", "hll", "hllc", "hlle", "hllem", "avg"};
+        int found = -1;
+        for (int i = 0; i < 9; ++i) if (lv == names[i]) found = i;
+        if (found < 0) { set_error("unknown Riemann " + val); return DG_ERR_ARG; }
+        cfg->riemann = found;
+      } else if (key == "splitdg") {
+        static const char* names[] = {"sd", "mo", "du", "kg", "pi"};
+        int found = -2;
+        if (lv == "none" || lv == "off" || lv == "weak") found = DG_SPLIT_NONE;
+        for (int i = 0; i < 5; ++i) if (lv == names[i]) found = i;
+        if (found < -1) { set_error("unknown SplitDG " + val); return DG_ERR_ARG; }
+        cfg->split_dg = found;
+      } else if (key == "lifting") {
+        if (lv == "br1") cfg->lifting = DG_LIFTING_BR1;
+        else if (lv == "br2") cfg->lifting = DG_LIFTING_BR2;
+        else { set_error("unknown Lifting " + val); return DG_ERR_ARG; }
+      } else if (key == "parabolic") {
+        int b; if (!parse_bool(val, b)) { set_error("bad Parabolic"); return DG_ERR_ARG; } cfg->parabolic = b;
+      } else if (key == "kappa") cfg->kappa = std::stod(val);
+      else if (key == "r") cfg->R = std::stod(val);
+      else if (key == "pr") cfg->Pr = std::stod(val);
+      else if (key == "mu0") cfg->mu0 = std::stod(val);
+      else if (key == "etabr2") cfg->eta_br2 = std::stod(val);
+      else if (key == "doweaklifting") {
+        int b; if (!parse_bool(val, b)) { set_error("bad doWeakLifting"); return DG_ERR_ARG; } cfg->do_weak_lifting = b;
+      } else if (key == "doconservativelifting") {
+        int b; if (!parse_bool(val, b)) { set_error("bad doConservativeLifting"); return DG_ERR_ARG; }
+        cfg->do_conservative_lifting = b;
+      } else if (key == "precision") {
+        if (lv == "fp64" || lv == "double") cfg->precision = DG_PRECISION_FP64;
+        else if (lv == "mixed") cfg->precision = DG_PRECISION_MIXED;
+        else { set_error("unknown Precision " + val); return DG_ERR_ARG; }
+      }
+    } catch (...) {
+      set_error("cannot parse value of " + key + ": " + val);
+      return DG_ERR_ARG;
+    }
+  }
+  return DG_OK;
+}
+
+extern "C" int dg_basis(int N, int node_type, double* xGP, double* wGP, double* wBary, double* L_minus,
+                        double* L_plus, double* D, double* D_hat_T, double* L_hat_minus, double* L_hat_plus,
+                        double* DVolSurf) {
+  if (N < 1 || N > 16 || (node_type != DG_NODETYPE_GAUSS && node_type != DG_NODETYPE_GAUSS_LOBATTO)) {
+    set_error("dg_basis: bad N or node type");
+    return DG_ERR_ARG;
+  }
+  Basis1D B;
+  basis_1d(N, node_type, B);
+  auto cp = [](double* d, const std::vector<double>& s) { if (d) std::memcpy(d, s.data(), s.size() * sizeof(double)); };
+  cp(xGP, B.x); cp(wGP, B.w); cp(wBary, B.wb); cp(L_minus, B.Lm); cp(L_plus, B.Lp); cp(D, B.D);
+  cp(D_hat_T, B.DhatT); cp(L_hat_minus, B.Lhm); cp(L_hat_plus, B.Lhp); cp(DVolSurf, B.DVS);
+  return DG_OK;
+}
+
+extern "C" int dg_mesh_cartesian_sizes(int nx, int ny, int nz, int* nElems, int* nSides) {
+  if (nx < 1 || ny < 1 || nz < 1) { set_error("mesh: bad element counts"); return DG_ERR_ARG; }
+  long long ne = (long long)nx * ny * nz;
+  if (ne * 3 > 0x7fffffffLL) { set_error("mesh: too many elements"); return DG_ERR_ARG; }
+  if (nElems) *nElems = (int)ne;
+  if (nSides) *nSides = (int)(3 * ne);
+  return DG_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Periodic box.  Local side numbering and orientation follow src/flexi.h:98-103 and
+// src/mesh/mappings.f90; each element is master (flip 0) of its XI_PLUS, ETA_PLUS and
+// ZETA_PLUS sides, and its neighbour's XI_MINUS, ETA_MINUS, ZETA_MINUS sides are the slaves.
+// The slave flips (1 for xi/zeta sides, 2 for eta sides) are the ones for which
+// SideToVol2(p,q,flip,slave side) lands on the same physical point as the master's (p,q).
+// ---------------------------------------------------------------------------------------------
+namespace {
+enum { ZETA_MINUS = 1, ETA_MINUS = 2, XI_PLUS = 3, ETA_PLUS = 4, XI_MINUS = 5, ZETA_PLUS = 6 };
+const int NormalDirs[7] = {0, 3, 2, 1, 2, 1, 3};            // mesh_vars.f90:112 (1-based locSide)
+const int TangDirs[7] = {0, 1, 3, 2, 3, 2, 1};              // mesh_vars.f90:114
+const double NormalSigns[7] = {0, -1., -1., 1., 1., -1., 1.}; // mesh_vars.f90:118
+
+struct Mapping {
+  double x0[3], L[3], amp;
+  int nel[3];
+  void operator()(int e3[3], const double xi[3], double X[3]) const {
+    for (int d = 0; d < 3; ++d) X[d] = x0[d] + ((double)e3[d] + 0.5 * (xi[d] + 1.)) * (L[d] / nel[d]);
+    if (amp != 0.) {
+      const double s = std::sin(2. * kPi * (X[0] - x0[0]) / L[0]) * std::sin(2. * kPi * (X[1] - x0[1]) / L[1]) *
+                       std::sin(2. * kPi * (X[2] - x0[2]) / L[2]);
+      for (int d = 0; d < 3; ++d) X[d] += amp * s;
+    }
+  }
+};
+
+inline size_t vidx(int n, int i, int j, int k, int e) { return (size_t)i + n * (j + n * (k + (size_t)n * e)); }
+}  // namespace
+
+extern "C" int dg_mesh_cartesian(int N, int node_type, int nx, int ny, int nz, const double* x0, const double* x1,
+                                 double deform_amp, double* elem_xgp, double* Mf, double* Mg, double* Mh, double* sJ,
+                                 double* nvec, double* t1vec, double* t2vec, double* surfelem, int* E2S, int* S2E) {
+  int nElems, nSides;
+  if (dg_mesh_cartesian_sizes(nx, ny, nz, &nElems, &nSides) != DG_OK) return DG_ERR_ARG;
+  if (N < 1 || N > DG_MAX_N) { set_error("mesh: N out of range"); return DG_ERR_ARG; }
+  const int n = N + 1, n2 = n * n;
+  Basis1D B;
+  basis_1d(N, node_type, B);
+  Mapping map;
+  for (int d = 0; d < 3; ++d) { map.x0[d] = x0[d]; map.L[d] = x1[d] - x0[d]; }
+  map.nel[0] = nx; map.nel[1] = ny; map.nel[2] = nz;
+  map.amp = deform_amp;
+  auto eid = [&](int ix, int iy, int iz) {
+    ix = (ix + nx) % nx; iy = (iy + ny) % ny; iz = (iz + nz) % nz;
+    return ix + nx * (iy + ny * iz);
+  };
+  // connectivity (1-based IDs as in the reference's ElemToSide / SideToElem)
+  for (int iz = 0; iz < nz; ++iz)
+    for (int iy = 0; iy < ny; ++iy)
+      for (int ix = 0; ix < nx; ++ix) {
+        const int e = eid(ix, iy, iz);
+        const int sx = 3 * e, sy = 3 * e + 1, sz = 3 * e + 2;
+        const int mx = eid(ix - 1, iy, iz), my = eid(ix, iy - 1, iz), mz = eid(ix, iy, iz - 1);
+        auto set = [&](int loc, int side0, int flip, int master) {
+          int* p = E2S + 3 * ((loc - 1) + 6 * (size_t)e);
+          p[0] = side0 + 1; p[1] = flip; p[2] = master;
+        };
+        set(XI_PLUS, sx, 0, 1); set(ETA_PLUS, sy, 0, 1); set(ZETA_PLUS, sz, 0, 1);
+        set(XI_MINUS, 3 * mx, 1, 0); set(ETA_MINUS, 3 * my + 1, 2, 0); set(ZETA_MINUS, 3 * mz + 2, 1, 0);
+      }
+  for (int iz = 0; iz < nz; ++iz)
+    for (int iy = 0; iy < ny; ++iy)
+      for (int ix = 0; ix < nx; ++ix) {
+        const int e = eid(ix, iy, iz);
+        const int nb[3] = {eid(ix + 1, iy, iz), eid(ix, iy + 1, iz), eid(ix, iy, iz + 1)};
+        const int mloc[3] = {XI_PLUS, ETA_PLUS, ZETA_PLUS}, sloc[3] = {XI_MINUS, ETA_MINUS, ZETA_MINUS};
+        const int flips[3] = {1, 2, 1};
+        for (int d = 0; d < 3; ++d) {
+          int* p = S2E + 5 * (size_t)(3 * e + d);
+          p[0] = e + 1; p[1] = nb[d] + 1; p[2] = mloc[d]; p[3] = sloc[d]; p[4] = flips[d];
+        }
+      }
+  // node coordinates
+  for (int e = 0; e < nElems; ++e) {
+    int e3[3] = {e % nx, (e / nx) % ny, e / (nx * ny)};
+    for (int k = 0; k <= N; ++k)
+      for (int j = 0; j <= N; ++j)
+        for (int i = 0; i <= N; ++i) {
+          const double xi[3] = {B.x[i], B.x[j], B.x[k]};
+          double X[3];
+          map(e3, xi, X);
+          if (elem_xgp)
+            for (int d = 0; d < 3; ++d) elem_xgp[d + 3 * vidx(n, i, j, k, e)] = X[d];
+        }
+  }
+  // volume metrics Ja^1 = Mf, Ja^2 = Mg, Ja^3 = Mh (Ja(nn,dd) = J a^nn_dd) and sJ
+  // face metrics (nn,dd) at every face node, indexed [e][loc][a][b] in volume face coordinates
+  std::vector<double> JaFace((size_t)nElems * 6 * n2 * 9, 0.);
+  if (deform_amp == 0.) {
+    const double h[3] = {map.L[0] / nx, map.L[1] / ny, map.L[2] / nz};
+    const double Ja[3] = {0.25 * h[1] * h[2], 0.25 * h[0] * h[2], 0.25 * h[0] * h[1]};
+    const double s = 8. / (h[0] * h[1] * h[2]);
+    for (size_t t = 0; t < (size_t)nElems * n * n2; ++t) {
+      for (int d = 0; d < 3; ++d) {
+        Mf[d + 3 * t] = d == 0 ? Ja[0] : 0.;
+        Mg[d + 3 * t] = d == 1 ? Ja[1] : 0.;
+        Mh[d + 3 * t] = d == 2 ? Ja[2] : 0.;
+      }
+      sJ[t] = s;
+    }
+    for (size_t t = 0; t < (size_t)nElems * 6 * n2; ++t)
+      for (int nn = 0; nn < 3; ++nn)
+        for (int dd = 0; dd < 3; ++dd) JaFace[t * 9 + nn * 3 + dd] = (nn == dd) ? Ja[nn] : 0.;
+  } else {
+    // Curved: conservative curl form of the metric terms on Chebyshev-Gauss-Lobatto points of
+    // degree N (metrics.f90:451-485), then interpolation to the solution nodes (metrics.f90:497-507).
+    Basis1D C;
+    basis_1d(N, 99, C);  // Chebyshev-Gauss-Lobatto
+    std::vector<double> Vcl;  // CL -> solution nodes
+    vandermonde(N, C.x.data(), C.wb.data(), N, B.x.data(), Vcl);
+    std::vector<double> X((size_t)3 * n * n2), dX((size_t)9 * n * n2), Rcl((size_t)9 * n * n2), Ja((size_t)9 * n * n2);
+    std::vector<double> JaN((size_t)9 * n * n2), dXN((size_t)9 * n * n2), tmp((size_t)9 * n * n2);
+    auto I3 = [&](int i, int j, int k) { return (size_t)i + n * (j + (size_t)n * k); };
+    // interpolate a 9-component CL field to the solution nodes (tensor product)
+    auto to_nodes = [&](const std::vector<double>& src, std::vector<double>& dst) {
+      std::vector<double> a(src.size()), b(src.size());
+      for (int c = 0; c < 9; ++c)
+        for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
+          double s = 0.; for (int l = 0; l < n; ++l) s += Vcl[i + n * l] * src[c + 9 * I3(l, j, k)]; a[c + 9 * I3(i, j, k)] = s;
+        }
+      for (int c = 0; c < 9; ++c)
+        for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
+          double s = 0.; for (int l = 0; l < n; ++l) s += Vcl[j + n * l] * a[c + 9 * I3(i, l, k)]; b[c + 9 * I3(i, j, k)] = s;
+        }
+      for (int c = 0; c < 9; ++c)
+        for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
+          double s = 0.; for (int l = 0; l < n; ++l) s += Vcl[k + n * l] * b[c + 9 * I3(i, j, l)]; dst[c + 9 * I3(i, j, k)] = s;
+        }
+    };
+    for (int e = 0; e < nElems; ++e) {
+      int e3[3] = {e % nx, (e / nx) % ny, e / (nx * ny)};
+      for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
+        const double xi[3] = {C.x[i], C.x[j], C.x[k]};
+        map(e3, xi, &X[3 * I3(i, j, k)]);
+      }
+      // dX(dd, nn) = d X_nn / d xi_dd
+      for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
+        double* d = &dX[9 * I3(i, j, k)];
+        for (int t = 0; t < 9; ++t) d[t] = 0.;
+        for (int l = 0; l < n; ++l)
+          for (int nn = 0; nn < 3; ++nn) {
+            d[0 * 3 + nn] += C.D[i + n * l] * X[nn + 3 * I3(l, j, k)];
+            d[1 * 3 + nn] += C.D[j + n * l] * X[nn + 3 * I3(i, l, k)];
+            d[2 * 3 + nn] += C.D[k + n * l] * X[nn + 3 * I3(i, j, l)];
+          }
+      }
+      // R(dd, nn) = 1/2 (X_{nn+2} dX_{nn+1}/dxi_dd - X_{nn+1} dX_{nn+2}/dxi_dd)
+      for (size_t t = 0; t < (size_t)n * n2; ++t)
+        for (int dd = 0; dd < 3; ++dd)
+          for (int nn = 0; nn < 3; ++nn) {
+            const int n1 = (nn + 1) % 3, n2_ = (nn + 2) % 3;
+            Rcl[t * 9 + dd * 3 + nn] = 0.5 * (X[n2_ + 3 * t] * dX[t * 9 + dd * 3 + n1] - X[n1 + 3 * t] * dX[t * 9 + dd * 3 + n2_]);
+          }
+      // Ja(dd, nn) = -(d/dxi_{dd+1} R(dd+2, nn) - d/dxi_{dd+2} R(dd+1, nn))
+      for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
+        double* J = &Ja[9 * I3(i, j, k)];
+        for (int t = 0; t < 9; ++t) J[t] = 0.;
+        for (int q = 0; q < n; ++q)
+          for (int nn = 0; nn < 3; ++nn) {
+            J[0 * 3 + nn] += -C.D[j + n * q] * Rcl[9 * I3(i, q, k) + 2 * 3 + nn] + C.D[k + n * q] * Rcl[9 * I3(i, j, q) + 1 * 3 + nn];
+            J[1 * 3 + nn] += -C.D[k + n * q] * Rcl[9 * I3(i, j, q) + 0 * 3 + nn] + C.D[i + n * q] * Rcl[9 * I3(q, j, k) + 2 * 3 + nn];
+            J[2 * 3 + nn] += -C.D[i + n * q] * Rcl[9 * I3(q, j, k) + 1 * 3 + nn] + C.D[j + n * q] * Rcl[9 * I3(i, q, k) + 0 * 3 + nn];
+          }
+      }
+      to_nodes(Ja, JaN);
+      to_nodes(dX, dXN);
+      for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
+        const size_t t = I3(i, j, k), g = vidx(n, i, j, k, e);
+        const double* J = &JaN[9 * t];
+        for (int d = 0; d < 3; ++d) { Mf[d + 3 * g] = J[0 * 3 + d]; Mg[d + 3 * g] = J[1 * 3 + d]; Mh[d + 3 * g] = J[2 * 3 + d]; }
+        const double* a = &dXN[9 * t];
+        const double det = a[0] * (a[4] * a[8] - a[5] * a[7]) - a[1] * (a[3] * a[8] - a[5] * a[6]) +
+                           a[2] * (a[3] * a[7] - a[4] * a[6]);
+        sJ[g] = 1. / det;
+      }
+      // face metrics: JaCL on the face planes (xi = -+1 are CL end points), interpolated in 2D
+      for (int loc = 1; loc <= 6; ++loc)
+        for (int b = 0; b < n; ++b)
+          for (int a = 0; a < n; ++a) {
+            double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+            for (int qb = 0; qb < n; ++qb)
+              for (int qa = 0; qa < n; ++qa) {
+                size_t src;
+                const int pl = (loc == XI_MINUS || loc == ETA_MINUS || loc == ZETA_MINUS) ? 0 : N;
+                if (loc == XI_MINUS || loc == XI_PLUS) src = I3(pl, qa, qb);
+                else if (loc == ETA_MINUS || loc == ETA_PLUS) src = I3(qa, pl, qb);
+                else src = I3(qa, qb, pl);
+                const double wgt = Vcl[a + n * qa] * Vcl[b + n * qb];
+                for (int c = 0; c < 9; ++c) acc[c] += wgt * Ja[9 * src + c];
+              }
+            for (int c = 0; c < 9; ++c) JaFace[(((size_t)e * 6 + (loc - 1)) * n2 + a + n * b) * 9 + c] = acc[c];
+          }
+    }
+  }
+  // SurfMetricsFromJa (metrics.f90:752-789) on master sides; master side node (p,q) sits at the
+  // volume face coordinates SideToVol2(p,q,0,loc) (CGNS_SideToVol2, mappings.f90:376-409).
+  for (int e = 0; e < nElems; ++e) {
+    const int locs[3] = {XI_PLUS, ETA_PLUS, ZETA_PLUS};
+    for (int d = 0; d < 3; ++d) {
+      const int loc = locs[d];
+      const int side = 3 * e + d;
+      const int nd = NormalDirs[loc] - 1, td = TangDirs[loc] - 1;
+      const double sgn = NormalSigns[loc];
+      for (int q = 0; q <= N; ++q)
+        for (int p = 0; p <= N; ++p) {
+          int a = p, b = q;
+          if (loc == ETA_PLUS) a = N - p;  // CGNS_SideToVol2 for the three plus sides
+          const double* J = &JaFace[(((size_t)e * 6 + (loc - 1)) * n2 + a + n * b) * 9];
+          const size_t f = (size_t)p + n * (q + (size_t)n * side);
+          double se = std::sqrt(J[nd * 3 + 0] * J[nd * 3 + 0] + J[nd * 3 + 1] * J[nd * 3 + 1] + J[nd * 3 + 2] * J[nd * 3 + 2]);
+          double nv[3], t1[3], t2[3];
+          for (int c = 0; c < 3; ++c) nv[c] = sgn * J[nd * 3 + c] / se;
+          const double dot = J[td * 3 + 0] * nv[0] + J[td * 3 + 1] * nv[1] + J[td * 3 + 2] * nv[2];
+          for (int c = 0; c < 3; ++c) t1[c] = J[td * 3 + c] - dot * nv[c];
+          const double tn = std::sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
+          for (int c = 0; c < 3; ++c) t1[c] = t1[c] / tn;
+          t2[0] = nv[1] * t1[2] - nv[2] * t1[1];
+          t2[1] = nv[2] * t1[0] - nv[0] * t1[2];
+          t2[2] = nv[0] * t1[1] - nv[1] * t1[0];
+          surfelem[f] = se;
+          for (int c = 0; c < 3; ++c) { nvec[c + 3 * f] = nv[c]; t1vec[c + 3 * f] = t1[c]; t2vec[c + 3 * f] = t2[c]; }
+        }
+    }
+  }
+  return DG_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Initial states
+// ---------------------------------------------------------------------------------------------
+static void prim_to_cons(const double prim[5], double kappa, double* cons) {
+  // PrimToCons (idealgas/eos.f90:467-489)
+  cons[0] = prim[0];
+  cons[1] = prim[1] * prim[0];
+  cons[2] = prim[2] * prim[0];
+  cons[3] = prim[3] * prim[0];
+  cons[4] = prim[4] / (kappa - 1.) + 0.5 * (cons[1] * prim[1] + cons[2] * prim[2] + cons[3] * prim[3]);
+}
+
+extern "C" int dg_fill_ini(int exactfunc, const double* prm, int nprm, long long nNodes, const double* xgp, double kappa,
+                           double R, double t, double* U) {
+  if (!xgp || !U || nNodes < 0) { set_error("dg_fill_ini: null argument"); return DG_ERR_ARG; }
+  for (long long m = 0; m < nNodes; ++m) {
+    const double* x = xgp + 3 * m;
+    double prim[5];
+    if (exactfunc == DG_EXACTFUNC_CONST) {
+      if (nprm < 5) { set_error("dg_fill_ini: constant state needs 5 parameters"); return DG_ERR_ARG; }
+      for (int c = 0; c < 5; ++c) prim[c] = prm[c];
+    } else if (exactfunc == DG_EXACTFUNC_SHU_VORTEX) {
+      // exactfunc.f90:482-502: RefState(5), IniCenter(3), IniAxis(3), IniAmplitude, IniHalfwidth
+      if (nprm < 13) { set_error("dg_fill_ini: Shu vortex needs 13 parameters"); return DG_ERR_ARG; }
+      for (int c = 0; c < 5; ++c) prim[c] = prm[c];
+      const double vel[3] = {prm[1], prm[2], prm[3]};
+      const double RT = prim[4] / prim[0];
+      double cent[3];
+      for (int d = 0; d < 3; ++d) cent[d] = x[d] - (prm[5 + d] + vel[d] * t);
+      const double* ax = prm + 8;
+      double cr[3] = {ax[1] * cent[2] - ax[2] * cent[1], ax[2] * cent[0] - ax[0] * cent[2], ax[0] * cent[1] - ax[1] * cent[0]};
+      for (int d = 0; d < 3; ++d) cr[d] = cr[d] / prm[12];
+      const double r2 = cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2];
+      const double du = prm[11] / (2. * kPi) * std::exp(0.5 * (1. - r2));
+      const double km1 = kappa - 1.;
+      const double dTemp = -km1 / (2. * kappa * RT) * du * du;
+      prim[0] = prim[0] * std::pow(1. + dTemp, 1. * (1. / km1));
+      for (int d = 0; d < 3; ++d) prim[1 + d] = prim[1 + d] + du * cr[d];
+      prim[4] = prim[4] * std::pow(1. + dTemp, kappa / km1);
+    } else if (exactfunc == DG_EXACTFUNC_TGV) {
+      // testcase/taylorgreenvortex/testcase.f90:145-149, 241-256: rho0, U0, Ma0, IniConstDens
+      if (nprm < 4) { set_error("dg_fill_ini: TGV needs 4 parameters"); return DG_ERR_ARG; }
+      const double rho0 = prm[0], U0 = prm[1], Ma0 = prm[2];
+      const double p0 = (U0 / Ma0) * (U0 / Ma0) / kappa * rho0;
+      const double T0 = p0 / (rho0 * R);
+      prim[1] = U0 * std::sin(x[0]) * std::cos(x[1]) * std::cos(x[2]);
+      prim[2] = -U0 * std::cos(x[0]) * std::sin(x[1]) * std::cos(x[2]);
+      prim[3] = 0.;
+      prim[4] = p0 + (rho0 * U0 * U0) / 16. *
+                         (std::cos(2 * x[0]) * std::cos(2. * x[2]) + 2. * std::cos(2. * x[1]) + 2. * std::cos(2. * x[0]) +
+                          std::cos(2 * x[1]) * std::cos(2. * x[2]));
+      if (prm[3] != 0.) prim[0] = rho0;
+      else prim[0] = prim[4] / (T0 * R);
+    } else {
+      set_error("dg_fill_ini: unknown exact function");
+      return DG_ERR_ARG;
+    }
+    prim_to_cons(prim, kappa, U + 5 * m);
+  }
+  return DG_OK;
+}

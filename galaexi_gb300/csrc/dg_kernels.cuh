@@ -1,0 +1,674 @@
+// Fused DGSEM kernels for sm_103a.
+//
+// One RHS evaluation (DGTimeDerivative_weakForm, src/dg/dg.f90:255-425) runs as four launches:
+//   k_prolong  element-per-block   ConsToPrim (volume) + ProlongToFace + ConsToPrim (faces)
+//   k_lift     element-per-block   BR1 lifting: volume part, surface part, Jacobian, gradient traces
+//   k_face     thread-per-face-node Riemann solver + BR1 viscous flux + SurfElem
+//   k_volume   element-per-block   volume integral (weak or split form, viscous part), surface
+//                                  integral, sign, Jacobian, and optionally the LSERK-W2 stage update
+// (k_lift is skipped for the Euler equations.)  The reference runs ~25-35 launches per stage with
+// full-size intermediates; here the element's state lives in shared memory inside each phase.
+//
+// Layouts (internal, all per element contiguous so that element blocks load coalesced):
+//   Pvol [e][7][n^3]     rho,u,v,w,p,T,1/rho                 (compute type R)
+//   Gvol [e][15][n^3]    d/dx (rho,u,v,w,T), d/dy (..), d/dz (..)
+//   Met  [e][10][n^3]    Mf(3), Mg(3), Mh(3), sJ
+//   Uf   [slot][side][5][n^2], Pf [slot][side][6][n^2], Gf [slot][side][15][n^2]  (slot 0 master, 1 slave)
+//   Fgeo [side][10][n^2] nv(3), t1(3), t2(3), SurfElem
+//   Flux [side][5][n^2]
+// The caller's U / Ut / Ut_tmp keep the reference layout (5,0:N,0:N,0:N,nElems), FP64.
+#pragma once
+#include "dg_physics.cuh"
+
+namespace gx {
+
+enum { L_ZETA_MINUS = 1, L_ETA_MINUS = 2, L_XI_PLUS = 3, L_ETA_PLUS = 4, L_XI_MINUS = 5, L_ZETA_PLUS = 6 };
+
+// Side <-> volume index maps of src/mesh/mappings.f90 (CGNS_SideToVol2 after Flip_M2S), computed
+// arithmetically instead of read from the S2V2 table.  Both factors are involutions.
+__device__ __forceinline__ void flip_map(int N, int p, int q, int flip, int& a, int& b) {
+  switch (flip) {
+    case 0: a = p; b = q; break;
+    case 1: a = q; b = p; break;
+    case 2: a = N - p; b = q; break;
+    case 3: a = N - q; b = N - p; break;
+    default: a = p; b = N - q; break;
+  }
+}
+__device__ __forceinline__ void cgns_map(int N, int p, int q, int ls, int& a, int& b) {
+  switch (ls) {
+    case L_XI_MINUS: case L_ZETA_MINUS: a = q; b = p; break;
+    case L_ETA_PLUS: a = N - p; b = q; break;
+    default: a = p; b = q; break;
+  }
+}
+// S2V2(p,q,flip,ls): side node (master frame) -> volume face coordinates (a,b)
+__device__ __forceinline__ void s2v2(int N, int p, int q, int flip, int ls, int& a, int& b) {
+  int pp, qq;
+  flip_map(N, p, q, flip, pp, qq);
+  cgns_map(N, pp, qq, ls, a, b);
+}
+// inverse: volume face coordinates (a,b) -> side node (p,q)
+__device__ __forceinline__ void s2v2_inv(int N, int a, int b, int flip, int ls, int& p, int& q) {
+  int pp, qq;
+  cgns_map(N, a, b, ls, pp, qq);
+  flip_map(N, pp, qq, flip, p, q);
+}
+// volume node of face coordinates (a,b) at line position l for local side ls
+__device__ __forceinline__ int face_node(int n, int ls, int a, int b, int l) {
+  switch (ls) {
+    case L_XI_MINUS: case L_XI_PLUS: return l + n * (a + n * b);
+    case L_ETA_MINUS: case L_ETA_PLUS: return a + n * (l + n * b);
+    default: return a + n * (b + n * l);
+  }
+}
+__device__ __forceinline__ bool is_minus(int ls) { return ls == L_XI_MINUS || ls == L_ETA_MINUS || ls == L_ZETA_MINUS; }
+
+template <typename R>
+struct DevBasis {
+  const R* D;          // D(i,l), column-major (0:N,0:N)
+  const R* DhatT;      // D_hat^T(l,i)
+  const R* DVS;        // DVolSurf(l,i)
+  const R* Lm;         // L_minus(0:N)
+  const R* Lp;         // L_plus(0:N)
+  const R* Lhm;        // L_hat_minus(0:N)
+  const R* Lhp;        // L_hat_plus(0:N)
+};
+
+// shared copy of the 1D operators (n^2 entries each)
+template <int NP, typename R>
+struct SBasis {
+  R D[NP * NP], DhatT[NP * NP], DVS[NP * NP], Lm[NP], Lp[NP], Lhm[NP], Lhp[NP];
+};
+template <int NP, typename R>
+__device__ __forceinline__ void load_basis(SBasis<NP, R>& s, const DevBasis<R>& b) {
+  for (int t = threadIdx.x; t < NP * NP; t += blockDim.x) {
+    s.D[t] = b.D[t]; s.DhatT[t] = b.DhatT[t]; s.DVS[t] = b.DVS[t];
+  }
+  for (int t = threadIdx.x; t < NP; t += blockDim.x) {
+    s.Lm[t] = b.Lm[t]; s.Lp[t] = b.Lp[t]; s.Lhm[t] = b.Lhm[t]; s.Lhp[t] = b.Lhp[t];
+  }
+}
+
+struct Launch {
+  int nElems, nSides;
+  int gauss;        // 1: Gauss nodes (prolongation by interpolation), 0: Gauss-Lobatto
+  int riemann, split, parabolic;
+  int lift_mode;    // 0: strong non-conservative, 1: strong conservative, 2: weak
+};
+
+template <int NP> struct EPBof { static constexpr int v = (NP * NP * NP >= 128) ? 1 : (256 / (NP * NP * NP)); };
+
+// =====================================================================================
+// k_prolong: ConsToPrim_Volume + ProlongToFace_CUDA + GetPrimitiveStateSurface
+// =====================================================================================
+template <int NP, typename R>
+__global__ void __launch_bounds__(EPBof<NP>::v * NP * NP * NP)
+k_prolong(const double* __restrict__ U, const int* __restrict__ E2S, DevBasis<R> basis, Gas<R> gas, Launch L,
+          R* __restrict__ Pvol, R* __restrict__ Uf, R* __restrict__ Pf) {
+  constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, EPB = EPBof<NP>::v, N = NP - 1;
+  __shared__ SBasis<NP, R> sb;
+  __shared__ R Us[EPB][5][n3];
+  load_basis(sb, basis);
+  const int e0 = blockIdx.x * EPB;
+  const int nloc = min(EPB, L.nElems - e0);
+  // coalesced load of the element block (AoS (5,n^3) per element in global memory)
+  const double* Ub = U + (size_t)e0 * 5 * n3;
+  for (int t = threadIdx.x; t < nloc * 5 * n3; t += blockDim.x) {
+    int el = t / (5 * n3), r = t - el * 5 * n3;
+    Us[el][r % 5][r / 5] = (R)Ub[t];
+  }
+  __syncthreads();
+  // volume prims
+  for (int t = threadIdx.x; t < nloc * n3; t += blockDim.x) {
+    int el = t / n3, node = t - el * n3;
+    R u[5] = {Us[el][0][node], Us[el][1][node], Us[el][2][node], Us[el][3][node], Us[el][4][node]};
+    R prim[6], srho;
+    cons_to_prim(u, gas, prim, srho);
+    R* P = Pvol + (size_t)(e0 + el) * 7 * n3 + node;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) P[c * n3] = prim[c];
+    P[6 * n3] = srho;
+  }
+  // face traces
+  for (int t = threadIdx.x; t < nloc * 6 * n2; t += blockDim.x) {
+    int el = t / (6 * n2), r = t - el * 6 * n2;
+    int ls = r / n2 + 1, pq = r - (ls - 1) * n2;
+    int p = pq % n, q = pq / n;
+    int e = e0 + el;
+    int side = E2S[(e * 6 + ls - 1) * 2 + 0];
+    int flip = E2S[(e * 6 + ls - 1) * 2 + 1];
+    int a, b;
+    s2v2(N, p, q, flip, ls, a, b);
+    R u[5];
+    if (!L.gauss) {
+      int node = face_node(n, ls, a, b, is_minus(ls) ? 0 : N);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) u[v] = Us[el][v][node];
+    } else {
+      const R* Lv = is_minus(ls) ? sb.Lm : sb.Lp;
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        R s = Us[el][v][face_node(n, ls, a, b, 0)] * Lv[0];
+#pragma unroll
+        for (int l = 1; l < n; ++l) s = s + Us[el][v][face_node(n, ls, a, b, l)] * Lv[l];
+        u[v] = s;
+      }
+    }
+    R prim[6], srho;
+    cons_to_prim(u, gas, prim, srho);
+    const int slot = (flip == 0) ? 0 : 1;
+    R* uf = Uf + ((size_t)slot * L.nSides + side) * 5 * n2 + pq;
+    R* pf = Pf + ((size_t)slot * L.nSides + side) * 6 * n2 + pq;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) uf[v * n2] = u[v];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) pf[c * n2] = prim[c];
+  }
+}
+
+// =====================================================================================
+// k_lift: Lifting_BR1 (lifting_br1.t90:47-167): volume part + surface part + sJ, then
+// ProlongToFaceLifting.  Lifted variables (rho,u,v,w,T) = PRIM_LIFT (eos.h:143).
+// =====================================================================================
+template <int NP, typename R>
+__global__ void __launch_bounds__(EPBof<NP>::v * NP * NP * NP)
+k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restrict__ Pf, const R* __restrict__ Fgeo,
+       const int* __restrict__ E2S, DevBasis<R> basis, Launch L, R* __restrict__ Gvol, R* __restrict__ Gf) {
+  constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, EPB = EPBof<NP>::v, N = NP - 1;
+  __shared__ SBasis<NP, R> sb;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R (*Ps)[5][n3] = reinterpret_cast<R (*)[5][n3]>(smem_raw);                                   // [EPB][5][n3]
+  R (*Gs)[15][n3] = reinterpret_cast<R (*)[15][n3]>(smem_raw + sizeof(R) * (size_t)EPB * 5 * n3); // [EPB][15][n3]
+  load_basis(sb, basis);
+  const int e0 = blockIdx.x * EPB;
+  const int nloc = min(EPB, L.nElems - e0);
+  const int liftc[5] = {0, 1, 2, 3, 5};
+  for (int t = threadIdx.x; t < nloc * 5 * n3; t += blockDim.x) {
+    int el = t / (5 * n3), r = t - el * 5 * n3;
+    int c = r / n3, node = r - c * n3;
+    Ps[el][c][node] = Pvol[(size_t)(e0 + el) * 7 * n3 + liftc[c] * n3 + node];
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nloc * n3; t += blockDim.x) {
+    const int el = t / n3, node = t - el * n3;
+    const int e = e0 + el;
+    const int i = node % n, j = (node / n) % n, k = node / n2;
+    const R* M = Met + (size_t)e * 10 * n3 + node;
+    R g[3][5];
+    if (L.lift_mode == 0) {
+      // Lifting_VolInt_Nonconservative_GPU_Kernel (lifting_volint.t90:262-328)
+      R gxi[5], geta[5], gzeta[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) { gxi[v] = R(0); geta[v] = R(0); gzeta[v] = R(0); }
+#pragma unroll
+      for (int l = 0; l < n; ++l) {
+        const R dxi = sb.D[i + n * l], deta = sb.D[j + n * l], dzeta = sb.D[k + n * l];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+          gxi[v] = gxi[v] + dxi * Ps[el][v][l + n * (j + n * k)];
+          geta[v] = geta[v] + deta * Ps[el][v][i + n * (l + n * k)];
+          gzeta[v] = gzeta[v] + dzeta * Ps[el][v][i + n * (j + n * l)];
+        }
+      }
+      const R mf[3] = {M[0], M[n3], M[2 * n3]}, mg[3] = {M[3 * n3], M[4 * n3], M[5 * n3]},
+              mh[3] = {M[6 * n3], M[7 * n3], M[8 * n3]};
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int v = 0; v < 5; ++v) g[d][v] = mf[d] * gxi[v] + mg[d] * geta[v] + mh[d] * gzeta[v];
+    } else {
+      // Lifting_VolInt_Conservative (lifting_volint.t90:345-455): D_T (strong) or D_hat_T (weak)
+      const R* Dm = (L.lift_mode == 2) ? sb.DhatT : sb.D;  // DhatT(l,i) vs D_T(l,i) = D(i,l)
+      const R* Me = Met + (size_t)e * 10 * n3;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) g[d][v] = R(0);
+        for (int l = 0; l < n; ++l) {
+          R ci, cj, ck;
+          if (L.lift_mode == 2) { ci = Dm[l + n * i]; cj = Dm[l + n * j]; ck = Dm[l + n * k]; }
+          else { ci = Dm[i + n * l]; cj = Dm[j + n * l]; ck = Dm[k + n * l]; }
+          const int ni = l + n * (j + n * k), nj = i + n * (l + n * k), nk = i + n * (j + n * l);
+          const R wf = ci * Me[(0 + d) * n3 + ni], wh = ck * Me[(6 + d) * n3 + nk], wg = cj * Me[(3 + d) * n3 + nj];
+#pragma unroll
+          for (int v = 0; v < 5; ++v) g[d][v] = g[d][v] + wf * Ps[el][v][ni] + wh * Ps[el][v][nk] + wg * Ps[el][v][nj];
+        }
+      }
+    }
+    // surface part (SurfInt_Device_Single_Flux, surfint.t90:591-725) from Lifting_FillFlux
+    // (lifting_fillflux.t90:39-103) and Lifting_FillFlux_NormVec (:212-256)
+    R sl[3][5];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+      for (int v = 0; v < 5; ++v) sl[d][v] = R(0);
+    const R sigflux = (L.lift_mode == 2) ? R(1) : R(-1);
+#pragma unroll
+    for (int ls = 1; ls <= 6; ++ls) {
+      int a, b, l;
+      switch (ls) {
+        case L_XI_MINUS: case L_XI_PLUS: a = j; b = k; l = i; break;
+        case L_ETA_MINUS: case L_ETA_PLUS: a = i; b = k; l = j; break;
+        default: a = i; b = j; l = k; break;
+      }
+      const bool minus = is_minus(ls);
+      R Lhat;
+      if (L.gauss) Lhat = minus ? sb.Lhm[l] : sb.Lhp[l];
+      else {
+        if (l != (minus ? 0 : N)) continue;
+        Lhat = minus ? sb.Lhm[0] : sb.Lhp[N];
+      }
+      const int side = E2S[(e * 6 + ls - 1) * 2 + 0];
+      const int flip = E2S[(e * 6 + ls - 1) * 2 + 1];
+      int p, q;
+      s2v2_inv(N, a, b, flip, ls, p, q);
+      const int pq = p + n * q;
+      const R* pm = Pf + (size_t)side * 6 * n2 + pq;
+      const R* ps = Pf + ((size_t)L.nSides + side) * 6 * n2 + pq;
+      const R* fg = Fgeo + (size_t)side * 10 * n2 + pq;
+      const R se = fg[9 * n2];
+      const R nvv[3] = {fg[0], fg[n2], fg[2 * n2]};
+      const R sig = (L.lift_mode == 2) ? ((flip == 0) ? R(1) : R(-1)) : R(1);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        const int c = liftc[v];
+        const R fl = R(0.5) * se * (sigflux * pm[c * n2] + ps[c * n2]);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) sl[d][v] = sl[d][v] + sig * (fl * nvv[d]) * Lhat;
+      }
+    }
+    const R sj = M[9 * n3];
+    R* G = Gvol + (size_t)e * 15 * n3 + node;
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        const R val = sj * (g[d][v] + sl[d][v]);
+        Gs[el][d * 5 + v][node] = val;
+        G[(d * 5 + v) * n3] = val;
+      }
+  }
+  __syncthreads();
+  // ProlongToFaceLifting
+  for (int t = threadIdx.x; t < nloc * 6 * n2; t += blockDim.x) {
+    int el = t / (6 * n2), r = t - el * 6 * n2;
+    int ls = r / n2 + 1, pq = r - (ls - 1) * n2;
+    int p = pq % n, q = pq / n;
+    int e = e0 + el;
+    int side = E2S[(e * 6 + ls - 1) * 2 + 0];
+    int flip = E2S[(e * 6 + ls - 1) * 2 + 1];
+    int a, b;
+    s2v2(N, p, q, flip, ls, a, b);
+    const int slot = (flip == 0) ? 0 : 1;
+    R* gf = Gf + ((size_t)slot * L.nSides + side) * 15 * n2 + pq;
+    if (!L.gauss) {
+      int node = face_node(n, ls, a, b, is_minus(ls) ? 0 : N);
+#pragma unroll
+      for (int c = 0; c < 15; ++c) gf[c * n2] = Gs[el][c][node];
+    } else {
+      const R* Lv = is_minus(ls) ? sb.Lm : sb.Lp;
+      for (int c = 0; c < 15; ++c) {
+        R s = Gs[el][c][face_node(n, ls, a, b, 0)] * Lv[0];
+#pragma unroll
+        for (int l = 1; l < n; ++l) s = s + Gs[el][c][face_node(n, ls, a, b, l)] * Lv[l];
+        gf[c * n2] = s;
+      }
+    }
+  }
+}
+
+// =====================================================================================
+// k_face: FillFlux (fillflux.f90:45-172): Riemann + ViscousFlux + SurfElem, thread per face node
+// =====================================================================================
+template <typename R>
+__global__ void __launch_bounds__(256)
+k_face(const R* __restrict__ Uf, const R* __restrict__ Pf, const R* __restrict__ Gf, const R* __restrict__ Fgeo,
+       Gas<R> gas, Launch L, int n2, R* __restrict__ Flux) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)L.nSides * n2) return;
+  const int side = (int)(t / n2), pq = (int)(t - (long long)side * n2);
+  const size_t S = L.nSides;
+  R UL[5], UR[5], PL[6], PR[6];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    UL[v] = Uf[(size_t)side * 5 * n2 + v * n2 + pq];
+    UR[v] = Uf[(S + side) * 5 * n2 + v * n2 + pq];
+  }
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    PL[c] = Pf[(size_t)side * 6 * n2 + c * n2 + pq];
+    PR[c] = Pf[(S + side) * 6 * n2 + c * n2 + pq];
+  }
+  const R* fg = Fgeo + (size_t)side * 10 * n2 + pq;
+  const R nv[3] = {fg[0], fg[n2], fg[2 * n2]};
+  const R t1[3] = {fg[3 * n2], fg[4 * n2], fg[5 * n2]};
+  const R t2[3] = {fg[6 * n2], fg[7 * n2], fg[8 * n2]};
+  const R se = fg[9 * n2];
+  R F[5];
+  riemann_face(L.riemann, L.split, UL, UR, PL, PR, nv, t1, t2, gas.kappa, F);
+  if (L.parabolic) {
+    // ViscousFlux_Kernel_CUDA (riemann.f90:638-700): F = F + 0.5*f(L); F = F + 0.5*f(R)
+    R gx[5], gy[5], gz[5], fd[5];
+    const R* gm = Gf + (size_t)side * 15 * n2 + pq;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) { gx[v] = gm[v * n2]; gy[v] = gm[(5 + v) * n2]; gz[v] = gm[(10 + v) * n2]; }
+    normal_diff_flux(PL, gx, gy, gz, nv, gas.mu, gas.lambda, fd);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) F[v] = F[v] + R(0.5) * fd[v];
+    const R* gs = Gf + (S + side) * 15 * n2 + pq;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) { gx[v] = gs[v * n2]; gy[v] = gs[(5 + v) * n2]; gz[v] = gs[(10 + v) * n2]; }
+    normal_diff_flux(PR, gx, gy, gz, nv, gas.mu, gas.lambda, fd);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) F[v] = F[v] + R(0.5) * fd[v];
+  }
+  R* out = Flux + (size_t)side * 5 * n2 + pq;
+#pragma unroll
+  for (int v = 0; v < 5; ++v) out[v * n2] = F[v] * se;
+}
+
+// =====================================================================================
+// k_volume: VolInt (weak: volint.f90:129-188 / split: volint.f90:211-353) + SurfIntCons
+// (surfint.t90:352-586) + VAX_GPU(-1) + ApplyJacobian, and in RK mode the fused
+// VAXPB_OUT_VAXPB_IN stage update (vector.f90:163-183).
+// =====================================================================================
+struct RKArgs {
+  double* U;         // in/out (RK mode)
+  double* Ut_tmp;    // in/out (RK mode)
+  double* Ut;        // out (RHS mode)
+  double mRKA, b_dt;
+};
+
+template <int NP, typename R, int SPLIT, int PARAB>
+__global__ void __launch_bounds__(EPBof<NP>::v * NP * NP * NP)
+k_volume(const double* __restrict__ U, const R* __restrict__ Pvol, const R* __restrict__ Gvol,
+         const R* __restrict__ Met, const R* __restrict__ Flux, const int* __restrict__ E2S, DevBasis<R> basis,
+         Gas<R> gas, Launch L, RKArgs rk, int rkmode) {
+  constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, EPB = EPBof<NP>::v, N = NP - 1;
+  constexpr int NA = (SPLIT >= 0) ? 19 : 15;  // staging: 10 node data + 9 metrics, or 15 fluxes
+  __shared__ SBasis<NP, R> sb;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R* A = reinterpret_cast<R*>(smem_raw);             // [EPB][NA][n3]
+  R* AccD = A + (size_t)EPB * NA * n3;               // [EPB][3][5][n3]  (split form only)
+  load_basis(sb, basis);
+  const int e0 = blockIdx.x * EPB;
+  const int nloc = min(EPB, L.nElems - e0);
+  const int tid = threadIdx.x;
+  const bool active = tid < nloc * n3;
+  const int el = tid / n3, node = tid - (tid / n3) * n3;
+  const int e = e0 + el;
+  const int i = node % n, j = (node / n) % n, k = node / n2;
+  R* Ae = A + (size_t)el * NA * n3;
+  R vacc[5] = {0, 0, 0, 0, 0};  // this node's volume integral, kept in registers through phase B
+
+  // ---- phase A: flux-form volume part (weak Euler/NS, or the viscous part of the split form)
+  if (SPLIT < 0 || PARAB) {
+    if (active) {
+      const R* M = Met + (size_t)e * 10 * n3 + node;
+      const R* P = Pvol + (size_t)e * 7 * n3 + node;
+      const R Ms[3][3] = {{M[0], M[n3], M[2 * n3]}, {M[3 * n3], M[4 * n3], M[5 * n3]}, {M[6 * n3], M[7 * n3], M[8 * n3]}};
+      const R vel[3] = {P[n3], P[2 * n3], P[3 * n3]};
+      R fl[3][5];
+      R tau[6] = {0, 0, 0, 0, 0, 0}, tq[3] = {0, 0, 0};
+      if (PARAB) {
+        const R* G = Gvol + (size_t)e * 15 * n3 + node;
+        R gx[5], gy[5], gz[5];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) { gx[v] = G[v * n3]; gy[v] = G[(5 + v) * n3]; gz[v] = G[(10 + v) * n3]; }
+        visc_stress(gx, gy, gz, vel, gas.mu, gas.lambda, tau, tq);
+      }
+      if (SPLIT < 0) {
+        // EvalTransformedEulerFlux3D_fast (flux.f90:137-186) / EvalTransformedEulerDiffFlux3D (:509-614)
+        const double* Un = U + ((size_t)e * n3 + node) * 5;
+        const R m1 = (R)Un[1], m2 = (R)Un[2], m3 = (R)Un[3], E = (R)Un[4];
+        const R p = P[4 * n3], srho = P[6 * n3];
+        const R Ep = (E + p) * srho;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const R Mmom = Ms[d][0] * m1 + Ms[d][1] * m2 + Ms[d][2] * m3;
+          fl[d][0] = Mmom;
+          fl[d][1] = Mmom * vel[0] + Ms[d][0] * p;
+          fl[d][2] = Mmom * vel[1] + Ms[d][1] * p;
+          fl[d][3] = Mmom * vel[2] + Ms[d][2] * p;
+          fl[d][4] = Mmom * Ep;
+          if (PARAB) {
+            fl[d][1] = fl[d][1] - Ms[d][0] * tau[0] - Ms[d][1] * tau[3] - Ms[d][2] * tau[4];
+            fl[d][2] = fl[d][2] - Ms[d][0] * tau[3] - Ms[d][1] * tau[1] - Ms[d][2] * tau[5];
+            fl[d][3] = fl[d][3] - Ms[d][0] * tau[4] - Ms[d][1] * tau[5] - Ms[d][2] * tau[2];
+            fl[d][4] = fl[d][4] - Ms[d][0] * tq[0] - Ms[d][1] * tq[1] - Ms[d][2] * tq[2];
+          }
+        }
+      } else {
+        // EvalTransformedDiffFlux3D (flux.f90:619-697)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          fl[d][0] = R(0);
+          fl[d][1] = -Ms[d][0] * tau[0] - Ms[d][1] * tau[3] - Ms[d][2] * tau[4];
+          fl[d][2] = -Ms[d][0] * tau[3] - Ms[d][1] * tau[1] - Ms[d][2] * tau[5];
+          fl[d][3] = -Ms[d][0] * tau[4] - Ms[d][1] * tau[5] - Ms[d][2] * tau[2];
+          fl[d][4] = -Ms[d][0] * tq[0] - Ms[d][1] * tq[1] - Ms[d][2] * tq[2];
+        }
+      }
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int v = 0; v < 5; ++v) Ae[(d * 5 + v) * n3 + node] = fl[d][v];
+    }
+    __syncthreads();
+    if (active) {
+      // ApplyDMatrix_Kernel (applydmatrix.t90:19-75), order f, h, g
+      constexpr int v0 = (SPLIT < 0) ? 0 : 1;
+#pragma unroll
+      for (int l = 0; l < n; ++l) {
+        const R ci = sb.DhatT[l + n * i], ck = sb.DhatT[l + n * k], cj = sb.DhatT[l + n * j];
+        const int ni = l + n * (j + n * k), nk = i + n * (j + n * l), nj = i + n * (l + n * k);
+#pragma unroll
+        for (int v = v0; v < 5; ++v)
+          vacc[v] = vacc[v] + ci * Ae[(0 + v) * n3 + ni] + ck * Ae[(10 + v) * n3 + nk] + cj * Ae[(5 + v) * n3 + nj];
+      }
+    }
+  }
+
+  // ---- phase B: split-form flux differencing with pair symmetry, one thread per 1D line.
+  // Node a keeps its sum in registers over its pairs (a,b>a); node b's share goes to the line
+  // owner's per-direction shared accumulator, so no two threads ever write the same entry.
+  if constexpr (SPLIT >= 0) {
+    __syncthreads();  // phase A reads of the staging area are complete
+    if (active) {
+      const double* Un = U + ((size_t)e * n3 + node) * 5;
+      const R* P = Pvol + (size_t)e * 7 * n3 + node;
+      const R* M = Met + (size_t)e * 10 * n3 + node;
+      const R E = (R)Un[4];
+      Ae[0 * n3 + node] = P[0];
+      Ae[1 * n3 + node] = (R)Un[1];
+      Ae[2 * n3 + node] = (R)Un[2];
+      Ae[3 * n3 + node] = (R)Un[3];
+      Ae[4 * n3 + node] = E;
+      Ae[5 * n3 + node] = P[n3];
+      Ae[6 * n3 + node] = P[2 * n3];
+      Ae[7 * n3 + node] = P[3 * n3];
+      Ae[8 * n3 + node] = P[4 * n3];
+      // aux: H = (E+p)/rho (PI) or E/rho (KG)
+      Ae[9 * n3 + node] = (SPLIT == DG_SPLIT_PI) ? (E + P[4 * n3]) * P[6 * n3] : E * P[6 * n3];
+#pragma unroll
+      for (int c = 0; c < 9; ++c) Ae[(10 + c) * n3 + node] = M[c * n3];
+      R* Ad = AccD + (size_t)el * 15 * n3;
+#pragma unroll
+      for (int c = 0; c < 15; ++c) Ad[c * n3 + node] = R(0);
+    }
+    __syncthreads();
+    const int lel = tid / (3 * n2);
+    const bool lactive = (lel < nloc) && (tid < EPB * 3 * n2);  // 3*n2 <= n3 for NP >= 3
+    if (lactive) {
+      const int lr = tid - lel * 3 * n2;
+      const int dir = lr / n2, li = lr - dir * n2;
+      const R* Al = A + (size_t)lel * NA * n3;
+      R* Ad = AccD + ((size_t)lel * 3 + dir) * 5 * n3;
+      int base, stride;  // nodes of the line: base + l*stride
+      if (dir == 0) { base = n * li; stride = 1; }
+      else if (dir == 1) { base = (li % n) + n2 * (li / n); stride = n; }
+      else { base = li; stride = n2; }
+      const int mc = 10 + 3 * dir;
+#pragma unroll 1
+      for (int a = 0; a < NP - 1; ++a) {
+        const int na = base + a * stride;
+        PairNode<R> A_;
+        A_.rho = Al[0 * n3 + na]; A_.m1 = Al[1 * n3 + na]; A_.m2 = Al[2 * n3 + na]; A_.m3 = Al[3 * n3 + na];
+        A_.E = Al[4 * n3 + na]; A_.u = Al[5 * n3 + na]; A_.v = Al[6 * n3 + na]; A_.w = Al[7 * n3 + na];
+        A_.p = Al[8 * n3 + na]; A_.aux = Al[9 * n3 + na];
+        const R ma0 = Al[mc * n3 + na], ma1 = Al[(mc + 1) * n3 + na], ma2 = Al[(mc + 2) * n3 + na];
+        R sa[5];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) sa[v] = Ad[v * n3 + na];
+#pragma unroll 4
+        for (int b = a + 1; b < NP; ++b) {
+          const int nb = base + b * stride;
+          PairNode<R> B_;
+          B_.rho = Al[0 * n3 + nb]; B_.m1 = Al[1 * n3 + nb]; B_.m2 = Al[2 * n3 + nb]; B_.m3 = Al[3 * n3 + nb];
+          B_.E = Al[4 * n3 + nb]; B_.u = Al[5 * n3 + nb]; B_.v = Al[6 * n3 + nb]; B_.w = Al[7 * n3 + nb];
+          B_.p = Al[8 * n3 + nb]; B_.aux = Al[9 * n3 + nb];
+          const R Ms0 = ma0 + Al[mc * n3 + nb], Ms1 = ma1 + Al[(mc + 1) * n3 + nb], Ms2 = ma2 + Al[(mc + 2) * n3 + nb];
+          R F[5];
+          split_pair_flux<SPLIT, R>(A_, B_, Ms0, Ms1, Ms2, F);
+          const R dba = sb.DVS[b + n * a], dab = sb.DVS[a + n * b];  // DVolSurf(l=b,i=a), DVolSurf(l=a,i=b)
+#pragma unroll
+          for (int v = 0; v < 5; ++v) {
+            sa[v] = sa[v] + dba * F[v];
+            Ad[v * n3 + nb] += dab * F[v];
+          }
+        }
+#pragma unroll
+        for (int v = 0; v < 5; ++v) Ad[v * n3 + na] = sa[v];
+      }
+    }
+    __syncthreads();
+    if (active) {
+      const R* Ad = AccD + (size_t)el * 15 * n3;
+#pragma unroll
+      for (int v = 0; v < 5; ++v) vacc[v] = vacc[v] + (Ad[v * n3 + node] + Ad[(5 + v) * n3 + node] + Ad[(10 + v) * n3 + node]);
+    }
+  }
+
+  // ---- phase C: surface integral, -1, Jacobian, output / RK stage
+  if (!active) return;
+  R ut[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) ut[v] = R(0);
+#pragma unroll
+  for (int ls = 1; ls <= 6; ++ls) {
+    int a, b, l;
+    switch (ls) {
+      case L_XI_MINUS: case L_XI_PLUS: a = j; b = k; l = i; break;
+      case L_ETA_MINUS: case L_ETA_PLUS: a = i; b = k; l = j; break;
+      default: a = i; b = j; l = k; break;
+    }
+    const bool minus = is_minus(ls);
+    R Lhat;
+    if (L.gauss) Lhat = minus ? sb.Lhm[l] : sb.Lhp[l];
+    else {
+      if (l != (minus ? 0 : N)) continue;
+      Lhat = minus ? sb.Lhm[0] : sb.Lhp[N];
+    }
+    const int side = E2S[(e * 6 + ls - 1) * 2 + 0];
+    const int flip = E2S[(e * 6 + ls - 1) * 2 + 1];
+    int p, q;
+    s2v2_inv(N, a, b, flip, ls, p, q);
+    const R* fx = Flux + (size_t)side * 5 * n2 + p + n * q;
+    if (flip == 0) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) ut[v] = ut[v] + fx[v * n2] * Lhat;
+    } else {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) ut[v] = ut[v] - fx[v * n2] * Lhat;
+    }
+  }
+  const R sj = Met[(size_t)e * 10 * n3 + 9 * n3 + node];
+  const size_t g = ((size_t)e * n3 + node) * 5;
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    R val = vacc[v] + ut[v];
+    val = val * R(-1);
+    val = val * sj;
+    if (rkmode == 0) {
+      rk.Ut[g + v] = (double)val;
+    } else {
+      const double utmp = rk.Ut_tmp[g + v] * rk.mRKA + (double)val;
+      rk.Ut_tmp[g + v] = utmp;
+      rk.U[g + v] = rk.U[g + v] + utmp * rk.b_dt;
+    }
+  }
+}
+
+// =====================================================================================
+// CFL: CalcMaxEigenvalue (calctimestep.f90:192-296) + min reduction (FP64 throughout)
+// =====================================================================================
+__device__ __forceinline__ void atomic_min_pos(double* addr, double val) {
+  // positive doubles order like their bit patterns
+  unsigned long long* a = reinterpret_cast<unsigned long long*>(addr);
+  unsigned long long v = (unsigned long long)__double_as_longlong(val);
+  atomicMin(a, v);
+}
+
+// one block per element, blockDim = n^3 rounded up to a warp multiple
+template <int NP>
+__global__ void __launch_bounds__(1024)
+k_cfl(const double* __restrict__ U, const double* __restrict__ MetD, int nElems, double kappa, double mu0,
+      int parabolic, double KappasPr_max, double CFLScale, double DFLScale, double* __restrict__ dt2,
+      unsigned long long* __restrict__ bad) {
+  constexpr int n3 = NP * NP * NP;
+  constexpr int NW = (n3 + 31) / 32;
+  __shared__ double red[6][NW];
+  const int e = blockIdx.x;
+  const int node = threadIdx.x;
+  double lam[6] = {0, 0, 0, 0, 0, 0};
+  if (node < n3) {
+    const double* u = U + ((size_t)e * n3 + node) * 5;
+    const double srho = 1. / u[0];
+    const double vel[3] = {u[1] * srho, u[2] * srho, u[3] * srho};
+    const double p = (kappa - 1.) * (u[4] - 0.5 * (vel[0] * u[1] + vel[1] * u[2] + vel[2] * u[3]));
+    if (!(u[0] > 0.) || !(p > 0.) || !isfinite(u[4]) || !isfinite(u[1] + u[2] + u[3])) atomicAdd(bad, 1ULL);
+    const double c = sqrt(kappa * p * srho);
+    const double* M = MetD + (size_t)e * 10 * n3 + node;
+    const double sj = M[9 * n3];
+    const double vs[3] = {vel[0] * sj, vel[1] * sj, vel[2] * sj};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const double m0 = M[(3 * d) * n3], m1 = M[(3 * d + 1) * n3], m2 = M[(3 * d + 2) * n3];
+      const double adv = sj * sqrt(m0 * m0 + m1 * m1 + m2 * m2);  // MetricsAdv (calctimestep.f90:68)
+      lam[d] = fabs(m0 * vs[0] + m1 * vs[1] + m2 * vs[2]) + c * adv;
+      if (parabolic) {  // MetricsVisc (calctimestep.f90:81)
+        const double vis = KappasPr_max * ((m0 * sj) * (m0 * sj) + (m1 * sj) * (m1 * sj) + (m2 * sj) * (m2 * sj));
+        lam[3 + d] = mu0 * srho * vis;
+      }
+    }
+  }
+  // max over the element's nodes: warp shuffle, then across the element's warps
+#pragma unroll
+  for (int d = 0; d < 6; ++d) {
+    double v = lam[d];
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) red[d][threadIdx.x >> 5] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double mx[6];
+    for (int d = 0; d < 6; ++d) {
+      mx[d] = red[d][0];
+      for (int w = 1; w < NW; ++w) mx[d] = fmax(mx[d], red[d][w]);
+    }
+    atomic_min_pos(dt2, CFLScale * 2. / (mx[0] + mx[1] + mx[2]));
+    if (parabolic) atomic_min_pos(dt2 + 1, DFLScale * 4. / (mx[3] + mx[4] + mx[5]));
+  }
+}
+
+// state scan: NaN/Inf, non-positive density or pressure
+static __global__ void k_check(const double* __restrict__ U, long long nNodes, double kappa, unsigned long long* __restrict__ bad) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < nNodes; t += (long long)gridDim.x * blockDim.x) {
+    const double* u = U + t * 5;
+    const double p = (kappa - 1.) * (u[4] - 0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0]);
+    if (!(u[0] > 0.) || !(p > 0.) || !isfinite(u[1] + u[2] + u[3] + u[4])) atomicAdd(bad, 1ULL);
+  }
+}
+
+}  // namespace gx

@@ -1,0 +1,214 @@
+"""Host-side mirror of the reference's DG operator interface for this path.
+
+The reference drives the operator through module procedures on module-global device arrays:
+  InitDG / InitDGbasis              src/dg/dg.f90:67-242
+  DGTimeDerivative_weakForm(t)      src/dg/dg.f90:255-425
+  TimeStepByLSERKW2(t)              src/timedisc/timestep.f90:49-120
+  CALCTIMESTEP(errType)             src/equations/navierstokes/calctimestep.f90:98-186
+  FillIni                           src/dg/dg.f90:432-456
+Here the same calls go through the C ABI of the GB300 library; device arrays are torch CUDA
+tensors (plumbing only: the arithmetic runs in the library's own kernels).  Arrays use the
+reference's Fortran layouts; a Fortran array A(5,0:N,0:N,0:N,nElems) is held as a C-order
+array of shape (nElems, N+1, N+1, N+1, 5) with identical memory order.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _native as nat
+
+
+def config(N=3, NodeType="gauss-lobatto", Riemann="lf", SplitDG="none", parabolic=False, kappa=1.4, R=287.058,
+           Pr=0.72, mu0=0.0, doWeakLifting=False, doConservativeLifting=False, etaBR2=2.0, precision="fp64",
+           Lifting="br1"):
+    """Build a dg_config from the reference's ini key names (see dg_config_from_ini)."""
+    cfg = nat.DGConfig()
+    nat.lib().dg_config_default(ctypes.byref(cfg))
+    text = "\n".join([
+        "N = %d" % N, "NodeType = %s" % NodeType, "Riemann = %s" % Riemann, "SplitDG = %s" % SplitDG,
+        "Parabolic = %s" % ("T" if parabolic else "F"), "kappa = %r" % kappa, "R = %r" % R, "Pr = %r" % Pr,
+        "mu0 = %r" % mu0, "doWeakLifting = %s" % ("T" if doWeakLifting else "F"),
+        "doConservativeLifting = %s" % ("T" if doConservativeLifting else "F"), "etaBR2 = %r" % etaBR2,
+        "Precision = %s" % precision, "Lifting = %s" % Lifting])
+    nat.check(nat.lib().dg_config_from_ini(text.encode(), ctypes.byref(cfg)), "dg_config_from_ini")
+    return cfg
+
+
+def config_from_ini(text, base=None):
+    """Parse ini text (reference parameter-file syntax) into a dg_config."""
+    cfg = nat.DGConfig()
+    if base is None:
+        nat.lib().dg_config_default(ctypes.byref(cfg))
+    else:
+        ctypes.pointer(cfg)[0] = base
+    nat.check(nat.lib().dg_config_from_ini(text.encode(), ctypes.byref(cfg)), "dg_config_from_ini")
+    return cfg
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def basis(N, node_type):
+    """InitInterpolationBasis + InitDGbasis: dict of the 1D operators (D, D_hat_T, ... column-major)."""
+    n = N + 1
+    out = {k: np.zeros(n) for k in ("xGP", "wGP", "wBary", "L_minus", "L_plus", "L_hat_minus", "L_hat_plus")}
+    out.update({k: np.zeros(n * n) for k in ("D", "D_hat_T", "DVolSurf")})
+    nat.check(nat.lib().dg_basis(N, node_type, *[_ptr(out[k]) for k in (
+        "xGP", "wGP", "wBary", "L_minus", "L_plus", "D", "D_hat_T", "L_hat_minus", "L_hat_plus", "DVolSurf")]),
+        "dg_basis")
+    return out
+
+
+class Mesh:
+    """Periodic hexahedral box with the reference's connectivity and metric arrays.
+
+    Stand-in for a HOPR mesh read by ReadMesh/InitMesh (src/mesh/mesh_readin.f90, mesh.f90) and
+    CalcMetrics (src/mesh/metrics.f90).  Arrays (C order, Fortran layout reversed):
+      Elem_xGP (nElems,n,n,n,3)   Metrics_f/g/hTilde (nElems,n,n,n,3)   sJ (nElems,n,n,n)
+      NormVec/TangVec1/TangVec2 (nSides,n,n,3)   SurfElem (nSides,n,n)
+      ElemToSide (nElems,6,3)   SideToElem (nSides,5)   (1-based IDs)
+    """
+
+    def __init__(self, N, node_type, nx, ny, nz, x0=(0.0, 0.0, 0.0), x1=(1.0, 1.0, 1.0), deform=0.0):
+        L = nat.lib()
+        ne, ns = ctypes.c_int(), ctypes.c_int()
+        nat.check(L.dg_mesh_cartesian_sizes(nx, ny, nz, ctypes.byref(ne), ctypes.byref(ns)), "mesh sizes")
+        self.N, self.node_type = N, node_type
+        self.nElems, self.nSides = ne.value, ns.value
+        self.nx, self.ny, self.nz = nx, ny, nz
+        self.x0, self.x1, self.deform = tuple(x0), tuple(x1), deform
+        n = N + 1
+        E, S = self.nElems, self.nSides
+        self.Elem_xGP = np.zeros((E, n, n, n, 3))
+        self.Metrics_fTilde = np.zeros((E, n, n, n, 3))
+        self.Metrics_gTilde = np.zeros((E, n, n, n, 3))
+        self.Metrics_hTilde = np.zeros((E, n, n, n, 3))
+        self.sJ = np.zeros((E, n, n, n))
+        self.NormVec = np.zeros((S, n, n, 3))
+        self.TangVec1 = np.zeros((S, n, n, 3))
+        self.TangVec2 = np.zeros((S, n, n, 3))
+        self.SurfElem = np.zeros((S, n, n))
+        self.ElemToSide = np.zeros((E, 6, 3), dtype=np.int32)
+        self.SideToElem = np.zeros((S, 5), dtype=np.int32)
+        a0 = np.asarray(x0, dtype=np.float64)
+        a1 = np.asarray(x1, dtype=np.float64)
+        nat.check(L.dg_mesh_cartesian(N, node_type, nx, ny, nz, _ptr(a0), _ptr(a1), float(deform),
+                                      _ptr(self.Elem_xGP), _ptr(self.Metrics_fTilde), _ptr(self.Metrics_gTilde),
+                                      _ptr(self.Metrics_hTilde), _ptr(self.sJ), _ptr(self.NormVec),
+                                      _ptr(self.TangVec1), _ptr(self.TangVec2), _ptr(self.SurfElem),
+                                      _ptr(self.ElemToSide), _ptr(self.SideToElem)), "dg_mesh_cartesian")
+
+    @property
+    def nDOF(self):
+        return self.nElems * (self.N + 1) ** 3
+
+
+def fill_ini(mesh, exactfunc, params, kappa=1.4, R=287.058, t=0.0):
+    """FillIni (src/dg/dg.f90:432-456): conservative state at the nodes, shape (nElems,n,n,n,5)."""
+    n = mesh.N + 1
+    U = np.zeros((mesh.nElems, n, n, n, 5))
+    p = np.asarray(params, dtype=np.float64)
+    nat.check(nat.lib().dg_fill_ini(exactfunc, _ptr(p), len(p), mesh.nElems * n ** 3, _ptr(mesh.Elem_xGP),
+                                    float(kappa), float(R), float(t), _ptr(U)), "dg_fill_ini")
+    return U
+
+
+def tgv_state(mesh, mach=0.1, kappa=1.4, R=287.058):
+    """Taylor-Green vortex initial state (testcase/taylorgreenvortex/testcase.f90:220-262), rho0=U0=1, rho const."""
+    return fill_ini(mesh, nat.DG_EXACTFUNC_TGV, [1.0, 1.0, mach, 1.0], kappa=kappa, R=R)
+
+
+class DG:
+    """The GB300 DG operator for one mesh: MOD_DG + MOD_TimeDisc for this path.
+
+    U, Ut, Ut_tmp are torch float64 CUDA tensors of shape (nElems, n, n, n, 5) (reference layout).
+    """
+
+    def __init__(self, cfg, mesh):
+        import torch  # device memory and streams only
+        self._torch = torch
+        self.cfg = cfg
+        self.mesh = mesh
+        L = nat.lib()
+        h = ctypes.c_void_p()
+        nat.check(L.dg_ctx_create(ctypes.byref(cfg), ctypes.byref(h)), "dg_ctx_create")
+        self._h = h
+        m = mesh
+        nat.check(L.dg_set_mesh(h, m.nElems, m.nSides, 0, _ptr(m.Metrics_fTilde), _ptr(m.Metrics_gTilde),
+                                _ptr(m.Metrics_hTilde), _ptr(m.sJ), _ptr(m.NormVec), _ptr(m.TangVec1),
+                                _ptr(m.TangVec2), _ptr(m.SurfElem), _ptr(m.ElemToSide), _ptr(m.SideToElem)),
+                  "dg_set_mesh")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            nat.lib().dg_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- helpers ---------------------------------------------------------------------------
+    def _stream(self, stream=None):
+        torch = self._torch
+        s = stream if stream is not None else torch.cuda.current_stream()
+        return ctypes.c_void_p(s.cuda_stream)
+
+    def _check_state(self, U):
+        torch = self._torch
+        n = self.mesh.N + 1
+        if not (isinstance(U, torch.Tensor) and U.is_cuda and U.dtype == torch.float64 and U.is_contiguous()
+                and tuple(U.shape) == (self.mesh.nElems, n, n, n, 5)):
+            raise ValueError("state must be a contiguous float64 CUDA tensor of shape (nElems,n,n,n,5)")
+
+    def new_state(self):
+        n = self.mesh.N + 1
+        return self._torch.zeros((self.mesh.nElems, n, n, n, 5), dtype=self._torch.float64, device="cuda")
+
+    @property
+    def kernel_launches(self):
+        return nat.lib().dg_kernel_launch_count(self._h)
+
+    # -- the reference's operator surface ----------------------------------------------------
+    def DGTimeDerivative_weakForm(self, t, U, Ut=None, stream=None):
+        """Ut = DGTimeDerivative_weakForm(U) (src/dg/dg.f90:255-425)."""
+        self._check_state(U)
+        if Ut is None:
+            Ut = self._torch.empty_like(U)
+        self._check_state(Ut)
+        nat.check(nat.lib().dg_rhs(self._h, float(t), ctypes.c_void_p(U.data_ptr()), ctypes.c_void_p(Ut.data_ptr()),
+                                   self._stream(stream)), "dg_rhs")
+        return Ut
+
+    def TimeStepByLSERKW2(self, t, dt, U, Ut_tmp, nSteps=1, stream=None):
+        """nSteps Carpenter RK4-5 steps of size dt in place (src/timedisc/timestep.f90:49-120)."""
+        self._check_state(U)
+        self._check_state(Ut_tmp)
+        nat.check(nat.lib().dg_lserk_steps(self._h, float(t), float(dt), int(nSteps), ctypes.c_void_p(U.data_ptr()),
+                                           ctypes.c_void_p(Ut_tmp.data_ptr()), self._stream(stream)),
+                  "dg_lserk_steps")
+
+    def CalcTimeStep(self, U, CFLScale, DFLScale=0.0, stream=None):
+        """dt from CFL/DFL (calctimestep.f90:98-296, FillCFL_DFL timedisc_func.f90:480-550).
+
+        Returns (dt, errType); errType = 1 when the state holds NaN or non-positive rho/p."""
+        self._check_state(U)
+        dt = ctypes.c_double()
+        rc = nat.lib().dg_calc_timestep(self._h, ctypes.c_void_p(U.data_ptr()), float(CFLScale), float(DFLScale),
+                                        ctypes.byref(dt), self._stream(stream))
+        if rc == nat.DG_ERR_NAN:
+            return dt.value, 1
+        nat.check(rc, "dg_calc_timestep")
+        return dt.value, 0
+
+    def check_state(self, U, stream=None):
+        """Number of nodes holding NaN/Inf or non-positive density/pressure."""
+        self._check_state(U)
+        bad = ctypes.c_longlong()
+        rc = nat.lib().dg_check_state(self._h, ctypes.c_void_p(U.data_ptr()), ctypes.byref(bad), self._stream(stream))
+        if rc not in (nat.DG_OK, nat.DG_ERR_NAN):
+            nat.check(rc, "dg_check_state")
+        return bad.value

@@ -1,0 +1,210 @@
+/*
+ * galaexi_gb300 -- C ABI of the GB300-native DGSEM right-hand side and its
+ * low-storage Runge-Kutta stepper.
+ *
+ * This boundary replaces the module-global operator of GALAEXI:
+ *   DGTimeDerivative_weakForm(t)        src/dg/dg.f90:255-425
+ *   TimeStepByLSERKW2(t)                src/timedisc/timestep.f90:49-120
+ *   CALCTIMESTEP(errType)               src/equations/navierstokes/calctimestep.f90:98-186
+ *   InitDGbasis / InitMesh device copies src/dg/dg.f90:181-242, src/mesh/mesh.f90:307-451
+ * The reference works on module-global device arrays (MOD_DG_Vars, MOD_Mesh_Vars,
+ * MOD_Lifting_Vars); here the same arrays are passed explicitly, in the
+ * reference's Fortran (column-major) layouts:
+ *   U, Ut           (nVar=5, 0:N, 0:N, 0:N, nElems)   conservative state / time derivative
+ *   Metrics_f/g/hTilde (3, 0:N, 0:N, 0:N, nElems)     contravariant metric terms J*a^i
+ *   sJ              (0:N, 0:N, 0:N, nElems)           inverse Jacobian
+ *   NormVec/TangVec1/TangVec2 (3, 0:N, 0:N, nSides)   master-side face frame
+ *   SurfElem        (0:N, 0:N, nSides)                surface element
+ *   ElemToSide      (3, 6, nElems)  int32, 1-based IDs (E2S_SIDE_ID, E2S_FLIP, E2S_IS_MASTER)
+ *   SideToElem      (5, nSides)     int32, 1-based IDs, -1 where absent
+ * All functions return 0 on success or a negative DG_ERR_* status; none of them
+ * aborts the process or traps on the device.  dg_last_error() describes the
+ * most recent failure of the calling thread.
+ *
+ * Ownership: the caller owns U, Ut and Ut_tmp (device pointers, FP64); the
+ * context owns copies of metrics, connectivity and all scratch, sized once in
+ * dg_set_mesh.  dg_rhs / dg_lserk_step allocate nothing.
+ * Threading: one context per host thread and stream; calls are asynchronous
+ * on the given stream except dg_calc_timestep and dg_check_state, which
+ * return one host scalar each.
+ */
+#ifndef GALAEXI_GB300_H
+#define GALAEXI_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define DG_OK               0
+#define DG_ERR_ARG         -1   /* invalid argument or call order            */
+#define DG_ERR_ALLOC       -2   /* device allocation failed                  */
+#define DG_ERR_CUDA        -3   /* a CUDA runtime call failed                */
+#define DG_ERR_NAN         -4   /* NaN, Inf or non-positive density/pressure */
+#define DG_ERR_TIMEOUT     -5   /* a bounded device wait gave up             */
+#define DG_ERR_UNSUPPORTED -6   /* option combination not built              */
+
+/* ---- option values (ini keys of the reference, see dg_config) ----------- */
+/* NodeType: PP_NodeType of the reference build (src/CMakeLists.txt) */
+#define DG_NODETYPE_GAUSS          1
+#define DG_NODETYPE_GAUSS_LOBATTO  2
+/* Riemann: the RIEMANN macro numbering of src/equations/navierstokes/riemann.f90:69-87 */
+#define DG_RIEMANN_LF              0
+#define DG_RIEMANN_ROE             1
+#define DG_RIEMANN_ROEL2           2
+#define DG_RIEMANN_ROEENTROPYFIX   3
+#define DG_RIEMANN_HLL             4
+#define DG_RIEMANN_HLLC            5
+#define DG_RIEMANN_HLLE            6
+#define DG_RIEMANN_HLLEM           7
+#define DG_RIEMANN_AVERAGE         8   /* Riemann_FluxAverage, split form only (riemann.f90:1239) */
+/* SplitDG: the SPLIT_DG macro numbering of splitflux.f90:36-66; -1 = weak form */
+#define DG_SPLIT_NONE             -1
+#define DG_SPLIT_SD                0
+#define DG_SPLIT_MO                1
+#define DG_SPLIT_DU                2
+#define DG_SPLIT_KG                3
+#define DG_SPLIT_PI                4
+/* Lifting: PP_Lifting (src/dg/lifting/lifting.f90:26-32) */
+#define DG_LIFTING_BR1             1
+#define DG_LIFTING_BR2             2
+/* precision form of the bulk operator */
+#define DG_PRECISION_FP64          0   /* plain FP64 everywhere                              */
+#define DG_PRECISION_MIXED         1   /* FP32 volume/face/lifting/surface work, FP64 U, RK,
+                                          metric precompute, CFL reduction and integrals     */
+
+/* Run-time configuration.  Field names follow the reference's ini keys
+ * (N, NodeType, Riemann, SplitDG, kappa, R, Pr, mu0, doWeakLifting,
+ * doConservativeLifting, etaBR2); in GALAEXI several of them are compile-time
+ * macros, here all are run-time. */
+typedef struct dg_config {
+  int    N;                     /* polynomial degree, 1..DG_MAX_N                     */
+  int    node_type;             /* DG_NODETYPE_*                                      */
+  int    parabolic;             /* 0: Euler, 1: Navier-Stokes (constant mu0)          */
+  int    riemann;               /* DG_RIEMANN_*                                       */
+  int    split_dg;              /* DG_SPLIT_*; split forms need Gauss-Lobatto nodes   */
+  int    lifting;               /* DG_LIFTING_*                                       */
+  int    do_weak_lifting;       /* doWeakLifting (BR1)                                */
+  int    do_conservative_lifting; /* doConservativeLifting (BR1, strong form)         */
+  double eta_br2;               /* etaBR2                                             */
+  double kappa, R, Pr, mu0;     /* EOS_Vars (idealgas/eos.f90:191-203)                */
+  int    precision;             /* DG_PRECISION_*                                     */
+} dg_config;
+
+#define DG_MAX_N 9
+
+typedef struct dg_ctx dg_ctx;
+
+/* Fill *cfg with the reference's defaults (N=3, Gauss-Lobatto, Euler, LF,
+ * weak form, BR1 strong non-conservative, kappa=1.4, R=287.058, Pr=0.72,
+ * mu0=0, etaBR2=2, FP64). */
+void dg_config_default(dg_config* cfg);
+
+/* Parse ini text (key = value lines, '!' comments, case-insensitive keys and
+ * string values) into *cfg, starting from the values already in *cfg.
+ * Recognised keys: N, NodeType, Riemann, SplitDG, Lifting, Parabolic, kappa, R, Pr,
+ * mu0, doWeakLifting, doConservativeLifting, etaBR2, Precision.  Replaces the
+ * GET* calls of src/readintools/readintools.f90:1021-1229 for these keys. */
+int dg_config_from_ini(const char* ini_text, dg_config* cfg);
+
+/* Create a context: builds D, D^T, D_hat^T, L+-, L_hat+-, DVolSurf
+ * (InitDGbasis, src/dg/dg.f90:181-242) and uploads them. */
+int dg_ctx_create(const dg_config* cfg, dg_ctx** ctx);
+int dg_ctx_destroy(dg_ctx* ctx);
+
+/* Upload mesh data (host pointers, layouts above) and size all scratch.
+ * Replaces the device copies of InitMesh (src/mesh/mesh.f90:307-451) and
+ * InitCalctimestep (calctimestep.f90:51-92).  Periodic and inner faces are
+ * resolved in-kernel; boundary sides (nBCSides > 0) are not supported yet
+ * and return DG_ERR_UNSUPPORTED. */
+int dg_set_mesh(dg_ctx* ctx, int nElems, int nSides, int nBCSides,
+                const double* metrics_f, const double* metrics_g, const double* metrics_h,
+                const double* sJ,
+                const double* normvec, const double* tangvec1, const double* tangvec2,
+                const double* surfelem,
+                const int* elem_to_side, const int* side_to_elem);
+
+/* Ut = DGTimeDerivative_weakForm(U) at time t (src/dg/dg.f90:255-425).
+ * d_U, d_Ut: device FP64 arrays (5,0:N,0:N,0:N,nElems); stream: cudaStream_t or NULL. */
+int dg_rhs(dg_ctx* ctx, double t, const double* d_U, double* d_Ut, void* stream);
+
+/* One Carpenter-Kennedy RK4-5 low-storage step (TimeStepByLSERKW2,
+ * timestep.f90:49-120, coefficients timedisc_vars.f90:213-227), updating
+ * d_U in place; d_Ut_tmp is the caller-owned second register (zero it before
+ * the first step, as the reference does). */
+int dg_lserk_step(dg_ctx* ctx, double t, double dt, double* d_U, double* d_Ut_tmp, void* stream);
+
+/* Several steps of fixed dt in one call (the same arithmetic as repeated
+ * dg_lserk_step calls). */
+int dg_lserk_steps(dg_ctx* ctx, double t, double dt, int nSteps, double* d_U, double* d_Ut_tmp,
+                   void* stream);
+
+/* dt = min over elements of CFLScale*2/lambda_conv and DFLScale*4/lambda_visc
+ * (CALCTIMESTEP, calctimestep.f90:98-296).  cfl_scale / dfl_scale are the
+ * ini values CFLScale / DFLScale; the N- and node-type-dependent scaling of
+ * FillCFL_DFL (timedisc_func.f90:480-550, Carpenter RK4-5 tables) is applied
+ * inside.  Synchronises the stream.  Returns DG_ERR_NAN if the state holds a
+ * NaN or a non-positive density or pressure. */
+int dg_calc_timestep(dg_ctx* ctx, const double* d_U, double cfl_scale, double dfl_scale,
+                     double* dt_out, void* stream);
+
+/* Scan the state for NaN/Inf or non-positive density/pressure; *bad_count
+ * receives the number of bad nodes.  Synchronises the stream. */
+int dg_check_state(dg_ctx* ctx, const double* d_U, long long* bad_count, void* stream);
+
+/* Measurement utilities (no counterpart in the reference).
+ * dg_profile_stage: run `reps` LSERK stages on d_U / d_Ut_tmp (modified in place) with CUDA events
+ * around each kernel; ms_out[0..4] = average ms of (prolong, lift, face, volume, whole stage).
+ * dg_measure_fma_peak: FMA-chain microkernel on the current device; precision 0 = FP64, 1 = FP32;
+ * *gflops receives the achieved FLOP rate (FMA = 2 flops). */
+int dg_profile_stage(dg_ctx* ctx, double* d_U, double* d_Ut_tmp, double dt, int reps, double* ms_out, void* stream);
+int dg_measure_fma_peak(int precision, double* gflops);
+
+/* Number of kernels this context launched since creation (for accounting). */
+long long dg_kernel_launch_count(const dg_ctx* ctx);
+
+/* Description of the last error on the calling thread. */
+const char* dg_last_error(void);
+
+/* ---- host-side mesh and state set-up (stand-ins for HOPR + ReadMesh) ------ */
+
+/* Basis of the reference (InitInterpolationBasis + InitDGbasis): arrays of
+ * length N+1 or (N+1)^2 (column-major (0:N,0:N)).  Any output may be NULL. */
+int dg_basis(int N, int node_type, double* xGP, double* wGP, double* wBary,
+             double* L_minus, double* L_plus, double* D, double* D_hat_T,
+             double* L_hat_minus, double* L_hat_plus, double* DVolSurf);
+
+/* Sizes of a periodic Cartesian box of nx*ny*nz hexahedra. */
+int dg_mesh_cartesian_sizes(int nx, int ny, int nz, int* nElems, int* nSides);
+
+/* Build a periodic box [x0,x1]^3 with nx*ny*nz elements, optionally displaced
+ * by x_i += deform_amp * sin(2 pi xh) sin(2 pi yh) sin(2 pi zh) with
+ * (xh,yh,zh) the coordinates normalised to [0,1] (deform_amp = 0: affine).
+ * Outputs in the layouts of dg_set_mesh plus the node coordinates
+ * Elem_xGP(3,0:N,0:N,0:N,nElems).  Metrics use the conservative curl form
+ * (metrics.f90:171-560) on the solution nodes; face vectors follow
+ * SurfMetricsFromJa (metrics.f90:752-789).  Every element is master of its
+ * XI_PLUS, ETA_PLUS and ZETA_PLUS sides. */
+int dg_mesh_cartesian(int N, int node_type, int nx, int ny, int nz,
+                      const double* x0, const double* x1, double deform_amp,
+                      double* elem_xgp,
+                      double* metrics_f, double* metrics_g, double* metrics_h, double* sJ,
+                      double* normvec, double* tangvec1, double* tangvec2, double* surfelem,
+                      int* elem_to_side, int* side_to_elem);
+
+/* Initial states at the nodes (FillIni, src/dg/dg.f90:432-456).  xgp: (3,nNodes), U: (5,nNodes).
+ *   DG_EXACTFUNC_CONST      params: RefState (rho,u,v,w,p)
+ *   DG_EXACTFUNC_SHU_VORTEX params: RefState(5), IniCenter(3), IniAxis(3), IniAmplitude, IniHalfwidth
+ *                           (IniExactFunc=7, idealgas/exactfunc.f90:482-502; t advects the centre)
+ *   DG_EXACTFUNC_TGV        params: rho0, U0, MachNumber, IniConstDens (0/1)
+ *                           (testcase/taylorgreenvortex/testcase.f90:145-149,220-262) */
+#define DG_EXACTFUNC_CONST       1
+#define DG_EXACTFUNC_SHU_VORTEX  7
+#define DG_EXACTFUNC_TGV       100
+int dg_fill_ini(int exactfunc, const double* params, int nParams, long long nNodes, const double* xgp,
+                double kappa, double R, double t, double* U);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GALAEXI_GB300_H */

@@ -1,0 +1,45 @@
+"""Copy the reference's golden unit-test data into tests/golden/.
+
+The GALAEXI reference keeps golden vectors for its basis and face operators as
+Fortran sequential-unformatted files (4-byte record markers, float64/int32
+little endian) under unitTests/.  They are data, not code.  This script copies
+the ones that pin the DGSEM path so that the tests also run where the reference
+tree is absent:
+
+  NodesAndWeights.bin          x, w, wBary for N=1..10, 4 node sets   (unitTests/NodesAndWeights.f90)
+  DerivativeMatrix.bin         D for N=1..10, 4 node sets             (unitTests/DerivativeMatrix.f90)
+  UnittestElementData3D.bin    one curved element, NRef=9             (unitTests/unittest.f90:50,97)
+  ProlongToFaceUvol.bin        random volume data                     (unitTests/ProlongToFace.f90)
+  ProlongToFace_{G,GL}3D.bin   prolonged face data
+  SurfIntFlux.bin              random face flux                       (unitTests/SurfInt.f90)
+  SurfInt_{G,GL}3D.bin         surface-integral result
+
+Usage:  python tests/golden/fetch_reference_fixtures.py [/path/to/reference]
+"""
+import os
+import shutil
+import sys
+
+FILES = [
+    "NodesAndWeights.bin",
+    "DerivativeMatrix.bin",
+    "UnittestElementData3D.bin",
+    "ProlongToFaceUvol.bin",
+    "ProlongToFace_G3D.bin",
+    "ProlongToFace_GL3D.bin",
+    "SurfIntFlux.bin",
+    "SurfInt_G3D.bin",
+    "SurfInt_GL3D.bin",
+]
+
+
+def main(ref_root):
+    here = os.path.dirname(os.path.abspath(__file__))
+    for name in FILES:
+        src = os.path.join(ref_root, "unitTests", name)
+        shutil.copyfile(src, os.path.join(here, name))
+        print("copied", name)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
