@@ -2,6 +2,7 @@
 // The entry points replace the reference's module-global operator (see include/galaexi_gb300.h).
 #include <cuda_runtime.h>
 #include <cstdio>
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -225,7 +226,8 @@ int dg_ctx_create(const dg_config* cfg, dg_ctx** out) {
   ctx->n3 = ctx->n2 * ctx->n;
   gxh::basis_1d(cfg->N, cfg->node_type, ctx->B);
   const gxc::NPTable* T = table_for(ctx->n);
-  int rc = (cfg->precision == DG_PRECISION_FP64) ? upload_basis(ctx, ctx->d) : upload_basis(ctx, ctx->f);
+  int rc = upload_basis(ctx, ctx->d);
+  if (rc == DG_OK && cfg->precision == DG_PRECISION_MIXED) rc = upload_basis(ctx, ctx->f);
   if (rc == DG_OK) rc = (cfg->precision == DG_PRECISION_FP64) ? T->configure_d() : T->configure_f();
   if (rc == DG_OK && !(ctx->red.alloc(2) && ctx->bad.alloc(1))) { set_error("cudaMalloc"); rc = DG_ERR_ALLOC; }
   if (rc != DG_OK) { dg_ctx_destroy(ctx); return rc; }
@@ -295,13 +297,14 @@ int dg_set_mesh(dg_ctx* ctx, int nElems, int nSides, int nBCSides, const double*
   ctx->nSides = nSides;
   ctx->d.release();
   ctx->f.release();
-  int rc;
-  if (ctx->cfg.precision == DG_PRECISION_FP64) {
-    rc = upload_basis(ctx, ctx->d);
-    if (rc == DG_OK) rc = alloc_prec(ctx, ctx->d, met, fgeo);
-  } else {
-    rc = upload_basis(ctx, ctx->f);
-    if (rc == DG_OK) rc = alloc_prec(ctx, ctx->f, met, fgeo);
+  int rc = upload_basis(ctx, ctx->d);
+  if (rc == DG_OK) {
+    if (ctx->cfg.precision == DG_PRECISION_FP64) {
+      rc = alloc_prec(ctx, ctx->d, met, fgeo);
+    } else {
+      rc = upload_basis(ctx, ctx->f);
+      if (rc == DG_OK) rc = alloc_prec(ctx, ctx->f, met, fgeo);
+    }
   }
   if (rc != DG_OK) return rc;
   if (!ctx->MetD.alloc(met.size()) || !ctx->E2S.alloc(he2s.size())) { set_error("cudaMalloc mesh"); return DG_ERR_ALLOC; }
@@ -382,5 +385,12 @@ int dg_check_state(dg_ctx* ctx, const double* d_U, long long* bad_count, void* s
 }
 
 long long dg_kernel_launch_count(const dg_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+int dg_set_pressure_offset(dg_ctx* ctx, double p_ref) {
+  if (int rc = check_ctx(ctx, false)) return rc;
+  if (!(p_ref >= 0.) || !std::isfinite(p_ref)) { set_error("pressure offset must be finite and >= 0"); return DG_ERR_ARG; }
+  ctx->pref = p_ref;
+  return DG_OK;
+}
 
 }  // extern "C"

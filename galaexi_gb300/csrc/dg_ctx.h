@@ -51,8 +51,12 @@ inline gx::DevBasis<R> dev_basis(const PrecData<R>& P, int n) {
 }
 
 template <typename R>
-inline gx::Gas<R> make_gas(const dg_config& c) {
+inline gx::Gas<R> make_gas(const dg_config& c, double pref) {
   gx::Gas<R> g;
+  g.pref = (R)pref;
+  g.prefD = pref;
+  g.kappaM1D = c.kappa - 1.;
+  g.sRD = 1. / c.R;
   g.kappa = (R)c.kappa;
   g.kappaM1 = (R)(c.kappa - 1.);
   g.sKappaM1 = (R)(1. / (c.kappa - 1.));
@@ -78,6 +82,7 @@ struct dg_ctx {
   gxc::DBuf<unsigned long long> bad;
   long long launches = 0;
   bool mesh_ok = false;
+  double pref = 0.;        // reference pressure of the mixed form (dg_set_pressure_offset)
 };
 
 namespace gxc {

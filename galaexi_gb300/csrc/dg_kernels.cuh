@@ -104,27 +104,28 @@ template <int NP> struct EPBof { static constexpr int v = (NP * NP * NP >= 128) 
 // =====================================================================================
 template <int NP, typename R>
 __global__ void __launch_bounds__(EPBof<NP>::v * NP * NP * NP)
-k_prolong(const double* __restrict__ U, const int* __restrict__ E2S, DevBasis<R> basis, Gas<R> gas, Launch L,
-          R* __restrict__ Pvol, R* __restrict__ Uf, R* __restrict__ Pf) {
+k_prolong(const double* __restrict__ U, const int* __restrict__ E2S, const double* __restrict__ Lm,
+          const double* __restrict__ Lp, Gas<R> gas, Launch L, R* __restrict__ Pvol, R* __restrict__ Uf,
+          R* __restrict__ Pf) {
   constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, EPB = EPBof<NP>::v, N = NP - 1;
-  __shared__ SBasis<NP, R> sb;
-  __shared__ R Us[EPB][5][n3];
-  load_basis(sb, basis);
+  __shared__ SBasis<NP, double> sb;
+  __shared__ double Us[EPB][5][n3];
+  for (int t = threadIdx.x; t < NP; t += blockDim.x) { sb.Lm[t] = Lm[t]; sb.Lp[t] = Lp[t]; }
   const int e0 = blockIdx.x * EPB;
   const int nloc = min(EPB, L.nElems - e0);
   // coalesced load of the element block (AoS (5,n^3) per element in global memory)
   const double* Ub = U + (size_t)e0 * 5 * n3;
   for (int t = threadIdx.x; t < nloc * 5 * n3; t += blockDim.x) {
     int el = t / (5 * n3), r = t - el * 5 * n3;
-    Us[el][r % 5][r / 5] = (R)Ub[t];
+    Us[el][r % 5][r / 5] = Ub[t];
   }
   __syncthreads();
   // volume prims
   for (int t = threadIdx.x; t < nloc * n3; t += blockDim.x) {
     int el = t / n3, node = t - el * n3;
-    R u[5] = {Us[el][0][node], Us[el][1][node], Us[el][2][node], Us[el][3][node], Us[el][4][node]};
+    const double u[5] = {Us[el][0][node], Us[el][1][node], Us[el][2][node], Us[el][3][node], Us[el][4][node]};
     R prim[6], srho;
-    cons_to_prim(u, gas, prim, srho);
+    cons_to_prim_d(u, gas, prim, srho);
     R* P = Pvol + (size_t)(e0 + el) * 7 * n3 + node;
 #pragma unroll
     for (int c = 0; c < 6; ++c) P[c * n3] = prim[c];
@@ -140,28 +141,28 @@ k_prolong(const double* __restrict__ U, const int* __restrict__ E2S, DevBasis<R>
     int flip = E2S[(e * 6 + ls - 1) * 2 + 1];
     int a, b;
     s2v2(N, p, q, flip, ls, a, b);
-    R u[5];
+    double u[5];
     if (!L.gauss) {
       int node = face_node(n, ls, a, b, is_minus(ls) ? 0 : N);
 #pragma unroll
       for (int v = 0; v < 5; ++v) u[v] = Us[el][v][node];
     } else {
-      const R* Lv = is_minus(ls) ? sb.Lm : sb.Lp;
+      const double* Lv = is_minus(ls) ? sb.Lm : sb.Lp;
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
-        R s = Us[el][v][face_node(n, ls, a, b, 0)] * Lv[0];
+        double s = Us[el][v][face_node(n, ls, a, b, 0)] * Lv[0];
 #pragma unroll
         for (int l = 1; l < n; ++l) s = s + Us[el][v][face_node(n, ls, a, b, l)] * Lv[l];
         u[v] = s;
       }
     }
     R prim[6], srho;
-    cons_to_prim(u, gas, prim, srho);
+    cons_to_prim_d(u, gas, prim, srho);
     const int slot = (flip == 0) ? 0 : 1;
     R* uf = Uf + ((size_t)slot * L.nSides + side) * 5 * n2 + pq;
     R* pf = Pf + ((size_t)slot * L.nSides + side) * 6 * n2 + pq;
 #pragma unroll
-    for (int v = 0; v < 5; ++v) uf[v * n2] = u[v];
+    for (int v = 0; v < 5; ++v) uf[v * n2] = (R)u[v];
 #pragma unroll
     for (int c = 0; c < 6; ++c) pf[c * n2] = prim[c];
   }
@@ -195,9 +196,11 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
     const int e = e0 + el;
     const int i = node % n, j = (node / n) % n, k = node / n2;
     const R* M = Met + (size_t)e * 10 * n3 + node;
+    const R sj = M[9 * n3];
     R g[3][5];
     if (L.lift_mode == 0) {
-      // Lifting_VolInt_Nonconservative_GPU_Kernel (lifting_volint.t90:262-328)
+      // Lifting_VolInt_Nonconservative_GPU_Kernel (lifting_volint.t90:262-328), with the Jacobian of
+      // the surface integral (surfint.t90:718-723) folded into the metric terms
       R gxi[5], geta[5], gzeta[5];
 #pragma unroll
       for (int v = 0; v < 5; ++v) { gxi[v] = R(0); geta[v] = R(0); gzeta[v] = R(0); }
@@ -211,8 +214,8 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
           gzeta[v] = gzeta[v] + dzeta * Ps[el][v][i + n * (j + n * l)];
         }
       }
-      const R mf[3] = {M[0], M[n3], M[2 * n3]}, mg[3] = {M[3 * n3], M[4 * n3], M[5 * n3]},
-              mh[3] = {M[6 * n3], M[7 * n3], M[8 * n3]};
+      const R mf[3] = {sj * M[0], sj * M[n3], sj * M[2 * n3]}, mg[3] = {sj * M[3 * n3], sj * M[4 * n3], sj * M[5 * n3]},
+              mh[3] = {sj * M[6 * n3], sj * M[7 * n3], sj * M[8 * n3]};
 #pragma unroll
       for (int d = 0; d < 3; ++d)
 #pragma unroll
@@ -234,15 +237,14 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
 #pragma unroll
           for (int v = 0; v < 5; ++v) g[d][v] = g[d][v] + wf * Ps[el][v][ni] + wh * Ps[el][v][nk] + wg * Ps[el][v][nj];
         }
+#pragma unroll
+        for (int v = 0; v < 5; ++v) g[d][v] = sj * g[d][v];
       }
     }
-    // surface part (SurfInt_Device_Single_Flux, surfint.t90:591-725) from Lifting_FillFlux
-    // (lifting_fillflux.t90:39-103) and Lifting_FillFlux_NormVec (:212-256)
-    R sl[3][5];
-#pragma unroll
-    for (int d = 0; d < 3; ++d)
-#pragma unroll
-      for (int v = 0; v < 5; ++v) sl[d][v] = R(0);
+    // surface part (SurfInt_Device_Single_Flux, surfint.t90:591-725) of the BR1 flux
+    // 0.5*SurfElem*(sig*U_master + U_slave) (Lifting_FillFlux, lifting_fillflux.t90:39-103) times the
+    // normal (Lifting_FillFlux_NormVec, :212-256) times L_hat and the Jacobian; the scalar factors of
+    // one face are folded into one weight.
     const R sigflux = (L.lift_mode == 2) ? R(1) : R(-1);
 #pragma unroll
     for (int ls = 1; ls <= 6; ++ls) {
@@ -267,24 +269,23 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
       const R* pm = Pf + (size_t)side * 6 * n2 + pq;
       const R* ps = Pf + ((size_t)L.nSides + side) * 6 * n2 + pq;
       const R* fg = Fgeo + (size_t)side * 10 * n2 + pq;
-      const R se = fg[9 * n2];
-      const R nvv[3] = {fg[0], fg[n2], fg[2 * n2]};
       const R sig = (L.lift_mode == 2) ? ((flip == 0) ? R(1) : R(-1)) : R(1);
+      const R wgt = sig * Lhat * R(0.5) * fg[9 * n2] * sj;
+      const R nvv[3] = {wgt * fg[0], wgt * fg[n2], wgt * fg[2 * n2]};
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
         const int c = liftc[v];
-        const R fl = R(0.5) * se * (sigflux * pm[c * n2] + ps[c * n2]);
+        const R fl = sigflux * pm[c * n2] + ps[c * n2];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) sl[d][v] = sl[d][v] + sig * (fl * nvv[d]) * Lhat;
+        for (int d = 0; d < 3; ++d) g[d][v] = g[d][v] + fl * nvv[d];
       }
     }
-    const R sj = M[9 * n3];
     R* G = Gvol + (size_t)e * 15 * n3 + node;
 #pragma unroll
     for (int d = 0; d < 3; ++d)
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
-        const R val = sj * (g[d][v] + sl[d][v]);
+        const R val = g[d][v];
         Gs[el][d * 5 + v][node] = val;
         G[(d * 5 + v) * n3] = val;
       }
@@ -346,7 +347,7 @@ k_face(const R* __restrict__ Uf, const R* __restrict__ Pf, const R* __restrict__
   const R t2[3] = {fg[6 * n2], fg[7 * n2], fg[8 * n2]};
   const R se = fg[9 * n2];
   R F[5];
-  riemann_face(L.riemann, L.split, UL, UR, PL, PR, nv, t1, t2, gas.kappa, F);
+  riemann_face(L.riemann, L.split, UL, UR, PL, PR, nv, t1, t2, gas, F);
   if (L.parabolic) {
     // ViscousFlux_Kernel_CUDA (riemann.f90:638-700): F = F + 0.5*f(L); F = F + 0.5*f(R)
     R gx[5], gy[5], gz[5], fd[5];
@@ -422,8 +423,8 @@ k_volume(const double* __restrict__ U, const R* __restrict__ Pvol, const R* __re
         // EvalTransformedEulerFlux3D_fast (flux.f90:137-186) / EvalTransformedEulerDiffFlux3D (:509-614)
         const double* Un = U + ((size_t)e * n3 + node) * 5;
         const R m1 = (R)Un[1], m2 = (R)Un[2], m3 = (R)Un[3], E = (R)Un[4];
-        const R p = P[4 * n3], srho = P[6 * n3];
-        const R Ep = (E + p) * srho;
+        const R p = P[4 * n3], srho = P[6 * n3];  // p: momentum pressure (p' in the mixed form)
+        const R Ep = (E + p_abs(p, gas)) * srho;
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
           const R Mmom = Ms[d][0] * m1 + Ms[d][1] * m2 + Ms[d][2] * m3;
@@ -480,17 +481,17 @@ k_volume(const double* __restrict__ U, const R* __restrict__ Pvol, const R* __re
       const R* P = Pvol + (size_t)e * 7 * n3 + node;
       const R* M = Met + (size_t)e * 10 * n3 + node;
       const R E = (R)Un[4];
-      Ae[0 * n3 + node] = P[0];
+      const R rho = P[0], uu = P[n3], vv = P[2 * n3], ww = P[3 * n3], pm = P[4 * n3];
+      Ae[0 * n3 + node] = rho;
       Ae[1 * n3 + node] = (R)Un[1];
       Ae[2 * n3 + node] = (R)Un[2];
       Ae[3 * n3 + node] = (R)Un[3];
-      Ae[4 * n3 + node] = E;
-      Ae[5 * n3 + node] = P[n3];
-      Ae[6 * n3 + node] = P[2 * n3];
-      Ae[7 * n3 + node] = P[3 * n3];
-      Ae[8 * n3 + node] = P[4 * n3];
-      // aux: H = (E+p)/rho (PI) or E/rho (KG)
-      Ae[9 * n3 + node] = (SPLIT == DG_SPLIT_PI) ? (E + P[4 * n3]) * P[6 * n3] : E * P[6 * n3];
+      Ae[4 * n3 + node] = pair_aux<SPLIT, R>(rho, uu, vv, ww, E, p_abs(pm, gas), P[6 * n3]);
+      Ae[5 * n3 + node] = uu;
+      Ae[6 * n3 + node] = vv;
+      Ae[7 * n3 + node] = ww;
+      Ae[8 * n3 + node] = pm;
+      Ae[9 * n3 + node] = R(0);
 #pragma unroll
       for (int c = 0; c < 9; ++c) Ae[(10 + c) * n3 + node] = M[c * n3];
       R* Ad = AccD + (size_t)el * 15 * n3;
@@ -515,8 +516,8 @@ k_volume(const double* __restrict__ U, const R* __restrict__ Pvol, const R* __re
         const int na = base + a * stride;
         PairNode<R> A_;
         A_.rho = Al[0 * n3 + na]; A_.m1 = Al[1 * n3 + na]; A_.m2 = Al[2 * n3 + na]; A_.m3 = Al[3 * n3 + na];
-        A_.E = Al[4 * n3 + na]; A_.u = Al[5 * n3 + na]; A_.v = Al[6 * n3 + na]; A_.w = Al[7 * n3 + na];
-        A_.p = Al[8 * n3 + na]; A_.aux = Al[9 * n3 + na];
+        A_.aux = Al[4 * n3 + na]; A_.u = Al[5 * n3 + na]; A_.v = Al[6 * n3 + na]; A_.w = Al[7 * n3 + na];
+        A_.pm = Al[8 * n3 + na];
         const R ma0 = Al[mc * n3 + na], ma1 = Al[(mc + 1) * n3 + na], ma2 = Al[(mc + 2) * n3 + na];
         R sa[5];
 #pragma unroll
@@ -526,11 +527,11 @@ k_volume(const double* __restrict__ U, const R* __restrict__ Pvol, const R* __re
           const int nb = base + b * stride;
           PairNode<R> B_;
           B_.rho = Al[0 * n3 + nb]; B_.m1 = Al[1 * n3 + nb]; B_.m2 = Al[2 * n3 + nb]; B_.m3 = Al[3 * n3 + nb];
-          B_.E = Al[4 * n3 + nb]; B_.u = Al[5 * n3 + nb]; B_.v = Al[6 * n3 + nb]; B_.w = Al[7 * n3 + nb];
-          B_.p = Al[8 * n3 + nb]; B_.aux = Al[9 * n3 + nb];
+          B_.aux = Al[4 * n3 + nb]; B_.u = Al[5 * n3 + nb]; B_.v = Al[6 * n3 + nb]; B_.w = Al[7 * n3 + nb];
+          B_.pm = Al[8 * n3 + nb];
           const R Ms0 = ma0 + Al[mc * n3 + nb], Ms1 = ma1 + Al[(mc + 1) * n3 + nb], Ms2 = ma2 + Al[(mc + 2) * n3 + nb];
           R F[5];
-          split_pair_flux<SPLIT, R>(A_, B_, Ms0, Ms1, Ms2, F);
+          split_pair_flux<SPLIT, R>(A_, B_, Ms0, Ms1, Ms2, R(2) * gas.pref, F);
           const R dba = sb.DVS[b + n * a], dab = sb.DVS[a + n * b];  // DVolSurf(l=b,i=a), DVolSurf(l=a,i=b)
 #pragma unroll
           for (int v = 0; v < 5; ++v) {

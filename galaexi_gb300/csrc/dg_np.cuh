@@ -71,7 +71,7 @@ int vol(dg_ctx* ctx, PrecData<R>& P, const double* U, gx::RKArgs rk, int rkmode,
   }
   const int grid = (ctx->nElems + EPB - 1) / EPB;
   const gx::DevBasis<R> b = gxc::dev_basis(P, NP);
-  const gx::Gas<R> gas = gxc::make_gas<R>(ctx->cfg);
+  const gx::Gas<R> gas = gxc::make_gas<R>(ctx->cfg, ctx->cfg.precision == DG_PRECISION_MIXED ? ctx->pref : 0.);
   const gx::Launch L = gxc::make_launch(ctx);
   if (ctx->cfg.parabolic)
     gx::k_volume<NP, R, SPL, 1><<<grid, NT, volume_smem<R, SPL>(), st>>>(U, P.Pvol.p, P.Gvol.p, P.Met.p, P.Flux.p,
@@ -89,8 +89,9 @@ int rhs(dg_ctx* ctx, PrecData<R>& P, const double* U, gx::RKArgs rk, int rkmode,
   if (ev) cudaEventRecord(ev[0], st);
   const gx::Launch L = gxc::make_launch(ctx);
   const gx::DevBasis<R> b = gxc::dev_basis(P, NP);
-  const gx::Gas<R> gas = gxc::make_gas<R>(ctx->cfg);
-  gx::k_prolong<NP, R><<<grid, NT, 0, st>>>(U, ctx->E2S.p, b, gas, L, P.Pvol.p, P.Uf.p, P.Pf.p);
+  const gx::Gas<R> gas = gxc::make_gas<R>(ctx->cfg, ctx->cfg.precision == DG_PRECISION_MIXED ? ctx->pref : 0.);
+  const gx::DevBasis<double> bd = gxc::dev_basis(ctx->d, NP);  // FP64 face interpolation in both forms
+  gx::k_prolong<NP, R><<<grid, NT, 0, st>>>(U, ctx->E2S.p, bd.Lm, bd.Lp, gas, L, P.Pvol.p, P.Uf.p, P.Pf.p);
   ctx->launches++;
   if (ev) cudaEventRecord(ev[1], st);
   if (ctx->cfg.parabolic) {

@@ -13,22 +13,49 @@
 
 namespace gx {
 
+// Gas constants.  pref is the reference pressure of the mixed form: there, the pressure held in the
+// primitive arrays is p' = p - pref (computed in FP64 from the FP64 state) and the momentum pressure
+// terms of the volume and surface fluxes use p'.  A constant pressure offset drops out of the full
+// operator for free-stream-preserving metrics, so this is exact in exact arithmetic; it keeps the
+// O(1) pressure differences of low-Mach flows from drowning in FP32 round-off of p ~ 1/(kappa Ma^2).
+// In the FP64 form pref is zero and never applied (kOffset<double> is false).
 template <typename R> struct Gas {
   R kappa, kappaM1, sKappaM1, R_gas, mu, lambda, sR;
+  R pref;
+  double prefD, kappaM1D, sRD;
 };
+template <typename R> struct OffsetOf { static constexpr bool v = false; };
+template <> struct OffsetOf<float> { static constexpr bool v = true; };
 
-template <typename R> __device__ __forceinline__ R rsq(R x) { return sqrt(x); }
-
-// ConsToPrim (idealgas/eos.f90:212-239): (rho, m) -> rho, u, v, w, p, T and 1/rho
+// ConsToPrim (idealgas/eos.f90:212-239) from the FP64 state: rho, u, v, w, p (p' in the mixed form), T, 1/rho
 template <typename R>
-__device__ __forceinline__ void cons_to_prim(const R u[5], const Gas<R>& g, R prim[6], R& srho) {
-  srho = R(1) / u[0];
-  prim[0] = u[0];
-  prim[1] = u[1] * srho;
-  prim[2] = u[2] * srho;
-  prim[3] = u[3] * srho;
-  prim[4] = g.kappaM1 * (u[4] - R(0.5) * (u[1] * prim[1] + u[2] * prim[2] + u[3] * prim[3]));
-  prim[5] = prim[4] * srho * g.sR;
+__device__ __forceinline__ void cons_to_prim_d(const double u[5], const Gas<R>& g, R prim[6], R& srho) {
+  if constexpr (!OffsetOf<R>::v) {
+    srho = R(1) / (R)u[0];
+    prim[0] = (R)u[0];
+    prim[1] = (R)u[1] * srho;
+    prim[2] = (R)u[2] * srho;
+    prim[3] = (R)u[3] * srho;
+    prim[4] = g.kappaM1 * ((R)u[4] - R(0.5) * ((R)u[1] * prim[1] + (R)u[2] * prim[2] + (R)u[3] * prim[3]));
+    prim[5] = prim[4] * srho * g.sR;
+  } else {
+    const double sr = 1. / u[0];
+    const double v1 = u[1] * sr, v2 = u[2] * sr, v3 = u[3] * sr;
+    const double p = g.kappaM1D * (u[4] - 0.5 * (u[1] * v1 + u[2] * v2 + u[3] * v3));
+    srho = (R)sr;
+    prim[0] = (R)u[0];
+    prim[1] = (R)v1;
+    prim[2] = (R)v2;
+    prim[3] = (R)v3;
+    prim[4] = (R)(p - g.prefD);
+    prim[5] = (R)(p * sr * g.sRD);
+  }
+}
+// absolute pressure from the stored one
+template <typename R>
+__device__ __forceinline__ R p_abs(R pstored, const Gas<R>& g) {
+  if constexpr (OffsetOf<R>::v) return pstored + g.pref;
+  else return pstored;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -36,18 +63,28 @@ __device__ __forceinline__ void cons_to_prim(const R u[5], const Gas<R>& g, R pr
 // With Ms = M_a + M_b (the metric sum; the reference averages 0.5*(MRef+M)) and the pair sums
 // rs = rho_a+rho_b, us = u_a+u_b, ..., the reference's  sum_d 0.5*Ms_d * f_d  becomes a
 // function of the contravariant velocity Vs = Ms . us; algebraically identical to the reference.
-// Node data: c = (rho, m1, m2, m3, E), v = (u, v, w), p, aux (H = (E+p)/rho for PI, E/rho for KG).
+// Node data: c = (rho, m1, m2, m3), v = (u, v, w), pm = momentum pressure (p, or p' in the mixed
+// form), aux = the per-node energy quantity of the flux: H=(E+p)/rho (PI), E/rho (KG), E+p (DU, SD),
+// rho*e+p = E - rho|v|^2/2 + p (MO).  pref2 = 2*pref (KG's energy term needs the absolute p sum).
 // ---------------------------------------------------------------------------------------------
 template <typename R>
 struct PairNode {
-  R rho, m1, m2, m3, E, u, v, w, p, aux;
+  R rho, m1, m2, m3, u, v, w, pm, aux;
 };
 
 template <int SPLIT, typename R>
+__device__ __forceinline__ R pair_aux(R rho, R u, R v, R w, R E, R pabs, R srho) {
+  if (SPLIT == DG_SPLIT_PI) return (E + pabs) * srho;
+  if (SPLIT == DG_SPLIT_KG) return E * srho;
+  if (SPLIT == DG_SPLIT_MO) return E - R(0.5) * rho * (u * u + v * v + w * w) + pabs;
+  return E + pabs;  // DU, SD
+}
+
+template <int SPLIT, typename R>
 __device__ __forceinline__ void split_pair_flux(const PairNode<R>& a, const PairNode<R>& b, R Ms0, R Ms1, R Ms2,
-                                                R F[5]) {
+                                                R pref2, R F[5]) {
   if (SPLIT == DG_SPLIT_PI || SPLIT == DG_SPLIT_KG) {
-    const R rs = a.rho + b.rho, us = a.u + b.u, vs = a.v + b.v, ws = a.w + b.w, ps = a.p + b.p;
+    const R rs = a.rho + b.rho, us = a.u + b.u, vs = a.v + b.v, ws = a.w + b.w, ps = a.pm + b.pm;
     const R Vs = Ms0 * us + Ms1 * vs + Ms2 * ws;
     const R q = R(0.125) * rs * Vs;
     const R hp = R(0.5) * ps;
@@ -56,9 +93,9 @@ __device__ __forceinline__ void split_pair_flux(const PairNode<R>& a, const Pair
     F[2] = q * vs + hp * Ms1;
     F[3] = q * ws + hp * Ms2;
     if (SPLIT == DG_SPLIT_PI) F[4] = q * (a.aux + b.aux);
-    else F[4] = q * (a.aux + b.aux) + R(0.25) * ps * Vs;
+    else F[4] = q * (a.aux + b.aux) + R(0.25) * (OffsetOf<R>::v ? ps + pref2 : ps) * Vs;
   } else if (SPLIT == DG_SPLIT_DU) {
-    const R rs = a.rho + b.rho, us = a.u + b.u, vs = a.v + b.v, ws = a.w + b.w, ps = a.p + b.p;
+    const R rs = a.rho + b.rho, us = a.u + b.u, vs = a.v + b.v, ws = a.w + b.w, ps = a.pm + b.pm;
     const R Vs = Ms0 * us + Ms1 * vs + Ms2 * ws;
     const R qv = R(0.25) * Vs;
     const R hp = R(0.5) * ps;
@@ -66,19 +103,19 @@ __device__ __forceinline__ void split_pair_flux(const PairNode<R>& a, const Pair
     F[1] = qv * (a.m1 + b.m1) + hp * Ms0;
     F[2] = qv * (a.m2 + b.m2) + hp * Ms1;
     F[3] = qv * (a.m3 + b.m3) + hp * Ms2;
-    F[4] = qv * (a.E + b.E + ps);
+    F[4] = qv * (a.aux + b.aux);
   } else if (SPLIT == DG_SPLIT_SD) {
     const R Va = Ms0 * a.u + Ms1 * a.v + Ms2 * a.w;
     const R Vb = Ms0 * b.u + Ms1 * b.v + Ms2 * b.w;
     const R ra = a.rho * Va, rb = b.rho * Vb;
-    const R hp = R(0.5) * (a.p + b.p);
+    const R hp = R(0.5) * (a.pm + b.pm);
     F[0] = R(0.5) * (ra + rb);
     F[1] = R(0.5) * (ra * a.u + rb * b.u) + hp * Ms0;
     F[2] = R(0.5) * (ra * a.v + rb * b.v) + hp * Ms1;
     F[3] = R(0.5) * (ra * a.w + rb * b.w) + hp * Ms2;
-    F[4] = R(0.5) * ((a.E + a.p) * Va + (b.E + b.p) * Vb);
+    F[4] = R(0.5) * (a.aux * Va + b.aux * Vb);
   } else {  // DG_SPLIT_MO
-    const R us = a.u + b.u, vs = a.v + b.v, ws = a.w + b.w, ps = a.p + b.p;
+    const R us = a.u + b.u, vs = a.v + b.v, ws = a.w + b.w, ps = a.pm + b.pm;
     const R Va = Ms0 * a.u + Ms1 * a.v + Ms2 * a.w;
     const R Vb = Ms0 * b.u + Ms1 * b.v + Ms2 * b.w;
     const R MsM = Ms0 * (a.m1 + b.m1) + Ms1 * (a.m2 + b.m2) + Ms2 * (a.m3 + b.m3);
@@ -88,10 +125,9 @@ __device__ __forceinline__ void split_pair_flux(const PairNode<R>& a, const Pair
     F[2] = R(0.25) * MsM * vs + hp * Ms1;
     F[3] = R(0.25) * MsM * ws + hp * Ms2;
     const R ka = a.u * a.u + a.v * a.v + a.w * a.w, kb = b.u * b.u + b.v * b.v + b.w * b.w;
-    const R repa = a.E - R(0.5) * a.rho * ka + a.p, repb = b.E - R(0.5) * b.rho * kb + b.p;
     const R ra = a.rho * Va, rb = b.rho * Vb;
     const R dota = a.u * us + a.v * vs + a.w * ws, dotb = b.u * us + b.v * vs + b.w * ws;
-    F[4] = R(0.5) * (repa * Va + repb * Vb + R(0.5) * (ra * dota + rb * dotb) - R(0.5) * (ra * ka + rb * kb));
+    F[4] = R(0.5) * (a.aux * Va + b.aux * Vb + R(0.5) * (ra * dota + rb * dotb) - R(0.5) * (ra * ka + rb * kb));
   }
 }
 
@@ -100,7 +136,7 @@ __device__ __forceinline__ void split_pair_flux(const PairNode<R>& a, const Pair
 // ---------------------------------------------------------------------------------------------
 template <typename R>
 struct Ext {
-  R rho, srho, m1, m2, m3, E, v1, v2, v3, p;
+  R rho, srho, m1, m2, m3, E, v1, v2, v3, p, pm;  // p absolute, pm the momentum pressure (p or p')
 };
 
 // Split surface fluxes (splitflux.f90:270-761), the central part of the split-form Riemann solvers
@@ -109,14 +145,14 @@ __device__ __forceinline__ void split_surface_flux(int split, const Ext<R>& L, c
   switch (split) {
     case DG_SPLIT_SD:
       F[0] = R(0.5) * (L.m1 + Rr.m1);
-      F[1] = R(0.5) * (L.m1 * L.v1 + L.p + Rr.m1 * Rr.v1 + Rr.p);
+      F[1] = R(0.5) * (L.m1 * L.v1 + L.pm + Rr.m1 * Rr.v1 + Rr.pm);
       F[2] = R(0.5) * (L.m1 * L.v2 + Rr.m1 * Rr.v2);
       F[3] = R(0.5) * (L.m1 * L.v3 + Rr.m1 * Rr.v3);
       F[4] = R(0.5) * ((L.E + L.p) * L.v1 + (Rr.E + Rr.p) * Rr.v1);
       break;
     case DG_SPLIT_DU:
       F[0] = R(0.25) * (L.rho + Rr.rho) * (L.v1 + Rr.v1);
-      F[1] = R(0.25) * (L.m1 + Rr.m1) * (L.v1 + Rr.v1) + R(0.5) * (L.p + Rr.p);
+      F[1] = R(0.25) * (L.m1 + Rr.m1) * (L.v1 + Rr.v1) + R(0.5) * (L.pm + Rr.pm);
       F[2] = R(0.25) * (L.m2 + Rr.m2) * (L.v1 + Rr.v1);
       F[3] = R(0.25) * (L.m3 + Rr.m3) * (L.v1 + Rr.v1);
       F[4] = R(0.25) * (L.E + Rr.E + L.p + Rr.p) * (L.v1 + Rr.v1);
@@ -125,7 +161,7 @@ __device__ __forceinline__ void split_surface_flux(int split, const Ext<R>& L, c
       const R eL = L.E * L.srho, eR = Rr.E * Rr.srho;
       const R rs = L.rho + Rr.rho, us = L.v1 + Rr.v1;
       F[0] = R(0.25) * rs * us;
-      F[1] = R(0.125) * rs * us * us + R(0.5) * (L.p + Rr.p);
+      F[1] = R(0.125) * rs * us * us + R(0.5) * (L.pm + Rr.pm);
       F[2] = R(0.125) * rs * us * (L.v2 + Rr.v2);
       F[3] = R(0.125) * rs * us * (L.v3 + Rr.v3);
       F[4] = R(0.125) * rs * (eL + eR) * us + R(0.25) * (L.p + Rr.p) * us;
@@ -135,7 +171,7 @@ __device__ __forceinline__ void split_surface_flux(int split, const Ext<R>& L, c
       const R rR = Rr.E - R(0.5) * Rr.rho * (Rr.v1 * Rr.v1 + Rr.v2 * Rr.v2 + Rr.v3 * Rr.v3) + Rr.p;
       const R ms = L.m1 + Rr.m1;
       F[0] = R(0.5) * ms;
-      F[1] = R(0.25) * ms * (L.v1 + Rr.v1) + R(0.5) * (L.p + Rr.p);
+      F[1] = R(0.25) * ms * (L.v1 + Rr.v1) + R(0.5) * (L.pm + Rr.pm);
       F[2] = R(0.25) * ms * (L.v2 + Rr.v2);
       F[3] = R(0.25) * ms * (L.v3 + Rr.v3);
       F[4] = R(0.5) * (rL * L.v1 + rR * Rr.v1) +
@@ -150,7 +186,7 @@ __device__ __forceinline__ void split_surface_flux(int split, const Ext<R>& L, c
       const R HL = (L.E + L.p) * L.srho, HR = (Rr.E + Rr.p) * Rr.srho;
       const R rs = L.rho + Rr.rho, us = L.v1 + Rr.v1;
       F[0] = R(0.25) * rs * us;
-      F[1] = R(0.125) * rs * us * us + R(0.5) * (L.p + Rr.p);
+      F[1] = R(0.125) * rs * us * us + R(0.5) * (L.pm + Rr.pm);
       F[2] = R(0.125) * rs * us * (L.v2 + Rr.v2);
       F[3] = R(0.125) * rs * us * (L.v3 + Rr.v3);
       F[4] = R(0.125) * rs * (HL + HR) * us;
@@ -162,7 +198,7 @@ __device__ __forceinline__ void split_surface_flux(int split, const Ext<R>& L, c
 template <typename R>
 __device__ __forceinline__ void euler_flux_1d(const Ext<R>& U, R F[5]) {
   F[0] = U.m1;
-  F[1] = U.m1 * U.v1 + U.p;
+  F[1] = U.m1 * U.v1 + U.pm;
   F[2] = U.m1 * U.v2;
   F[3] = U.m1 * U.v3;
   F[4] = (U.E + U.p) * U.v1;
@@ -337,15 +373,16 @@ __device__ __forceinline__ void riemann_solver(int riemann, int split, const Ext
 // Riemann (riemann.f90:216-289): rotate (u,v,w) into (n,t1,t2), solve, back-rotate momentum
 template <typename R>
 __device__ __forceinline__ void riemann_face(int riemann, int split, const R UL[5], const R UR[5], const R PL[6],
-                                             const R PR[6], const R nv[3], const R t1[3], const R t2[3], R kappa,
-                                             R Fout[5]) {
+                                             const R PR[6], const R nv[3], const R t1[3], const R t2[3],
+                                             const Gas<R>& gas, R Fout[5]) {
+  const R kappa = gas.kappa;
   Ext<R> L, Rr;
-  L.rho = UL[0]; L.srho = R(1) / L.rho; L.E = UL[4]; L.p = PL[4];
+  L.rho = UL[0]; L.srho = R(1) / L.rho; L.E = UL[4]; L.pm = PL[4]; L.p = p_abs(PL[4], gas);
   L.v1 = PL[1] * nv[0] + PL[2] * nv[1] + PL[3] * nv[2];
   L.v2 = PL[1] * t1[0] + PL[2] * t1[1] + PL[3] * t1[2];
   L.v3 = PL[1] * t2[0] + PL[2] * t2[1] + PL[3] * t2[2];
   L.m1 = L.rho * L.v1; L.m2 = L.rho * L.v2; L.m3 = L.rho * L.v3;
-  Rr.rho = UR[0]; Rr.srho = R(1) / Rr.rho; Rr.E = UR[4]; Rr.p = PR[4];
+  Rr.rho = UR[0]; Rr.srho = R(1) / Rr.rho; Rr.E = UR[4]; Rr.pm = PR[4]; Rr.p = p_abs(PR[4], gas);
   Rr.v1 = PR[1] * nv[0] + PR[2] * nv[1] + PR[3] * nv[2];
   Rr.v2 = PR[1] * t1[0] + PR[2] * t1[1] + PR[3] * t1[2];
   Rr.v3 = PR[1] * t2[0] + PR[2] * t2[1] + PR[3] * t2[2];

@@ -125,8 +125,11 @@ class DG:
     U, Ut, Ut_tmp are torch float64 CUDA tensors of shape (nElems, n, n, n, 5) (reference layout).
     """
 
-    def __init__(self, cfg, mesh):
+    def __init__(self, cfg, mesh, pressure_offset=None):
+        """pressure_offset: reference pressure of the mixed form (dg_set_pressure_offset); None picks
+        the volume-mean pressure of the first state this operator sees (mixed form only)."""
         import torch  # device memory and streams only
+        self._pref = pressure_offset
         self._torch = torch
         self.cfg = cfg
         self.mesh = mesh
@@ -139,6 +142,21 @@ class DG:
                                 _ptr(m.Metrics_hTilde), _ptr(m.sJ), _ptr(m.NormVec), _ptr(m.TangVec1),
                                 _ptr(m.TangVec2), _ptr(m.SurfElem), _ptr(m.ElemToSide), _ptr(m.SideToElem)),
                   "dg_set_mesh")
+        if pressure_offset is not None:
+            nat.check(L.dg_set_pressure_offset(h, float(pressure_offset)), "dg_set_pressure_offset")
+
+    def _auto_offset(self, U):
+        if self._pref is not None or self.cfg.precision != nat.DG_PRECISION_MIXED:
+            return
+        torch = self._torch
+        m = self.mesh
+        w = torch.from_numpy(basis(m.N, m.node_type)["wGP"]).to(U.device)
+        W = w[None, :, None, None] * w[None, None, :, None] * w[None, None, None, :]
+        J = W / torch.from_numpy(m.sJ).to(U.device)
+        kin = 0.5 * (U[..., 1] ** 2 + U[..., 2] ** 2 + U[..., 3] ** 2) / U[..., 0]
+        p = (self.cfg.kappa - 1.0) * (U[..., 4] - kin)
+        self._pref = float((p * J).sum() / J.sum())
+        nat.check(nat.lib().dg_set_pressure_offset(self._h, self._pref), "dg_set_pressure_offset")
 
     def close(self):
         if getattr(self, "_h", None):
@@ -179,6 +197,7 @@ class DG:
         if Ut is None:
             Ut = self._torch.empty_like(U)
         self._check_state(Ut)
+        self._auto_offset(U)
         nat.check(nat.lib().dg_rhs(self._h, float(t), ctypes.c_void_p(U.data_ptr()), ctypes.c_void_p(Ut.data_ptr()),
                                    self._stream(stream)), "dg_rhs")
         return Ut
@@ -187,6 +206,7 @@ class DG:
         """nSteps Carpenter RK4-5 steps of size dt in place (src/timedisc/timestep.f90:49-120)."""
         self._check_state(U)
         self._check_state(Ut_tmp)
+        self._auto_offset(U)
         nat.check(nat.lib().dg_lserk_steps(self._h, float(t), float(dt), int(nSteps), ctypes.c_void_p(U.data_ptr()),
                                            ctypes.c_void_p(Ut_tmp.data_ptr()), self._stream(stream)),
                   "dg_lserk_steps")

@@ -152,6 +152,13 @@ int dg_calc_timestep(dg_ctx* ctx, const double* d_U, double cfl_scale, double df
  * receives the number of bad nodes.  Synchronises the stream. */
 int dg_check_state(dg_ctx* ctx, const double* d_U, long long* bad_count, void* stream);
 
+/* Reference pressure of the mixed form (no counterpart in the reference).  With p_ref > 0 the FP32
+ * bulk works with p' = p - p_ref (formed in FP64 from the FP64 state) in the momentum pressure terms
+ * of the volume and surface fluxes.  The constant p_ref drops out of the operator for
+ * free-stream-preserving metrics, so results are unchanged in exact arithmetic, while low-Mach
+ * pressure differences keep FP32 precision.  Ignored by the FP64 form.  Default 0. */
+int dg_set_pressure_offset(dg_ctx* ctx, double p_ref);
+
 /* Measurement utilities (no counterpart in the reference).
  * dg_profile_stage: run `reps` LSERK stages on d_U / d_Ut_tmp (modified in place) with CUDA events
  * around each kernel; ms_out[0..4] = average ms of (prolong, lift, face, volume, whole stage).
