@@ -35,8 +35,8 @@ ALG_FLOPS_N7 = {"prolong": 14.0, "lift": 30 * 8 + 75 + 270 / 8 + 15, "face": 120
                 "volume": 135 * 7 + 115 + 30 * 8 + 60 / 8 + 30}
 ALG_BYTES_N7 = 510.0  # compulsory HBM bytes per DOF-stage of a fully fused implementation (FP64)
 TGV_R = 71.42857
-CFL = 0.9
-DFL = 0.9
+CFL = 0.8  # CFLscale / DFLscale of the reference's TGV regression (regressioncheck/checks/tgv/split/parameter.ini)
+DFL = 0.8
 
 
 def parse():

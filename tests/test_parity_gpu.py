@@ -104,10 +104,10 @@ def test_free_stream_preservation_curved():
 
 def test_lserk_100_steps_matches_oracle():
     cfg = gx.config(N=5, Riemann="roe", SplitDG="pi", parabolic=True, mu0=6.25e-4, R=71.42857)
-    m, U0 = tgv_case(5, 2, 2, 2)
+    m, U0 = tgv_case(5, 3, 3, 3)
     op = gx.DG(cfg, m)
     U = torch.from_numpy(U0).cuda()
-    dt, err = op.CalcTimeStep(U, 0.9, 0.9)
+    dt, err = op.CalcTimeStep(U, 0.5, 0.5)
     assert err == 0
     Ut_tmp = torch.zeros_like(U)
     op.TimeStepByLSERKW2(0.0, dt, U, Ut_tmp, nSteps=100)
@@ -149,16 +149,16 @@ def kinetic_energy(mesh, U):
 
 
 def test_mixed_precision_run_close_to_fp64():
-    """Mixed form (FP32 bulk, FP64 RK accumulation) vs the FP64 oracle after 20 TGV steps:
-    relative kinetic-energy error <= 1e-6, relative L2 of U and total-mass drift stated."""
+    """Mixed form (FP32 bulk, FP64 RK accumulation) vs the FP64 oracle after 30 TGV steps at
+    CFL 0.5: relative kinetic-energy error <= 1e-6; relative L2 of U and total-mass drift stated."""
     kw = dict(Riemann="roe", SplitDG="pi", parabolic=True, mu0=6.25e-4, R=71.42857)
-    m, U0 = tgv_case(7, 2, 2, 2)
+    m, U0 = tgv_case(7, 3, 3, 3)
     cfg = gx.config(N=7, **kw)
-    dt, _ = Oracle(cfg, m).calc_timestep(U0, 0.9, 0.9)
-    ref, _ = Oracle(cfg, m).lserk_steps(U0, dt, 20)
+    dt, _ = Oracle(cfg, m).calc_timestep(U0, 0.5, 0.5)
+    ref, _ = Oracle(cfg, m).lserk_steps(U0, dt, 30)
     op = gx.DG(gx.config(N=7, precision="mixed", **kw), m)
     U = torch.from_numpy(U0).cuda()
-    op.TimeStepByLSERKW2(0.0, dt, U, torch.zeros_like(U), nSteps=20)
+    op.TimeStepByLSERKW2(0.0, dt, U, torch.zeros_like(U), nSteps=30)
     Um = U.cpu().numpy()
     ke_err = abs(kinetic_energy(m, Um) - kinetic_energy(m, ref)) / kinetic_energy(m, ref)
     w = gx.basis(7, 2)["wGP"]
