@@ -148,6 +148,30 @@ int dg_lserk_steps(dg_ctx* ctx, double t, double dt, int nSteps, double* d_U, do
 int dg_calc_timestep(dg_ctx* ctx, const double* d_U, double cfl_scale, double dfl_scale,
                      double* dt_out, void* stream);
 
+/* Allocation-free time step (no counterpart in the reference).
+ *
+ * Some callers cannot allocate device memory: a host code whose device arrays all belong to another
+ * runtime's allocator (GALAEXI's CUDA Fortran arrays live in nvfortran's heap), a process that must
+ * keep a fixed device-memory budget once its time loop has started, or a loop that cannot afford the
+ * device-wide synchronisation cudaMalloc/cudaFree may imply.  For them this entry point computes the
+ * same dt as dg_calc_timestep without a context and without any allocation: the caller passes the
+ * state and the metric arrays it already holds on the device, in the reference layouts
+ * U(5,0:N,0:N,0:N,nElems), Metrics_f/g/hTilde(3,0:N,0:N,0:N,nElems), sJ(0:N,0:N,0:N,nElems), and the
+ * scratch comes from a static device array of the library (DG_NOALLOC_MAX_ELEMS eigenvalue pairs,
+ * 8 MiB, held on every GPU that loads the library until the process exits).
+ *   - nElems above DG_NOALLOC_MAX_ELEMS is rejected with DG_ERR_ARG.
+ *   - The first call on a device looks up the device address of the static array for that device
+ *     (cudaGetSymbolAddress); make that first call before any stream capture on that device.
+ *   - Every call uses the same static array; the previous call's contents stay in it (the error
+ *     counter is cleared at the start of each call).  Calls whose work overlaps on the GPU (other
+ *     streams, other host threads) race on that array: serialise them.
+ * Synchronises the stream; returns DG_ERR_NAN for NaN/Inf or non-positive density/pressure. */
+#define DG_NOALLOC_MAX_ELEMS (1 << 19)
+int dg_calc_timestep_noalloc(int N, int node_type, int nElems, int parabolic, double kappa, double mu0, double Pr,
+                             const double* d_U, const double* d_metrics_f, const double* d_metrics_g,
+                             const double* d_metrics_h, const double* d_sJ, double cfl_scale, double dfl_scale,
+                             double* dt_out, void* stream);
+
 /* Scan the state for NaN/Inf or non-positive density/pressure; *bad_count
  * receives the number of bad nodes.  Synchronises the stream. */
 int dg_check_state(dg_ctx* ctx, const double* d_U, long long* bad_count, void* stream);
