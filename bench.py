@@ -34,6 +34,12 @@ WORKLOADS = {
 ALG_FLOPS_N7 = {"prolong": 14.0, "lift": 30 * 8 + 75 + 270 / 8 + 15, "face": 1200 / 8,
                 "volume": 135 * 7 + 115 + 30 * 8 + 60 / 8 + 30}
 ALG_BYTES_N7 = 510.0  # compulsory HBM bytes per DOF-stage of a fully fused implementation (FP64)
+# ncu on the 16^3 case of the same kernels (profiles/dgsem_fp64_kernels_tgv_n7_16cube.md): DRAM bytes
+# and executed FP64 thread-instructions (DFMA+DADD+DMUL) per DOF for one k_volume launch; traffic
+# grows with the number of elements, so it is scaled to a launch by nDOF
+KVOL_DRAM_BYTES_PER_DOF = (669.970688e6 + 144.893696e6) / 2097152
+KVOL_FP64_INSTR_PER_DOF = 548.3
+FP64_ISSUE_PER_CYCLE = 304  # sm__sass_thread_inst_executed_op_dfma_pred_on.sum.peak_sustained (152 SMs x 2)
 TGV_R = 71.42857
 CFL = 0.8  # CFLscale / DFLscale of the reference's TGV regression (regressioncheck/checks/tgv/split/parameter.ini)
 DFL = 0.8
@@ -283,7 +289,10 @@ def profile_roofline(args, op, U, dt, stream, nDOF):
         "achieved": achieved, "peak": peak * 1e-3, "unit": "TFLOP/s", "frac": achieved / (peak * 1e-3),
         "peak_source": "FMA-chain microkernel measured in this run (no FP64/FP32 CUDA-core peak in MEASURED_PEAKS.json)",
         "alg_flops_per_dof": ALG_FLOPS_N7["volume"],
-        "traffic": None,
+        "traffic": KVOL_DRAM_BYTES_PER_DOF * nDOF if args.precision == "fp64" else None,
+        "traffic_source": "ncu dram__bytes_read+write of one k_volume launch on 16^3, scaled by nDOF",
+        "exec_fp64_issue_frac": (KVOL_FP64_INSTR_PER_DOF * nDOF / (kms["volume"] * 1e-3))
+                                / (FP64_ISSUE_PER_CYCLE * 2.07e9) if args.precision == "fp64" else None,
         "kernel_ms": kms,
         "stage": {"alg_flops_per_dof_stage": sum(ALG_FLOPS_N7.values()),
                   "achieved_tflops": sum(ALG_FLOPS_N7.values()) * nDOF / stage_s * 1e-12,
