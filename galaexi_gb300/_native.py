@@ -75,6 +75,7 @@ _SIGS = {
     "dg_calc_timestep": (_I, [_P, _P, _D, _D, _DP, _P]),
     "dg_check_state": (_I, [_P, _P, ctypes.POINTER(ctypes.c_longlong), _P]),
     "dg_kernel_launch_count": (ctypes.c_longlong, [_P]),
+    "dg_get_gradients": (_I, [_P, _P, _P, _P, _P]),
     "dg_last_error": (ctypes.c_char_p, []),
     "dg_basis": (_I, [_I, _I] + [_P] * 10),
     "dg_mesh_cartesian_sizes": (_I, [_I, _I, _I, _IP, _IP]),

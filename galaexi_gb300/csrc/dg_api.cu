@@ -85,7 +85,27 @@ int upload_basis(dg_ctx* ctx, gxc::PrecData<R>& P) {
 int run_rhs(dg_ctx* ctx, const double* U, gx::RKArgs rk, int rkmode, cudaStream_t st) {
   const gxc::NPTable* T = table_for(ctx->n);
   if (!T) { set_error("unsupported N"); return DG_ERR_UNSUPPORTED; }
-  return ctx->cfg.precision == DG_PRECISION_FP64 ? T->rhs_d(ctx, U, rk, rkmode, st) : T->rhs_f(ctx, U, rk, rkmode, st);
+  const int rc = ctx->cfg.precision == DG_PRECISION_FP64 ? T->rhs_d(ctx, U, rk, rkmode, st)
+                                                         : T->rhs_f(ctx, U, rk, rkmode, st);
+  ctx->grad_ok = rc == DG_OK && ctx->cfg.parabolic;
+  return rc;
+}
+
+// Gvol [e][d*5+v][node] (d = x,y,z; v = rho,u,v,w,T) -> GradUx/y/z(v, node, e) in FP64
+template <typename R>
+__global__ void __launch_bounds__(256) k_export_grad(const R* __restrict__ G, long long nNodes, int n3,
+                                                     double* __restrict__ gx_, double* __restrict__ gy_,
+                                                     double* __restrict__ gz_) {
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < nNodes;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long e = idx / n3, node = idx - e * n3;
+    const R* g = G + e * 15 * n3 + node;
+    double* out[3] = {gx_, gy_, gz_};
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+      for (int v = 0; v < 5; ++v) out[d][idx * 5 + v] = (double)g[(d * 5 + v) * n3];
+  }
 }
 
 template <typename R>
@@ -214,7 +234,11 @@ int dg_ctx_create(const dg_config* cfg, dg_ctx** out) {
   }
   if (cfg->split_dg < 0 && cfg->riemann == DG_RIEMANN_AVERAGE) { set_error("Riemann=avg needs SplitDG"); return DG_ERR_ARG; }
   if (cfg->split_dg >= 0 && cfg->N < 2) { set_error("split form needs N >= 2"); return DG_ERR_UNSUPPORTED; }
-  if (cfg->parabolic && cfg->lifting != DG_LIFTING_BR1) { set_error("only BR1 lifting is built"); return DG_ERR_UNSUPPORTED; }
+  if (cfg->lifting != DG_LIFTING_BR1 && cfg->lifting != DG_LIFTING_BR2) { set_error("bad lifting"); return DG_ERR_ARG; }
+  if (cfg->parabolic && cfg->lifting == DG_LIFTING_BR2 && cfg->do_weak_lifting) {
+    // the BR2 lifting is always in strong form (lifting.f90:103)
+    set_error("BR2 lifting is strong-form only: doWeakLifting must be F"); return DG_ERR_ARG;
+  }
   if (!(cfg->kappa > 1.) || !(cfg->R > 0.)) { set_error("bad kappa or R"); return DG_ERR_ARG; }
   if (cfg->parabolic && !(cfg->Pr > 0.)) { set_error("bad Pr"); return DG_ERR_ARG; }
   if (cfg->precision != DG_PRECISION_FP64 && cfg->precision != DG_PRECISION_MIXED) { set_error("bad precision"); return DG_ERR_ARG; }
@@ -311,6 +335,7 @@ int dg_set_mesh(dg_ctx* ctx, int nElems, int nSides, int nBCSides, const double*
   CUDA_TRY(cudaMemcpy(ctx->MetD.p, met.data(), met.size() * sizeof(double), cudaMemcpyHostToDevice), "upload metrics");
   CUDA_TRY(cudaMemcpy(ctx->E2S.p, he2s.data(), he2s.size() * sizeof(int), cudaMemcpyHostToDevice), "upload E2S");
   ctx->mesh_ok = true;
+  ctx->grad_ok = false;
   return DG_OK;
 }
 
@@ -382,6 +407,24 @@ int dg_check_state(dg_ctx* ctx, const double* d_U, long long* bad_count, void* s
   CUDA_TRY(cudaStreamSynchronize(st), "sync check");
   *bad_count = (long long)bad;
   return bad ? DG_ERR_NAN : DG_OK;
+}
+
+int dg_get_gradients(dg_ctx* ctx, double* d_gradUx, double* d_gradUy, double* d_gradUz, void* stream) {
+  if (int rc = check_ctx(ctx, true)) return rc;
+  if (!d_gradUx || !d_gradUy || !d_gradUz) { set_error("dg_get_gradients: null argument"); return DG_ERR_ARG; }
+  if (!ctx->cfg.parabolic) { set_error("dg_get_gradients: operator is not parabolic"); return DG_ERR_UNSUPPORTED; }
+  if (!ctx->grad_ok) { set_error("dg_get_gradients: no RHS evaluated on this mesh yet"); return DG_ERR_ARG; }
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long nNodes = (long long)ctx->nElems * ctx->n3;
+  int grid = (int)((nNodes + 255) / 256);
+  if (grid > 152 * 16) grid = 152 * 16;
+  if (ctx->cfg.precision == DG_PRECISION_FP64)
+    k_export_grad<double><<<grid, 256, 0, st>>>(ctx->d.Gvol.p, nNodes, ctx->n3, d_gradUx, d_gradUy, d_gradUz);
+  else
+    k_export_grad<float><<<grid, 256, 0, st>>>(ctx->f.Gvol.p, nNodes, ctx->n3, d_gradUx, d_gradUy, d_gradUz);
+  ctx->launches++;
+  CUDA_TRY(cudaGetLastError(), "k_export_grad launch");
+  return DG_OK;
 }
 
 long long dg_kernel_launch_count(const dg_ctx* ctx) { return ctx ? ctx->launches : 0; }

@@ -82,7 +82,8 @@ struct dg_ctx {
   gxc::DBuf<unsigned long long> bad;
   long long launches = 0;
   bool mesh_ok = false;
-  double pref = 0.;        // reference pressure of the mixed form (dg_set_pressure_offset)
+  bool grad_ok = false;    // Gvol holds the lifted gradients of the last RHS evaluation
+  double pref = 0.;       // reference pressure of the mixed form (dg_set_pressure_offset)
 };
 
 namespace gxc {
@@ -96,6 +97,8 @@ inline gx::Launch make_launch(const dg_ctx* ctx) {
   L.split = ctx->cfg.split_dg;
   L.parabolic = ctx->cfg.parabolic;
   L.lift_mode = ctx->cfg.do_weak_lifting ? 2 : (ctx->cfg.do_conservative_lifting ? 1 : 0);
+  L.br2 = ctx->cfg.lifting == DG_LIFTING_BR2 ? 1 : 0;
+  L.eta_br2 = ctx->cfg.eta_br2;
   return L;
 }
 

@@ -95,6 +95,8 @@ struct Launch {
   int gauss;        // 1: Gauss nodes (prolongation by interpolation), 0: Gauss-Lobatto
   int riemann, split, parabolic;
   int lift_mode;    // 0: strong non-conservative, 1: strong conservative, 2: weak
+  int br2;          // 1: BR2 face traces (lifting_br2.t90:191-310), strong form only
+  double eta_br2;   // BR2 penalty etaBR2
 };
 
 template <int NP> struct EPBof { static constexpr int v = (NP * NP * NP >= 128) ? 1 : (256 / (NP * NP * NP)); };
@@ -241,6 +243,14 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
         for (int v = 0; v < 5; ++v) g[d][v] = sj * g[d][v];
       }
     }
+    if (L.br2) {
+      // BR2: the face traces prolong the volume part only (ApplyJacobianLifting before
+      // ProlongToFaceLifting, lifting_br2.t90:120-147)
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int v = 0; v < 5; ++v) Gs[el][d * 5 + v][node] = g[d][v];
+    }
     // surface part (SurfInt_Device_Single_Flux, surfint.t90:591-725) of the BR1 flux
     // 0.5*SurfElem*(sig*U_master + U_slave) (Lifting_FillFlux, lifting_fillflux.t90:39-103) times the
     // normal (Lifting_FillFlux_NormVec, :212-256) times L_hat and the Jacobian; the scalar factors of
@@ -286,7 +296,7 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
         const R val = g[d][v];
-        Gs[el][d * 5 + v][node] = val;
+        if (!L.br2) Gs[el][d * 5 + v][node] = val;
         G[(d * 5 + v) * n3] = val;
       }
   }
@@ -303,18 +313,39 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
     s2v2(N, p, q, flip, ls, a, b);
     const int slot = (flip == 0) ? 0 : 1;
     R* gf = Gf + ((size_t)slot * L.nSides + side) * 15 * n2 + pq;
-    if (!L.gauss) {
-      int node = face_node(n, ls, a, b, is_minus(ls) ? 0 : N);
-#pragma unroll
-      for (int c = 0; c < 15; ++c) gf[c * n2] = Gs[el][c][node];
-    } else {
+    // BR2 (Lifting_SurfInt_BR2, lifting_br2.t90:191-310): the trace also gets etaBR2 times the
+    // lifting of this face's own strong flux 0.5*SurfElem*(U_slave - U_master)*n, prolonged back:
+    // eta * Flux * sum_l L(l) * Lhat(l) * sJ(l) over the line normal to the face (GL: face node only)
+    R bw = R(0);
+    const R* pm = nullptr;
+    const R* ps = nullptr;
+    const R* fg = nullptr;
+    if (L.br2) {
       const R* Lv = is_minus(ls) ? sb.Lm : sb.Lp;
-      for (int c = 0; c < 15; ++c) {
-        R s = Gs[el][c][face_node(n, ls, a, b, 0)] * Lv[0];
+      const R* Lh = is_minus(ls) ? sb.Lhm : sb.Lhp;
+      const R* sJe = Met + ((size_t)e * 10 + 9) * n3;
+      const int l0 = L.gauss ? 0 : (is_minus(ls) ? 0 : N), l1 = L.gauss ? N : l0;
+      for (int l = l0; l <= l1; ++l) bw = bw + Lv[l] * Lh[l] * sJe[face_node(n, ls, a, b, l)];
+      fg = Fgeo + (size_t)side * 10 * n2 + pq;
+      bw = R(L.eta_br2) * R(0.5) * fg[9 * n2] * bw;
+      pm = Pf + (size_t)side * 6 * n2 + pq;
+      ps = Pf + ((size_t)L.nSides + side) * 6 * n2 + pq;
+    }
+    for (int c = 0; c < 15; ++c) {
+      R s;
+      if (!L.gauss) {
+        s = Gs[el][c][face_node(n, ls, a, b, is_minus(ls) ? 0 : N)];
+      } else {
+        const R* Lv = is_minus(ls) ? sb.Lm : sb.Lp;
+        s = Gs[el][c][face_node(n, ls, a, b, 0)] * Lv[0];
 #pragma unroll
         for (int l = 1; l < n; ++l) s = s + Gs[el][c][face_node(n, ls, a, b, l)] * Lv[l];
-        gf[c * n2] = s;
       }
+      if (L.br2) {
+        const int d = c / 5, v = c - 5 * d;
+        s = s + bw * (ps[liftc[v] * n2] - pm[liftc[v] * n2]) * fg[d * n2];
+      }
+      gf[c * n2] = s;
     }
   }
 }

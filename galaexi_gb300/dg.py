@@ -224,6 +224,17 @@ class DG:
         nat.check(rc, "dg_calc_timestep")
         return dt.value, 0
 
+    def gradients(self, stream=None):
+        """Lifted gradients (GradUx, GradUy, GradUz) of the last RHS evaluation, each a float64 CUDA
+        tensor (nElems, n, n, n, 5) over the lifting variables (rho, u, v, w, T)."""
+        torch = self._torch
+        m = self.mesh
+        n = self.cfg.N + 1
+        g = [torch.empty((m.nElems, n, n, n, 5), dtype=torch.float64, device="cuda") for _ in range(3)]
+        nat.check(nat.lib().dg_get_gradients(self._h, *[ctypes.c_void_p(x.data_ptr()) for x in g],
+                                             self._stream(stream)), "dg_get_gradients")
+        return tuple(g)
+
     def check_state(self, U, stream=None):
         """Number of nodes holding NaN/Inf or non-positive density/pressure."""
         self._check_state(U)

@@ -176,6 +176,14 @@ int dg_calc_timestep_noalloc(int N, int node_type, int nElems, int parabolic, do
  * receives the number of bad nodes.  Synchronises the stream. */
 int dg_check_state(dg_ctx* ctx, const double* d_U, long long* bad_count, void* stream);
 
+/* Lifted gradients of the last RHS evaluation (dg_rhs or the last stage of dg_lserk_step[s]):
+ * the reference's GradUx/GradUy/GradUz(PP_nVarLifting=5, 0:N,0:N,0:N, nElems) module arrays
+ * (lifting_vars.f90), lifting variables (rho, u, v, w, T) = LIFT_DENS..LIFT_TEMP (eos.h:136-142),
+ * which the reference's analysis routines read (testcase/taylorgreenvortex/testcase.f90:283-510).
+ * Each output is a device array of 5*(N+1)^3*nElems doubles; the mixed form converts from FP32.
+ * DG_ERR_UNSUPPORTED for a non-parabolic operator, DG_ERR_ARG before the first RHS on the mesh. */
+int dg_get_gradients(dg_ctx* ctx, double* d_gradUx, double* d_gradUy, double* d_gradUz, void* stream);
+
 /* Reference pressure of the mixed form (no counterpart in the reference).  With p_ref > 0 the FP32
  * bulk works with p' = p - p_ref (formed in FP64 from the FP64 state) in the momentum pressure terms
  * of the volume and surface fluxes.  The constant p_ref drops out of the operator for

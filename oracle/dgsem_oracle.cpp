@@ -1001,27 +1001,9 @@ static inline double thermal_conductivity(const dg_config& c, double mu) {
   return mu * c.R * c.kappa / ((c.kappa - 1.) * c.Pr);
 }
 
-// Lifting_BR1  src/dg/lifting/lifting_br1.t90:47-167 (no BC sides, no MPI)
-static void Lifting_BR1(const Ctx& C, Work& W) {
+// Volume part of the lifting (gradients in physical space without the Jacobian factor)
+static void Lifting_VolInt(const Ctx& C, Work& W, bool weak) {
   const int N = C.B.N, n = C.n;
-  const size_t nF = (size_t)C.n2 * C.M.nSides;
-  const bool weak = C.cfg.do_weak_lifting != 0;
-  // Lifting_FillFlux  lifting_fillflux.t90:39-103
-  double sig = weak ? 1. : -1.;
-#pragma omp parallel for schedule(static)
-  for (long long fidx = 0; fidx < (long long)nF; ++fidx)
-    for (int iv = 0; iv < 5; ++iv)
-      W.liftflux[iv + 5 * fidx] = 0.5 * C.M.SurfElem[fidx] *
-                                  (sig * W.UPrim_master[PRIM_LIFT[iv] + 6 * fidx] + W.UPrim_slave[PRIM_LIFT[iv] + 6 * fidx]);
-  // Lifting_FillFlux_NormVec  lifting_fillflux.t90:212-256 (stored in gradU*_master)
-#pragma omp parallel for schedule(static)
-  for (long long fidx = 0; fidx < (long long)nF; ++fidx)
-    for (int iv = 0; iv < 5; ++iv) {
-      W.gx_m[iv + 5 * fidx] = W.liftflux[iv + 5 * fidx] * C.M.nv[0 + 3 * fidx];
-      W.gy_m[iv + 5 * fidx] = W.liftflux[iv + 5 * fidx] * C.M.nv[1 + 3 * fidx];
-      W.gz_m[iv + 5 * fidx] = W.liftflux[iv + 5 * fidx] * C.M.nv[2 + 3 * fidx];
-    }
-  // volume integral
   if (weak || C.cfg.do_conservative_lifting) {
     // Lifting_VolInt_Conservative  lifting_volint.t90:345-455
     const std::vector<double>& DM = weak ? C.B.D_Hat_T : C.B.D_T;
@@ -1075,6 +1057,29 @@ static void Lifting_BR1(const Ctx& C, Work& W) {
         }
       }
   }
+}
+
+// Lifting_BR1  src/dg/lifting/lifting_br1.t90:47-167 (no BC sides, no MPI)
+static void Lifting_BR1(const Ctx& C, Work& W) {
+  const int N = C.B.N, n = C.n;
+  const size_t nF = (size_t)C.n2 * C.M.nSides;
+  const bool weak = C.cfg.do_weak_lifting != 0;
+  // Lifting_FillFlux  lifting_fillflux.t90:39-103
+  double sig = weak ? 1. : -1.;
+#pragma omp parallel for schedule(static)
+  for (long long fidx = 0; fidx < (long long)nF; ++fidx)
+    for (int iv = 0; iv < 5; ++iv)
+      W.liftflux[iv + 5 * fidx] = 0.5 * C.M.SurfElem[fidx] *
+                                  (sig * W.UPrim_master[PRIM_LIFT[iv] + 6 * fidx] + W.UPrim_slave[PRIM_LIFT[iv] + 6 * fidx]);
+  // Lifting_FillFlux_NormVec  lifting_fillflux.t90:212-256 (stored in gradU*_master)
+#pragma omp parallel for schedule(static)
+  for (long long fidx = 0; fidx < (long long)nF; ++fidx)
+    for (int iv = 0; iv < 5; ++iv) {
+      W.gx_m[iv + 5 * fidx] = W.liftflux[iv + 5 * fidx] * C.M.nv[0 + 3 * fidx];
+      W.gy_m[iv + 5 * fidx] = W.liftflux[iv + 5 * fidx] * C.M.nv[1 + 3 * fidx];
+      W.gz_m[iv + 5 * fidx] = W.liftflux[iv + 5 * fidx] * C.M.nv[2 + 3 * fidx];
+    }
+  Lifting_VolInt(C, W, weak);
   // SurfIntLifting with doApplyJacobian  (surfint.t90:295-347, 591-725)
   int mode = weak ? 2 : 1;
   SurfInt_GPUorder(C, 5, W.gx_m.data(), nullptr, W.gradUx.data(), mode, true);
@@ -1085,6 +1090,76 @@ static void Lifting_BR1(const Ctx& C, Work& W) {
   ProlongToFace_GPUorder(C, 5, W.gradUy.data(), W.gy_m.data(), W.gy_s.data());
   ProlongToFace_GPUorder(C, 5, W.gradUz.data(), W.gz_m.data(), W.gz_s.data());
   (void)n;
+}
+
+// Lifting_BR2 + Lifting_SurfInt_BR2  src/dg/lifting/lifting_br2.t90:43-310 (always strong form; no BC
+// sides, no MPI, no mortars).  The volume gradient gets the same surface lifting as BR1; the face
+// traces are the prolonged volume-only gradient plus etaBR2 times the lifting of that face's own jump.
+static void Lifting_BR2(const Ctx& C, Work& W) {
+  const int N = C.B.N;
+  const size_t nF = (size_t)C.n2 * C.M.nSides, nDOF = (size_t)C.n3 * C.M.nElems;
+  const bool gauss = C.B.node_type == DG_NODETYPE_GAUSS;
+  // Lifting_FillFlux (strong: 0.5*SurfElem*(U_slave - U_master)) and the normal components
+  std::vector<double> FX(5 * nF), FY(5 * nF), FZ(5 * nF);
+#pragma omp parallel for schedule(static)
+  for (long long f = 0; f < (long long)nF; ++f)
+    for (int iv = 0; iv < 5; ++iv) {
+      const double fl = 0.5 * C.M.SurfElem[f] * (-1. * W.UPrim_master[PRIM_LIFT[iv] + 6 * f] + W.UPrim_slave[PRIM_LIFT[iv] + 6 * f]);
+      FX[iv + 5 * f] = fl * C.M.nv[0 + 3 * f];
+      FY[iv + 5 * f] = fl * C.M.nv[1 + 3 * f];
+      FZ[iv + 5 * f] = fl * C.M.nv[2 + 3 * f];
+    }
+  Lifting_VolInt(C, W, false);
+  // ApplyJacobianLifting
+#pragma omp parallel for schedule(static)
+  for (long long id = 0; id < (long long)nDOF; ++id)
+    for (int iv = 0; iv < 5; ++iv) {
+      W.gradUx[iv + 5 * id] = W.gradUx[iv + 5 * id] * C.M.sJ[id];
+      W.gradUy[iv + 5 * id] = W.gradUy[iv + 5 * id] * C.M.sJ[id];
+      W.gradUz[iv + 5 * id] = W.gradUz[iv + 5 * id] * C.M.sJ[id];
+    }
+  // ProlongToFaceLifting of the volume-only gradients
+  ProlongToFace_GPUorder(C, 5, W.gradUx.data(), W.gx_m.data(), W.gx_s.data());
+  ProlongToFace_GPUorder(C, 5, W.gradUy.data(), W.gy_m.data(), W.gy_s.data());
+  ProlongToFace_GPUorder(C, 5, W.gradUz.data(), W.gz_m.data(), W.gz_s.data());
+  // Lifting_SurfInt_BR2: slave sides first, then master sides, sequentially in side order
+  const double eta = C.cfg.eta_br2;
+  const double* Flux[3] = {FX.data(), FY.data(), FZ.data()};
+  double* grad[3] = {W.gradUx.data(), W.gradUy.data(), W.gradUz.data()};
+  double* gm[3] = {W.gx_m.data(), W.gy_m.data(), W.gz_m.data()};
+  double* gs[3] = {W.gx_s.data(), W.gy_s.data(), W.gz_s.data()};
+  const int lmax = gauss ? N : 0;
+  for (int d = 0; d < 3; ++d) {
+    for (int pass = 0; pass < 2; ++pass) {
+      for (int s = 0; s < C.M.nSides; ++s) {
+        // SideToElem(S2E_ELEM_ID, S2E_NB_ELEM_ID, S2E_LOC_SIDE_ID, S2E_NB_LOC_SIDE_ID, S2E_FLIP), 1-based
+        const int e = (pass == 0 ? C.s2e(1, s) : C.s2e(0, s)) - 1;
+        if (e < 0) continue;
+        const int loc = pass == 0 ? C.s2e(3, s) : C.s2e(2, s);
+        const int flip = pass == 0 ? C.s2e(4, s) : 0;
+        double* gface = pass == 0 ? gs[d] : gm[d];
+        const bool minus = loc == XI_MINUS || loc == ETA_MINUS || loc == ZETA_MINUS;
+        for (int q = 0; q <= N; ++q)
+          for (int p = 0; p <= N; ++p) {
+            const int a = C.s2v2(0, p, q, flip, loc), b = C.s2v2(1, p, q, flip, loc);
+            const size_t f = C.fac(p, q, s);
+            for (int l = 0; l <= lmax; ++l) {
+              // CGNS_SideToVol: distance l from the face -> volume index along the normal
+              const int lv = minus ? l : N - l;
+              size_t id;
+              if (loc == XI_MINUS || loc == XI_PLUS) id = C.vol(lv, a, b, e);
+              else if (loc == ETA_MINUS || loc == ETA_PLUS) id = C.vol(a, lv, b, e);
+              else id = C.vol(a, b, lv, e);
+              for (int iv = 0; iv < 5; ++iv) {
+                const double Floc = C.M.sJ[id] * Flux[d][iv + 5 * f] * C.B.L_HatMinus[l];
+                grad[d][iv + 5 * id] = grad[d][iv + 5 * id] + Floc;
+                gface[iv + 5 * f] = gface[iv + 5 * f] + eta * C.B.L_Minus[l] * Floc;
+              }
+            }
+          }
+      }
+    }
+  }
 }
 
 // ApplyDMatrix_Kernel  applydmatrix.t90:19-75
@@ -1123,7 +1198,10 @@ static void DGTimeDerivative(const Ctx& C, Work& W, const double* U, double* Ut)
     ConsToPrim(&W.UPrim_slave[6 * f], &W.U_slave[5 * f], Kappa, R);
   }
   // 6. Lifting
-  if (cfg.parabolic) Lifting_BR1(C, W);
+  if (cfg.parabolic) {
+    if (cfg.lifting == DG_LIFTING_BR2) Lifting_BR2(C, W);
+    else Lifting_BR1(C, W);
+  }
   // 8. VolInt
   const double mu = cfg.mu0, lambda = thermal_conductivity(cfg, cfg.mu0);
   if (cfg.split_dg < 0) {

@@ -56,7 +56,8 @@ def test_config_from_ini_uses_reference_keys():
 
 
 def test_context_rejects_invalid_combinations():
-    for kw in [dict(NodeType="gauss", SplitDG="pi"), dict(SplitDG="pi", Riemann="hllc"), dict(Riemann="avg")]:
+    for kw in [dict(NodeType="gauss", SplitDG="pi"), dict(SplitDG="pi", Riemann="hllc"), dict(Riemann="avg"),
+               dict(parabolic=True, mu0=1e-3, Lifting="br2", doWeakLifting=True)]:
         cfg = gx.config(N=3, **kw)
         h = ctypes.c_void_p()
         rc = nat.lib().dg_ctx_create(ctypes.byref(cfg), ctypes.byref(h))

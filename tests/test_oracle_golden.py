@@ -115,3 +115,56 @@ def test_sbp_property():
         x = b["xGP"]
         for k in range(N + 1):
             assert np.abs(D @ x ** k - (k * x ** (k - 1) if k else 0 * x)).max() < 1e-11
+
+
+def _lifting_pair(N, node_type, deform, U_fn, **kw):
+    import galaexi_gb300 as gx
+    m = gx.Mesh(N, node_type, 3, 2, 2, (0.0,) * 3, (1.0,) * 3, deform=deform)
+    U = U_fn(m)
+    out = {}
+    for lift in ("br1", "br2"):
+        cfg = gx.config(N=N, NodeType="gauss" if node_type == 1 else "gauss-lobatto", parabolic=True, mu0=1e-3,
+                        Riemann="lf", Lifting=lift, **kw)
+        o = orc.Oracle(cfg, m)
+        Ut = o.rhs(U)
+        out[lift] = (Ut, [o.work(1 + d, U.shape) for d in range(3)])
+    return out
+
+
+@pytest.mark.parametrize("node_type,deform,cons", [(1, 0.05, False), (2, 0.0, True), (2, 0.05, False)])
+def test_br2_volume_gradients_equal_br1(node_type, deform, cons):
+    """BR2 changes only the face traces: the volume gradients equal BR1's (lifting_br2.t90:43-310)."""
+    import galaexi_gb300 as gx
+
+    def noisy(m):
+        rng = np.random.default_rng(3)
+        U = gx.fill_ini(m, 1, [1.0, 0.3, 0.2, 0.1, 1.0 / 1.4])
+        return U + 1e-2 * rng.standard_normal(U.shape) * np.abs(U).mean(axis=(0, 1, 2, 3))
+
+    out = _lifting_pair(4, node_type, deform, noisy, doConservativeLifting=cons)
+    for g1, g2 in zip(out["br1"][1], out["br2"][1]):
+        assert np.abs(g1 - g2).max() <= 1e-12 * np.abs(g1).max()
+    # the jumps of the noisy state make the BR2 face traces, hence Ut, differ from BR1
+    assert np.abs(out["br1"][0] - out["br2"][0]).max() > 1e-6 * np.abs(out["br1"][0]).max()
+
+
+def test_br2_equals_br1_for_continuous_data():
+    """On Gauss-Lobatto nodes a state sampled from one smooth periodic field has no jumps at the
+    faces, so the BR2 penalty vanishes and the operator equals BR1."""
+    import galaexi_gb300 as gx
+
+    def smooth(m):
+        x = m.Elem_xGP
+        s = np.sin(2 * np.pi * x[..., 0]) * np.cos(2 * np.pi * x[..., 1]) + 0.5 * np.sin(2 * np.pi * x[..., 2])
+        U = np.empty(x.shape[:-1] + (5,))
+        rho = 1.0 + 0.1 * s
+        U[..., 0] = rho
+        U[..., 1] = rho * (0.3 + 0.05 * s)
+        U[..., 2] = rho * 0.2
+        U[..., 3] = rho * (0.1 - 0.05 * s)
+        U[..., 4] = (1.0 + 0.05 * s) / 0.4 + 0.5 * (U[..., 1] ** 2 + U[..., 2] ** 2 + U[..., 3] ** 2) / rho
+        return U
+
+    out = _lifting_pair(5, 2, 0.0, smooth)
+    a, b = out["br1"][0], out["br2"][0]
+    assert np.abs(a - b).max() <= 1e-11 * np.abs(a).max()

@@ -168,3 +168,52 @@ def test_mixed_precision_run_close_to_fp64():
         ke_err, rel_l2(Um, ref), abs(mass(Um) - mass(U0)) / mass(U0)))
     assert ke_err <= 1e-6
     assert rel_l2(Um, ref) < 1e-4
+
+
+@pytest.mark.parametrize("lift", ["strong", "conservative", "weak"])
+def test_lifted_gradients_match_oracle(lift):
+    kw = dict(Riemann="roe", parabolic=True, mu0=1e-3, doWeakLifting=lift == "weak",
+              doConservativeLifting=lift == "conservative")
+    N, nt = (5, 1) if lift == "weak" else (5, 2)
+    cfg = gx.config(N=N, NodeType="gauss" if nt == 1 else "gauss-lobatto", **kw)
+    m = gx.Mesh(N, nt, 2, 3, 2, (-math.pi,) * 3, (math.pi,) * 3, deform=0.05)
+    U = perturbed_state(m, gx.tgv_state(m, mach=0.3, R=cfg.R), seed=11)
+    op = gx.DG(cfg, m)
+    op.DGTimeDerivative_weakForm(0.0, torch.from_numpy(U).cuda())
+    grads = [g.cpu().numpy() for g in op.gradients()]
+    orc = Oracle(cfg, m)
+    orc.rhs(U)
+    for d, g in enumerate(grads):
+        ref = orc.work(1 + d, g.shape)
+        err = rel_l2(g, ref)
+        assert err <= RTOL_RHS, "grad %s: relative L2 %.3e" % ("xyz"[d], err)
+    op.close()
+
+
+BR2_CASES = [
+    # the curved-box Gauss case of the BR2 workload (weak form, HLLC, etaBR2 = 2)
+    ("gauss_weak_hllc_br2_curved", dict(NodeType="gauss", Riemann="hllc", Lifting="br2", etaBR2=2.0), 5, 1, 0.05),
+    ("gl_split_pi_roe_br2_conslift", dict(Riemann="roe", SplitDG="pi", Lifting="br2", etaBR2=3.0,
+                                          doConservativeLifting=True), 4, 2, 0.0),
+    ("gauss_weak_lf_br2_curved_n3", dict(NodeType="gauss", Riemann="lf", Lifting="br2", etaBR2=2.0), 3, 1, 0.05),
+]
+
+
+@pytest.mark.parametrize("name,kw,N,nt,deform", BR2_CASES, ids=[c[0] for c in BR2_CASES])
+def test_br2_rhs_and_gradients_match_oracle(name, kw, N, nt, deform):
+    cfg = gx.config(N=N, parabolic=True, mu0=1e-3, **kw)
+    m = gx.Mesh(N, nt, 3, 2, 2, (0.0,) * 3, (1.0,) * 3, deform=deform)
+    rng = np.random.default_rng(zlib.crc32(name.encode()))
+    U = gx.fill_ini(m, 1, [1.0, 0.3, 0.2, 0.1, 1.0 / 1.4])
+    U = U + 1e-2 * rng.standard_normal(U.shape) * np.abs(U).mean(axis=(0, 1, 2, 3))
+    op = gx.DG(cfg, m)
+    Ut = op.DGTimeDerivative_weakForm(0.0, torch.from_numpy(U).cuda()).cpu().numpy()
+    grads = [g.cpu().numpy() for g in op.gradients()]
+    op.close()
+    orc = Oracle(cfg, m)
+    ref = orc.rhs(U)
+    err = rel_l2(Ut, ref)
+    assert err <= RTOL_RHS, "%s: Ut relative L2 %.3e" % (name, err)
+    for d, g in enumerate(grads):
+        e = rel_l2(g, orc.work(1 + d, g.shape))
+        assert e <= RTOL_RHS, "%s: grad %s relative L2 %.3e" % (name, "xyz"[d], e)
