@@ -76,6 +76,14 @@ _SIGS = {
     "dg_check_state": (_I, [_P, _P, ctypes.POINTER(ctypes.c_longlong), _P]),
     "dg_kernel_launch_count": (ctypes.c_longlong, [_P]),
     "dg_get_gradients": (_I, [_P, _P, _P, _P, _P]),
+    "dg_integrals": (_I, [_P, _P, _P, _P]),
+    "dg_kinetic_energy": (_I, [_P, _P, _P, _P, _P]),
+    "dg_rhs_jvp": (_I, [_P, _D, _P, _P, _D, _P, _P, _P]),
+    "dg_tlm_steps": (_I, [_P, _D, _D, _I, _P, _P, _D, _P, _P]),
+    "dg_rhs_vjp": (_I, [_P, _D, _P, _P, _P, _P, _P]),
+    "dg_adjoint_forward": (_I, [_P, _D, _D, _I, _P, _P, ctypes.c_size_t, _P, _P]),
+    "dg_adjoint_reverse": (_I, [_P, _P, _P, _P]),
+    "dg_adjoint_window": (_I, [_P, _D, _D, _I, _P, ctypes.c_size_t, _P, _P, _P, _P, _P]),
     "dg_last_error": (ctypes.c_char_p, []),
     "dg_basis": (_I, [_I, _I] + [_P] * 10),
     "dg_mesh_cartesian_sizes": (_I, [_I, _I, _I, _IP, _IP]),

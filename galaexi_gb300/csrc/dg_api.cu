@@ -179,6 +179,175 @@ int fma_peak(double* gflops) {
 
 }  // namespace
 
+// ---------------------------------------------------------------------------------------------
+// tangent-linear and adjoint helpers
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+using D1 = gx::Dual<1>;
+
+__global__ void k_to_dual(const double* __restrict__ in, D1* __restrict__ out, size_t cnt) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < cnt; t += (size_t)gridDim.x * blockDim.x)
+    out[t] = D1(in[t]);
+}
+__global__ void k_pack(const double* __restrict__ v, const double* __restrict__ d, D1* __restrict__ out, size_t cnt) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < cnt; t += (size_t)gridDim.x * blockDim.x) {
+    D1 x(v[t]);
+    x.d[0] = d ? d[t] : 0.;
+    out[t] = x;
+  }
+}
+__global__ void k_unpack(const D1* __restrict__ in, double* __restrict__ v, double* __restrict__ d, size_t cnt) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < cnt; t += (size_t)gridDim.x * blockDim.x) {
+    if (v) v[t] = in[t].v;
+    if (d) d[t] = in[t].d[0];
+  }
+}
+int grid_for(size_t cnt) {
+  size_t g = (cnt + 255) / 256;
+  return (int)(g > 152 * 32 ? 152 * 32 : (g < 1 ? 1 : g));
+}
+
+// volume integrals over the state: rho, m1, m2, m3, E, kinetic energy 0.5 |m|^2 / rho
+// (quadrature on the solution nodes: w_i w_j w_k / sJ); per-block partials part[6][gridDim]
+__global__ void __launch_bounds__(256) k_integrals(const double* __restrict__ U, const double* __restrict__ MetD,
+                                                   const double* __restrict__ wq, int n, int nElems,
+                                                   double* __restrict__ part) {
+  __shared__ double red[6][8];
+  const int n3 = n * n * n;
+  const long long nn = (long long)nElems * n3;
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nn; t += (long long)gridDim.x * blockDim.x) {
+    const long long e = t / n3;
+    const int node = (int)(t - e * n3);
+    const int i = node % n, j = (node / n) % n, k = node / (n * n);
+    const double w = wq[i] * wq[j] * wq[k] / MetD[(e * 10 + 9) * n3 + node];
+    const double* u = U + t * 5;
+    acc[0] += w * u[0]; acc[1] += w * u[1]; acc[2] += w * u[2]; acc[3] += w * u[3]; acc[4] += w * u[4];
+    acc[5] += w * 0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0];
+  }
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    double v = acc[c];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[c][threadIdx.x >> 5] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double v = 0.;
+    for (int w = 0; w < 8; ++w) v += red[threadIdx.x][w];
+    part[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = v;
+  }
+}
+// gradient of the kinetic-energy integral with respect to U
+__global__ void k_ke_grad(const double* __restrict__ U, const double* __restrict__ MetD, const double* __restrict__ wq,
+                          int n, int nElems, double* __restrict__ G) {
+  const int n3 = n * n * n;
+  const long long nn = (long long)nElems * n3;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nn; t += (long long)gridDim.x * blockDim.x) {
+    const long long e = t / n3;
+    const int node = (int)(t - e * n3);
+    const int i = node % n, j = (node / n) % n, k = node / (n * n);
+    const double w = wq[i] * wq[j] * wq[k] / MetD[(e * 10 + 9) * n3 + node];
+    const double* u = U + t * 5;
+    const double sr = 1. / u[0];
+    const double ke = 0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) * sr;
+    G[t * 5 + 0] = -w * ke * sr;
+    G[t * 5 + 1] = w * u[1] * sr;
+    G[t * 5 + 2] = w * u[2] * sr;
+    G[t * 5 + 3] = w * u[3] * sr;
+    G[t * 5 + 4] = 0.;
+  }
+}
+
+int need_fp64(dg_ctx* ctx, const char* what) {
+  if (ctx->cfg.precision != DG_PRECISION_FP64) {
+    set_error(std::string(what) + ": FP64 operator only");
+    return DG_ERR_UNSUPPORTED;
+  }
+  return DG_OK;
+}
+
+int tlm_setup(dg_ctx* ctx) {
+  if (int rc = need_fp64(ctx, "tangent-linear operator")) return rc;
+  if (ctx->cfg.split_dg != DG_SPLIT_NONE && ctx->cfg.split_dg != DG_SPLIT_PI && ctx->cfg.split_dg != DG_SPLIT_KG) {
+    set_error("tangent-linear operator: split forms PI and KG only"); return DG_ERR_UNSUPPORTED;
+  }
+  if (ctx->t_ok) return DG_OK;
+  const gxc::NPTable* T = table_for(ctx->n);
+  if (int rc = T->configure_t()) return rc;
+  const size_t nE = ctx->nElems, nS = ctx->nSides, n2 = ctx->n2, n3 = ctx->n3;
+  gxc::PrecData<D1>& P = ctx->t;
+  bool ok = P.basis.alloc(ctx->d.basis.n) && P.Met.alloc(ctx->d.Met.n) && P.Fgeo.alloc(ctx->d.Fgeo.n) &&
+            P.Pvol.alloc(nE * 7 * n3) && P.Uf.alloc(2 * nS * 5 * n2) && P.Pf.alloc(2 * nS * 6 * n2) &&
+            P.Flux.alloc(nS * 5 * n2) && ctx->Ud.alloc(nE * 5 * n3) && ctx->Utd.alloc(nE * 5 * n3);
+  if (ok && ctx->cfg.parabolic) ok = P.Gvol.alloc(nE * 15 * n3) && P.Gf.alloc(2 * nS * 15 * n2);
+  if (!ok) { set_error("cudaMalloc tangent-linear data"); return DG_ERR_ALLOC; }
+  k_to_dual<<<grid_for(P.basis.n), 256>>>(ctx->d.basis.p, P.basis.p, P.basis.n);
+  k_to_dual<<<grid_for(P.Met.n), 256>>>(ctx->d.Met.p, P.Met.p, P.Met.n);
+  k_to_dual<<<grid_for(P.Fgeo.n), 256>>>(ctx->d.Fgeo.p, P.Fgeo.p, P.Fgeo.n);
+  CUDA_TRY(cudaDeviceSynchronize(), "tangent-linear set-up");
+  ctx->t_ok = true;
+  return DG_OK;
+}
+
+int adj_setup(dg_ctx* ctx) {
+  if (int rc = need_fp64(ctx, "adjoint")) return rc;
+  const dg_config& c = ctx->cfg;
+  if (c.split_dg != DG_SPLIT_NONE && c.split_dg != DG_SPLIT_PI && c.split_dg != DG_SPLIT_KG) {
+    set_error("adjoint: split forms PI and KG only"); return DG_ERR_UNSUPPORTED;
+  }
+  if (c.parabolic && (c.lifting != DG_LIFTING_BR1 || c.do_weak_lifting)) {
+    set_error("adjoint: BR1 lifting in strong form only"); return DG_ERR_UNSUPPORTED;
+  }
+  if (ctx->UBv.p) return DG_OK;
+  const gxc::NPTable* T = table_for(ctx->n);
+  if (int rc = T->configure_a()) return rc;
+  const size_t nE = ctx->nElems, nS = ctx->nSides, n2 = ctx->n2, n3 = ctx->n3;
+  const size_t epb = n3 >= 128 ? 1 : 256 / n3;
+  const size_t nparts = (nS * n2 + 127) / 128 + (nE + epb - 1) / epb;
+  const size_t ipart = 6 * (size_t)grid_for(nE * n3);
+  bool ok = ctx->UfB.alloc(2 * nS * 5 * n2) && ctx->JB.alloc(2 * nS * 5 * n2) && ctx->UBv.alloc(nE * 5 * n3) &&
+            ctx->part.alloc(nparts > ipart ? nparts : ipart) && ctx->acc.alloc(8);
+  if (ok) ok = ctx->GfB.alloc(2 * nS * 15 * n2);
+  if (!ok) { ctx->UBv.release(); set_error("cudaMalloc adjoint scratch"); return DG_ERR_ALLOC; }
+  // the face gradient cotangents stay zero for the Euler equations
+  CUDA_TRY(cudaMemset(ctx->GfB.p, 0, ctx->GfB.n * sizeof(double)), "clear face gradient cotangents");
+  CUDA_TRY(cudaMemset(ctx->JB.p, 0, ctx->JB.n * sizeof(double)), "clear lifting cotangents");
+  return DG_OK;
+}
+
+int integrals(dg_ctx* ctx, const double* d_U, double out[6], cudaStream_t st) {
+  const size_t nn = (size_t)ctx->nElems * ctx->n3;
+  const int grid = grid_for(nn);
+  if (!ctx->part.p || ctx->part.n < (size_t)6 * grid) {
+    if (!ctx->part.alloc((size_t)6 * grid)) { set_error("cudaMalloc"); return DG_ERR_ALLOC; }
+  }
+  if (!ctx->acc.p && !ctx->acc.alloc(8)) { set_error("cudaMalloc"); return DG_ERR_ALLOC; }
+  CUDA_TRY(cudaMemsetAsync(ctx->acc.p, 0, 8 * sizeof(double), st), "clear");
+  k_integrals<<<grid, 256, 0, st>>>(d_U, ctx->MetD.p, ctx->wq.p, ctx->n, ctx->nElems, ctx->part.p);
+  for (int c = 0; c < 6; ++c) gx::k_adj_sum<<<1, 256, 0, st>>>(ctx->part.p + (size_t)c * grid, grid, ctx->acc.p + c);
+  ctx->launches += 7;
+  CUDA_TRY(cudaGetLastError(), "integrals launch");
+  CUDA_TRY(cudaMemcpyAsync(out, ctx->acc.p, 6 * sizeof(double), cudaMemcpyDeviceToHost, st), "read integrals");
+  CUDA_TRY(cudaStreamSynchronize(st), "sync integrals");
+  return DG_OK;
+}
+
+// one forward LSERK stage (1..5) on (W, K)
+int fwd_stage(dg_ctx* ctx, int stage, double dt, double* W, double* K, cudaStream_t st) {
+  gx::RKArgs rk{W, K, nullptr, stage == 1 ? 0. : -1. * kRKA[stage], kRKb[stage] * dt};
+  return run_rhs(ctx, W, rk, 1, st);
+}
+// one reverse LSERK stage at the stage input X
+int rev_stage(dg_ctx* ctx, int stage, double dt, const double* X, double* Ubar, double* Kbar, cudaStream_t st) {
+  const double b = kRKb[stage] * dt, mA = stage == 1 ? 0. : -1. * kRKA[stage];
+  gx::CotSrc cs{Kbar, Ubar, b};
+  return table_for(ctx->n)->adj(ctx, X, cs, 1, nullptr, Ubar, Kbar, b, mA, ctx->acc.p, st);
+}
+
+}  // namespace
+
 extern "C" {
 
 int dg_measure_fma_peak(int precision, double* gflops) {
@@ -267,6 +436,10 @@ int dg_ctx_destroy(dg_ctx* ctx) {
   ctx->E2S.release();
   ctx->red.release();
   ctx->bad.release();
+  ctx->S2E.release(); ctx->wq.release();
+  ctx->t.release(); ctx->Ud.release(); ctx->Utd.release();
+  ctx->UfB.release(); ctx->GfB.release(); ctx->JB.release(); ctx->UBv.release(); ctx->part.release();
+  ctx->acc.release(); ctx->W.release(); ctx->K.release(); ctx->tape.store.release();
   delete ctx;
   return DG_OK;
 }
@@ -334,6 +507,23 @@ int dg_set_mesh(dg_ctx* ctx, int nElems, int nSides, int nBCSides, const double*
   if (!ctx->MetD.alloc(met.size()) || !ctx->E2S.alloc(he2s.size())) { set_error("cudaMalloc mesh"); return DG_ERR_ALLOC; }
   CUDA_TRY(cudaMemcpy(ctx->MetD.p, met.data(), met.size() * sizeof(double), cudaMemcpyHostToDevice), "upload metrics");
   CUDA_TRY(cudaMemcpy(ctx->E2S.p, he2s.data(), he2s.size() * sizeof(int), cudaMemcpyHostToDevice), "upload E2S");
+  // SideToElem on the device, from the validated ElemToSide: master elem/side, slave elem/side, flip
+  std::vector<int> hs2e((size_t)nSides * 5, 0);
+  for (int e = 0; e < nElems; ++e)
+    for (int ls = 0; ls < 6; ++ls) {
+      const int side = he2s[(e * 6 + ls) * 2], flip = he2s[(e * 6 + ls) * 2 + 1];
+      int* q = &hs2e[(size_t)side * 5];
+      if (flip == 0) { q[0] = e; q[1] = ls + 1; }
+      else { q[2] = e; q[3] = ls + 1; q[4] = flip; }
+    }
+  if (!ctx->S2E.alloc(hs2e.size()) || !ctx->wq.alloc(n)) { set_error("cudaMalloc mesh"); return DG_ERR_ALLOC; }
+  CUDA_TRY(cudaMemcpy(ctx->S2E.p, hs2e.data(), hs2e.size() * sizeof(int), cudaMemcpyHostToDevice), "upload S2E");
+  CUDA_TRY(cudaMemcpy(ctx->wq.p, ctx->B.w.data(), n * sizeof(double), cudaMemcpyHostToDevice), "upload weights");
+  ctx->t_ok = false;
+  ctx->tape.ok = false;
+  ctx->t.release(); ctx->Ud.release(); ctx->Utd.release();
+  ctx->UfB.release(); ctx->GfB.release(); ctx->JB.release(); ctx->UBv.release(); ctx->part.release();
+  ctx->W.release(); ctx->K.release(); ctx->tape.store.release();
   ctx->mesh_ok = true;
   ctx->grad_ok = false;
   return DG_OK;
@@ -434,6 +624,221 @@ int dg_set_pressure_offset(dg_ctx* ctx, double p_ref) {
   if (!(p_ref >= 0.) || !std::isfinite(p_ref)) { set_error("pressure offset must be finite and >= 0"); return DG_ERR_ARG; }
   ctx->pref = p_ref;
   return DG_OK;
+}
+
+int dg_integrals(dg_ctx* ctx, const double* d_U, double* out6, void* stream) {
+  if (int rc = check_ctx(ctx, true)) return rc;
+  if (!d_U || !out6) { set_error("dg_integrals: null argument"); return DG_ERR_ARG; }
+  return integrals(ctx, d_U, out6, (cudaStream_t)stream);
+}
+
+int dg_kinetic_energy(dg_ctx* ctx, const double* d_U, double* J, double* d_dJdU, void* stream) {
+  if (int rc = check_ctx(ctx, true)) return rc;
+  if (!d_U || !J) { set_error("dg_kinetic_energy: null argument"); return DG_ERR_ARG; }
+  cudaStream_t st = (cudaStream_t)stream;
+  double out[6];
+  if (int rc = integrals(ctx, d_U, out, st)) return rc;
+  *J = out[5];
+  if (d_dJdU) {
+    k_ke_grad<<<grid_for((size_t)ctx->nElems * ctx->n3), 256, 0, st>>>(d_U, ctx->MetD.p, ctx->wq.p, ctx->n,
+                                                                     ctx->nElems, d_dJdU);
+    ctx->launches++;
+    CUDA_TRY(cudaGetLastError(), "k_ke_grad launch");
+  }
+  return DG_OK;
+}
+
+int dg_rhs_jvp(dg_ctx* ctx, double t, const double* d_U, const double* d_Udot, double mu_dot, double* d_Ut,
+               double* d_Utdot, void* stream) {
+  if (int rc = check_ctx(ctx, true)) return rc;
+  if (!d_U || !d_Utdot) { set_error("dg_rhs_jvp: null argument"); return DG_ERR_ARG; }
+  if (int rc = tlm_setup(ctx)) return rc;
+  (void)t;
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t cnt = (size_t)ctx->nElems * 5 * ctx->n3;
+  k_pack<<<grid_for(cnt), 256, 0, st>>>(d_U, d_Udot, ctx->Ud.p, cnt);
+  gx::RKArgsT<D1> rk{nullptr, nullptr, ctx->Utd.p, 0., 0.};
+  if (int rc = table_for(ctx->n)->rhs_t(ctx, ctx->Ud.p, rk, 0, mu_dot, st)) return rc;
+  k_unpack<<<grid_for(cnt), 256, 0, st>>>(ctx->Utd.p, d_Ut, d_Utdot, cnt);
+  ctx->launches += 2;
+  CUDA_TRY(cudaGetLastError(), "dg_rhs_jvp");
+  return DG_OK;
+}
+
+int dg_tlm_steps(dg_ctx* ctx, double t, double dt, int nSteps, double* d_U, double* d_Udot, double mu_dot,
+                 double* d_Ut_tmp, void* stream) {
+  if (int rc = check_ctx(ctx, true)) return rc;
+  if (!d_U || !d_Udot || !d_Ut_tmp || nSteps < 0) { set_error("dg_tlm_steps: bad argument"); return DG_ERR_ARG; }
+  if (int rc = tlm_setup(ctx)) return rc;
+  (void)t;
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t cnt = (size_t)ctx->nElems * 5 * ctx->n3;
+  k_pack<<<grid_for(cnt), 256, 0, st>>>(d_U, d_Udot, ctx->Ud.p, cnt);
+  k_pack<<<grid_for(cnt), 256, 0, st>>>(d_Ut_tmp, nullptr, ctx->Utd.p, cnt);
+  for (int s = 0; s < nSteps; ++s)
+    for (int stage = 1; stage <= 5; ++stage) {
+      gx::RKArgsT<D1> rk{ctx->Ud.p, ctx->Utd.p, nullptr, stage == 1 ? 0. : -1. * kRKA[stage], kRKb[stage] * dt};
+      if (int rc = table_for(ctx->n)->rhs_t(ctx, ctx->Ud.p, rk, 1, mu_dot, st)) return rc;
+    }
+  k_unpack<<<grid_for(cnt), 256, 0, st>>>(ctx->Ud.p, d_U, d_Udot, cnt);
+  k_unpack<<<grid_for(cnt), 256, 0, st>>>(ctx->Utd.p, d_Ut_tmp, nullptr, cnt);
+  ctx->launches += 4;
+  CUDA_TRY(cudaGetLastError(), "dg_tlm_steps");
+  return DG_OK;
+}
+
+int dg_rhs_vjp(dg_ctx* ctx, double t, const double* d_U, const double* d_Utbar, double* d_Ubar, double* mu_bar,
+               void* stream) {
+  if (int rc = check_ctx(ctx, true)) return rc;
+  if (!d_U || !d_Utbar || !d_Ubar) { set_error("dg_rhs_vjp: null argument"); return DG_ERR_ARG; }
+  if (int rc = adj_setup(ctx)) return rc;
+  (void)t;
+  cudaStream_t st = (cudaStream_t)stream;
+  CUDA_TRY(cudaMemsetAsync(ctx->acc.p, 0, sizeof(double), st), "clear");
+  gx::CotSrc cs{d_Utbar, nullptr, 0.};
+  if (int rc = table_for(ctx->n)->adj(ctx, d_U, cs, 0, d_Ubar, nullptr, nullptr, 0., 0., ctx->acc.p, st)) return rc;
+  if (mu_bar) {
+    CUDA_TRY(cudaMemcpyAsync(mu_bar, ctx->acc.p, sizeof(double), cudaMemcpyDeviceToHost, st), "read mu_bar");
+    CUDA_TRY(cudaStreamSynchronize(st), "sync");
+  }
+  return DG_OK;
+}
+
+int dg_adjoint_forward(dg_ctx* ctx, double t0, double dt, int nSteps, const double* d_U0, double* d_U_final,
+                       size_t budget_bytes, int* plan_out, void* stream) {
+  if (int rc = check_ctx(ctx, true)) return rc;
+  if (!d_U0 || nSteps < 1) { set_error("dg_adjoint_forward: bad argument"); return DG_ERR_ARG; }
+  if (int rc = adj_setup(ctx)) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  AdjTape& T = ctx->tape;
+  T.ok = false;
+  T.store.release();
+  const size_t S = (size_t)ctx->nElems * 5 * ctx->n3;
+  const size_t bytes = S * sizeof(double);
+  if (!ctx->W.p && !(ctx->W.alloc(S) && ctx->K.alloc(S))) { set_error("cudaMalloc adjoint work states"); return DG_ERR_ALLOC; }
+  const size_t slots_max = budget_bytes / bytes;
+  // plan 1: every stage input; plan 2: segment starts + the stage inputs of one segment (one extra
+  // forward sweep); plan 3: segment starts + step starts of one segment + the stage inputs of one step
+  // (two extra forward sweeps)
+  int plan = 0, k = 0, nSeg = 0;
+  size_t slots = 0;
+  if ((size_t)5 * nSteps <= slots_max) { plan = 1; k = nSteps; nSeg = 1; slots = (size_t)5 * nSteps; }
+  else {
+    size_t best = (size_t)-1; int bk = 0;
+    for (int kk = 1; kk <= nSteps; ++kk) {
+      const size_t need = (size_t)((nSteps + kk - 1) / kk) + (size_t)5 * kk;
+      if (need < best) { best = need; bk = kk; }
+    }
+    if (best <= slots_max) { plan = 2; k = bk; nSeg = (nSteps + bk - 1) / bk; slots = best; }
+    else {
+      best = (size_t)-1; bk = 0;
+      for (int kk = 1; kk <= nSteps; ++kk) {
+        const size_t need = (size_t)((nSteps + kk - 1) / kk) + (size_t)kk + 5;
+        if (need < best) { best = need; bk = kk; }
+      }
+      if (best <= slots_max) { plan = 3; k = bk; nSeg = (nSteps + bk - 1) / bk; slots = best; }
+    }
+  }
+  if (!plan) { set_error("dg_adjoint_forward: checkpoint budget too small for this window"); return DG_ERR_ALLOC; }
+  if (!T.store.alloc(slots * S)) { set_error("cudaMalloc checkpoints"); return DG_ERR_ALLOC; }
+  T.plan = plan; T.k = k; T.nSeg = nSeg; T.nSteps = nSteps; T.t0 = t0; T.dt = dt; T.state = S;
+  double* W = ctx->W.p;
+  double* K = ctx->K.p;
+  CUDA_TRY(cudaMemcpyAsync(W, d_U0, bytes, cudaMemcpyDeviceToDevice, st), "copy U0");
+  CUDA_TRY(cudaMemsetAsync(K, 0, bytes, st), "clear K");
+  for (int nstep = 0; nstep < nSteps; ++nstep) {
+    if (plan != 1 && nstep % k == 0)
+      CUDA_TRY(cudaMemcpyAsync(T.store.p + (size_t)(nstep / k) * S, W, bytes, cudaMemcpyDeviceToDevice, st), "checkpoint");
+    for (int stage = 1; stage <= 5; ++stage) {
+      if (plan == 1)
+        CUDA_TRY(cudaMemcpyAsync(T.store.p + ((size_t)nstep * 5 + stage - 1) * S, W, bytes, cudaMemcpyDeviceToDevice, st),
+                 "stage checkpoint");
+      if (int rc = fwd_stage(ctx, stage, dt, W, K, st)) return rc;
+    }
+  }
+  if (d_U_final) CUDA_TRY(cudaMemcpyAsync(d_U_final, W, bytes, cudaMemcpyDeviceToDevice, st), "copy U_final");
+  T.ok = true;
+  if (plan_out) *plan_out = plan;
+  return DG_OK;
+}
+
+int dg_adjoint_reverse(dg_ctx* ctx, double* d_Ubar, double* mu_bar, void* stream) {
+  if (int rc = check_ctx(ctx, true)) return rc;
+  if (!d_Ubar) { set_error("dg_adjoint_reverse: null argument"); return DG_ERR_ARG; }
+  AdjTape& T = ctx->tape;
+  if (!T.ok) { set_error("dg_adjoint_reverse: no recorded forward window (dg_adjoint_forward)"); return DG_ERR_ARG; }
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t S = T.state, bytes = S * sizeof(double);
+  double* Kbar = ctx->K.p;  // the forward K is not needed any more; reused for K_bar
+  double* W = ctx->W.p;
+  // a second K for the recomputation sweeps
+  gxc::DBuf<double> K2;
+  if (T.plan != 1 && !K2.alloc(S)) { set_error("cudaMalloc"); return DG_ERR_ALLOC; }
+  CUDA_TRY(cudaMemsetAsync(Kbar, 0, bytes, st), "clear K_bar");
+  CUDA_TRY(cudaMemsetAsync(ctx->acc.p, 0, sizeof(double), st), "clear mu_bar");
+  const double dt = T.dt;
+  int rc = DG_OK;
+  if (T.plan == 1) {
+    for (int nstep = T.nSteps - 1; nstep >= 0 && rc == DG_OK; --nstep)
+      for (int stage = 5; stage >= 1 && rc == DG_OK; --stage)
+        rc = rev_stage(ctx, stage, dt, T.store.p + ((size_t)nstep * 5 + stage - 1) * S, d_Ubar, Kbar, st);
+  } else {
+    double* seg = T.store.p;
+    double* buf = T.store.p + (size_t)T.nSeg * S;  // plan 2: 5k stage inputs; plan 3: k step starts + 5 stage inputs
+    for (int sg = T.nSeg - 1; sg >= 0 && rc == DG_OK; --sg) {
+      const int n0 = sg * T.k, n1 = (n0 + T.k < T.nSteps) ? n0 + T.k : T.nSteps;
+      CUDA_TRY(cudaMemcpyAsync(W, seg + (size_t)sg * S, bytes, cudaMemcpyDeviceToDevice, st), "restore");
+      CUDA_TRY(cudaMemsetAsync(K2.p, 0, bytes, st), "clear");
+      for (int nstep = n0; nstep < n1 && rc == DG_OK; ++nstep) {
+        if (T.plan == 3)
+          CUDA_TRY(cudaMemcpyAsync(buf + (size_t)(nstep - n0) * S, W, bytes, cudaMemcpyDeviceToDevice, st), "step start");
+        for (int stage = 1; stage <= 5 && rc == DG_OK; ++stage) {
+          if (T.plan == 2)
+            CUDA_TRY(cudaMemcpyAsync(buf + ((size_t)(nstep - n0) * 5 + stage - 1) * S, W, bytes, cudaMemcpyDeviceToDevice,
+                                     st), "stage input");
+          rc = fwd_stage(ctx, stage, dt, W, K2.p, st);
+        }
+      }
+      for (int nstep = n1 - 1; nstep >= n0 && rc == DG_OK; --nstep) {
+        const double* X = nullptr;
+        if (T.plan == 3) {
+          double* sbuf = buf + (size_t)T.k * S;
+          CUDA_TRY(cudaMemcpyAsync(W, buf + (size_t)(nstep - n0) * S, bytes, cudaMemcpyDeviceToDevice, st), "restore step");
+          CUDA_TRY(cudaMemsetAsync(K2.p, 0, bytes, st), "clear");
+          for (int stage = 1; stage <= 4 && rc == DG_OK; ++stage) {
+            CUDA_TRY(cudaMemcpyAsync(sbuf + (size_t)(stage - 1) * S, W, bytes, cudaMemcpyDeviceToDevice, st), "stage input");
+            rc = fwd_stage(ctx, stage, dt, W, K2.p, st);
+          }
+          CUDA_TRY(cudaMemcpyAsync(sbuf + (size_t)4 * S, W, bytes, cudaMemcpyDeviceToDevice, st), "stage input");
+          for (int stage = 5; stage >= 1 && rc == DG_OK; --stage)
+            rc = rev_stage(ctx, stage, dt, sbuf + (size_t)(stage - 1) * S, d_Ubar, Kbar, st);
+          continue;
+        }
+        for (int stage = 5; stage >= 1 && rc == DG_OK; --stage) {
+          X = buf + ((size_t)(nstep - n0) * 5 + stage - 1) * S;
+          rc = rev_stage(ctx, stage, dt, X, d_Ubar, Kbar, st);
+        }
+      }
+    }
+  }
+  if (rc != DG_OK) return rc;
+  if (mu_bar) {
+    CUDA_TRY(cudaMemcpyAsync(mu_bar, ctx->acc.p, sizeof(double), cudaMemcpyDeviceToHost, st), "read mu_bar");
+    CUDA_TRY(cudaStreamSynchronize(st), "sync");
+  }
+  T.ok = false;  // the window's K was overwritten; record again before the next reverse sweep
+  return DG_OK;
+}
+
+int dg_adjoint_window(dg_ctx* ctx, double t0, double dt, int nSteps, const double* d_U0, size_t budget_bytes,
+                      double* J, double* d_dJdU0, double* dJdmu, double* d_U_final, void* stream) {
+  if (int rc = check_ctx(ctx, true)) return rc;
+  if (!d_U0 || !J || !d_dJdU0) { set_error("dg_adjoint_window: null argument"); return DG_ERR_ARG; }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (int rc = dg_adjoint_forward(ctx, t0, dt, nSteps, d_U0, d_U_final, budget_bytes, nullptr, stream)) return rc;
+  if (int rc = dg_kinetic_energy(ctx, ctx->W.p, J, d_dJdU0, stream)) return rc;
+  (void)st;
+  return dg_adjoint_reverse(ctx, d_dJdU0, dJdmu, stream);
 }
 
 }  // extern "C"

@@ -8,6 +8,7 @@
 #include "../../include/galaexi_gb300.h"
 #include "dg_host.h"
 #include "dg_kernels.cuh"
+#include "dg_adjoint.cuh"
 
 namespace gxc {
 
@@ -69,6 +70,17 @@ inline gx::Gas<R> make_gas(const dg_config& c, double pref) {
 
 }  // namespace gxc
 
+// recorded forward window of the adjoint (checkpoints of dg_adjoint_forward)
+struct AdjTape {
+  int plan = 0;                 // 1: all stage inputs, 2: segment starts + stage inputs of one segment,
+                                // 3: segment starts + step starts of one segment + stage inputs of one step
+  int nSteps = 0, k = 0, nSeg = 0;
+  double t0 = 0., dt = 0.;
+  gxc::DBuf<double> store;      // checkpoint slots, each one state
+  size_t state = 0;             // doubles per state
+  bool ok = false;
+};
+
 struct dg_ctx {
   dg_config cfg;
   int N = 0, n = 0, n2 = 0, n3 = 0;
@@ -81,6 +93,15 @@ struct dg_ctx {
   gxc::DBuf<double> red;   // dt reduction result (2)
   gxc::DBuf<unsigned long long> bad;
   long long launches = 0;
+  gxc::DBuf<int> S2E;      // [side][5]: master elem, master local side, slave elem, slave local side, flip (0-based)
+  gxc::DBuf<double> wq;    // 1D quadrature weights (n)
+  // tangent-linear operator (R = S = Dual<1>), set up on first use
+  gxc::PrecData<gx::Dual<1>> t;
+  gxc::DBuf<gx::Dual<1>> Ud, Utd;
+  bool t_ok = false;
+  // adjoint scratch, set up on first use
+  gxc::DBuf<double> UfB, GfB, JB, UBv, part, acc, W, K;
+  AdjTape tape;
   bool mesh_ok = false;
   bool grad_ok = false;    // Gvol holds the lifted gradients of the last RHS evaluation
   double pref = 0.;       // reference pressure of the mixed form (dg_set_pressure_offset)
@@ -111,6 +132,14 @@ struct NPTable {
   int (*cfl)(dg_ctx*, const double* U, double cflS, double dflS, double kpr, cudaStream_t st);
   // one RK-mode stage with an event recorded after each kernel (ev[0..4]); lift may be skipped
   int (*stage_events)(dg_ctx*, double* U, gx::RKArgs rk, cudaStream_t st, cudaEvent_t* ev);
+  // tangent-linear operator: the forward kernels on Dual<1> state and data
+  int (*configure_t)();
+  int (*rhs_t)(dg_ctx*, const gx::Dual<1>* U, gx::RKArgsT<gx::Dual<1>> rk, int rkmode, double mu_dot, cudaStream_t st);
+  // adjoint of one RHS evaluation at U with cotangent source cs; mode 0: Uout = dR^T Ut_bar,
+  // mode 1: reverse LSERK stage on (Ubar, Kbar); adds <Ut_bar, dR/dmu> to *acc (device)
+  int (*configure_a)();
+  int (*adj)(dg_ctx*, const double* U, gx::CotSrc cs, int mode, double* Uout, double* Ubar, double* Kbar,
+             double b_dt, double mRKA, double* acc, cudaStream_t st);
 };
 
 }  // namespace gxc

@@ -104,19 +104,19 @@ template <int NP> struct EPBof { static constexpr int v = (NP * NP * NP >= 128) 
 // =====================================================================================
 // k_prolong: ConsToPrim_Volume + ProlongToFace_CUDA + GetPrimitiveStateSurface
 // =====================================================================================
-template <int NP, typename R>
+template <int NP, typename R, typename S = double>
 __global__ void __launch_bounds__(EPBof<NP>::v * NP * NP * NP)
-k_prolong(const double* __restrict__ U, const int* __restrict__ E2S, const double* __restrict__ Lm,
+k_prolong(const S* __restrict__ U, const int* __restrict__ E2S, const double* __restrict__ Lm,
           const double* __restrict__ Lp, Gas<R> gas, Launch L, R* __restrict__ Pvol, R* __restrict__ Uf,
           R* __restrict__ Pf) {
   constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, EPB = EPBof<NP>::v, N = NP - 1;
   __shared__ SBasis<NP, double> sb;
-  __shared__ double Us[EPB][5][n3];
+  __shared__ S Us[EPB][5][n3];
   for (int t = threadIdx.x; t < NP; t += blockDim.x) { sb.Lm[t] = Lm[t]; sb.Lp[t] = Lp[t]; }
   const int e0 = blockIdx.x * EPB;
   const int nloc = min(EPB, L.nElems - e0);
   // coalesced load of the element block (AoS (5,n^3) per element in global memory)
-  const double* Ub = U + (size_t)e0 * 5 * n3;
+  const S* Ub = U + (size_t)e0 * 5 * n3;
   for (int t = threadIdx.x; t < nloc * 5 * n3; t += blockDim.x) {
     int el = t / (5 * n3), r = t - el * 5 * n3;
     Us[el][r % 5][r / 5] = Ub[t];
@@ -125,7 +125,7 @@ k_prolong(const double* __restrict__ U, const int* __restrict__ E2S, const doubl
   // volume prims
   for (int t = threadIdx.x; t < nloc * n3; t += blockDim.x) {
     int el = t / n3, node = t - el * n3;
-    const double u[5] = {Us[el][0][node], Us[el][1][node], Us[el][2][node], Us[el][3][node], Us[el][4][node]};
+    const S u[5] = {Us[el][0][node], Us[el][1][node], Us[el][2][node], Us[el][3][node], Us[el][4][node]};
     R prim[6], srho;
     cons_to_prim_d(u, gas, prim, srho);
     R* P = Pvol + (size_t)(e0 + el) * 7 * n3 + node;
@@ -143,7 +143,7 @@ k_prolong(const double* __restrict__ U, const int* __restrict__ E2S, const doubl
     int flip = E2S[(e * 6 + ls - 1) * 2 + 1];
     int a, b;
     s2v2(N, p, q, flip, ls, a, b);
-    double u[5];
+    S u[5];
     if (!L.gauss) {
       int node = face_node(n, ls, a, b, is_minus(ls) ? 0 : N);
 #pragma unroll
@@ -152,7 +152,7 @@ k_prolong(const double* __restrict__ U, const int* __restrict__ E2S, const doubl
       const double* Lv = is_minus(ls) ? sb.Lm : sb.Lp;
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
-        double s = Us[el][v][face_node(n, ls, a, b, 0)] * Lv[0];
+        S s = Us[el][v][face_node(n, ls, a, b, 0)] * Lv[0];
 #pragma unroll
         for (int l = 1; l < n; ++l) s = s + Us[el][v][face_node(n, ls, a, b, l)] * Lv[l];
         u[v] = s;
@@ -405,18 +405,21 @@ k_face(const R* __restrict__ Uf, const R* __restrict__ Pf, const R* __restrict__
 // (surfint.t90:352-586) + VAX_GPU(-1) + ApplyJacobian, and in RK mode the fused
 // VAXPB_OUT_VAXPB_IN stage update (vector.f90:163-183).
 // =====================================================================================
-struct RKArgs {
-  double* U;         // in/out (RK mode)
-  double* Ut_tmp;    // in/out (RK mode)
-  double* Ut;        // out (RHS mode)
+template <typename S>
+struct RKArgsT {
+  S* U;              // in/out (RK mode)
+  S* Ut_tmp;         // in/out (RK mode)
+  S* Ut;             // out (RHS mode)
   double mRKA, b_dt;
 };
+using RKArgs = RKArgsT<double>;
 
-template <int NP, typename R, int SPLIT, int PARAB>
+// S: type of the state arrays U, Ut, Ut_tmp (double; Dual<1> for the tangent-linear operator)
+template <int NP, typename R, int SPLIT, int PARAB, typename S = double>
 __global__ void __launch_bounds__(EPBof<NP>::v * NP * NP * NP)
-k_volume(const double* __restrict__ U, const R* __restrict__ Pvol, const R* __restrict__ Gvol,
+k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restrict__ Gvol,
          const R* __restrict__ Met, const R* __restrict__ Flux, const int* __restrict__ E2S, DevBasis<R> basis,
-         Gas<R> gas, Launch L, RKArgs rk, int rkmode) {
+         Gas<R> gas, Launch L, RKArgsT<S> rk, int rkmode) {
   constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, EPB = EPBof<NP>::v, N = NP - 1;
   constexpr int NA = (SPLIT >= 0) ? 19 : 15;  // staging: 10 node data + 9 metrics, or 15 fluxes
   __shared__ SBasis<NP, R> sb;
@@ -452,7 +455,7 @@ k_volume(const double* __restrict__ U, const R* __restrict__ Pvol, const R* __re
       }
       if (SPLIT < 0) {
         // EvalTransformedEulerFlux3D_fast (flux.f90:137-186) / EvalTransformedEulerDiffFlux3D (:509-614)
-        const double* Un = U + ((size_t)e * n3 + node) * 5;
+        const S* Un = U + ((size_t)e * n3 + node) * 5;
         const R m1 = (R)Un[1], m2 = (R)Un[2], m3 = (R)Un[3], E = (R)Un[4];
         const R p = P[4 * n3], srho = P[6 * n3];  // p: momentum pressure (p' in the mixed form)
         const R Ep = (E + p_abs(p, gas)) * srho;
@@ -508,7 +511,7 @@ k_volume(const double* __restrict__ U, const R* __restrict__ Pvol, const R* __re
   if constexpr (SPLIT >= 0) {
     __syncthreads();  // phase A reads of the staging area are complete
     if (active) {
-      const double* Un = U + ((size_t)e * n3 + node) * 5;
+      const S* Un = U + ((size_t)e * n3 + node) * 5;
       const R* P = Pvol + (size_t)e * 7 * n3 + node;
       const R* M = Met + (size_t)e * 10 * n3 + node;
       const R E = (R)Un[4];
@@ -623,9 +626,9 @@ k_volume(const double* __restrict__ U, const R* __restrict__ Pvol, const R* __re
     val = val * R(-1);
     val = val * sj;
     if (rkmode == 0) {
-      rk.Ut[g + v] = (double)val;
+      rk.Ut[g + v] = (S)val;
     } else {
-      const double utmp = rk.Ut_tmp[g + v] * rk.mRKA + (double)val;
+      const S utmp = rk.Ut_tmp[g + v] * rk.mRKA + (S)val;
       rk.Ut_tmp[g + v] = utmp;
       rk.U[g + v] = rk.U[g + v] + utmp * rk.b_dt;
     }

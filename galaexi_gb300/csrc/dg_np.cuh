@@ -42,10 +42,10 @@ bool vol_fits() {
   return volume_smem<R, SPL>() + sizeof(gx::SBasis<NP, R>) <= (size_t)smem_limit();
 }
 
-template <typename R, int SPL, int PAR>
+template <typename R, int SPL, int PAR, typename S = double>
 int cfg_vol() {
   if (!vol_fits<R, SPL>()) return DG_OK;  // variant not runnable on this device; rejected at launch
-  GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_volume<NP, R, SPL, PAR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_volume<NP, R, SPL, PAR, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)volume_smem<R, SPL>()),
               "k_volume shared-memory attribute");
   return DG_OK;
@@ -63,35 +63,34 @@ int configure() {
   return rc ? DG_ERR_CUDA : DG_OK;
 }
 
-template <typename R, int SPL>
-int vol(dg_ctx* ctx, PrecData<R>& P, const double* U, gx::RKArgs rk, int rkmode, cudaStream_t st) {
+template <typename R, int SPL, typename S = double>
+int vol(dg_ctx* ctx, PrecData<R>& P, const S* U, gx::RKArgsT<S> rk, int rkmode, const gx::Gas<R>& gas,
+        cudaStream_t st) {
   if (!vol_fits<R, SPL>()) {
     gxh::set_error("this N / precision / form needs more shared memory per block than the device offers");
     return DG_ERR_UNSUPPORTED;
   }
   const int grid = (ctx->nElems + EPB - 1) / EPB;
   const gx::DevBasis<R> b = gxc::dev_basis(P, NP);
-  const gx::Gas<R> gas = gxc::make_gas<R>(ctx->cfg, ctx->cfg.precision == DG_PRECISION_MIXED ? ctx->pref : 0.);
   const gx::Launch L = gxc::make_launch(ctx);
   if (ctx->cfg.parabolic)
-    gx::k_volume<NP, R, SPL, 1><<<grid, NT, volume_smem<R, SPL>(), st>>>(U, P.Pvol.p, P.Gvol.p, P.Met.p, P.Flux.p,
-                                                                     ctx->E2S.p, b, gas, L, rk, rkmode);
+    gx::k_volume<NP, R, SPL, 1, S><<<grid, NT, volume_smem<R, SPL>(), st>>>(U, P.Pvol.p, P.Gvol.p, P.Met.p, P.Flux.p,
+                                                                        ctx->E2S.p, b, gas, L, rk, rkmode);
   else
-    gx::k_volume<NP, R, SPL, 0><<<grid, NT, volume_smem<R, SPL>(), st>>>(U, P.Pvol.p, P.Gvol.p, P.Met.p, P.Flux.p,
-                                                                     ctx->E2S.p, b, gas, L, rk, rkmode);
+    gx::k_volume<NP, R, SPL, 0, S><<<grid, NT, volume_smem<R, SPL>(), st>>>(U, P.Pvol.p, P.Gvol.p, P.Met.p, P.Flux.p,
+                                                                        ctx->E2S.p, b, gas, L, rk, rkmode);
   return DG_OK;
 }
 
-template <typename R>
-int rhs(dg_ctx* ctx, PrecData<R>& P, const double* U, gx::RKArgs rk, int rkmode, cudaStream_t st,
-        cudaEvent_t* ev = nullptr) {
+// forward kernels up to (and excluding) the volume kernel: prims + face traces, lifting, face fluxes
+template <typename R, typename S = double>
+void rhs_front(dg_ctx* ctx, PrecData<R>& P, const S* U, const gx::Gas<R>& gas, cudaStream_t st, cudaEvent_t* ev,
+               bool face) {
   const int grid = (ctx->nElems + EPB - 1) / EPB;
-  if (ev) cudaEventRecord(ev[0], st);
   const gx::Launch L = gxc::make_launch(ctx);
   const gx::DevBasis<R> b = gxc::dev_basis(P, NP);
-  const gx::Gas<R> gas = gxc::make_gas<R>(ctx->cfg, ctx->cfg.precision == DG_PRECISION_MIXED ? ctx->pref : 0.);
-  const gx::DevBasis<double> bd = gxc::dev_basis(ctx->d, NP);  // FP64 face interpolation in both forms
-  gx::k_prolong<NP, R><<<grid, NT, 0, st>>>(U, ctx->E2S.p, bd.Lm, bd.Lp, gas, L, P.Pvol.p, P.Uf.p, P.Pf.p);
+  const gx::DevBasis<double> bd = gxc::dev_basis(ctx->d, NP);  // FP64 face interpolation in every form
+  gx::k_prolong<NP, R, S><<<grid, NT, 0, st>>>(U, ctx->E2S.p, bd.Lm, bd.Lp, gas, L, P.Pvol.p, P.Uf.p, P.Pf.p);
   ctx->launches++;
   if (ev) cudaEventRecord(ev[1], st);
   if (ctx->cfg.parabolic) {
@@ -100,24 +99,32 @@ int rhs(dg_ctx* ctx, PrecData<R>& P, const double* U, gx::RKArgs rk, int rkmode,
     ctx->launches++;
   }
   if (ev) cudaEventRecord(ev[2], st);
-  {
+  if (face) {
     const long long nt = (long long)ctx->nSides * NP * NP;
     const int fgrid = (int)((nt + 255) / 256);
     gx::k_face<R><<<fgrid, 256, 0, st>>>(P.Uf.p, P.Pf.p, P.Gf.p, P.Fgeo.p, gas, L, NP * NP, P.Flux.p);
     ctx->launches++;
   }
   if (ev) cudaEventRecord(ev[3], st);
+}
+
+template <typename R>
+int rhs(dg_ctx* ctx, PrecData<R>& P, const double* U, gx::RKArgs rk, int rkmode, cudaStream_t st,
+        cudaEvent_t* ev = nullptr) {
+  if (ev) cudaEventRecord(ev[0], st);
+  const gx::Gas<R> gas = gxc::make_gas<R>(ctx->cfg, ctx->cfg.precision == DG_PRECISION_MIXED ? ctx->pref : 0.);
+  rhs_front<R>(ctx, P, U, gas, st, ev, true);
   int vrc = DG_OK;
   switch (ctx->cfg.split_dg) {
-    case DG_SPLIT_NONE: vrc = vol<R, -1>(ctx, P, U, rk, rkmode, st); break;
+    case DG_SPLIT_NONE: vrc = vol<R, -1>(ctx, P, U, rk, rkmode, gas, st); break;
     default:
       if constexpr (NP >= 3) {
         switch (ctx->cfg.split_dg) {
-          case DG_SPLIT_SD: vrc = vol<R, 0>(ctx, P, U, rk, rkmode, st); break;
-          case DG_SPLIT_MO: vrc = vol<R, 1>(ctx, P, U, rk, rkmode, st); break;
-          case DG_SPLIT_DU: vrc = vol<R, 2>(ctx, P, U, rk, rkmode, st); break;
-          case DG_SPLIT_KG: vrc = vol<R, 3>(ctx, P, U, rk, rkmode, st); break;
-          default: vrc = vol<R, 4>(ctx, P, U, rk, rkmode, st); break;
+          case DG_SPLIT_SD: vrc = vol<R, 0>(ctx, P, U, rk, rkmode, gas, st); break;
+          case DG_SPLIT_MO: vrc = vol<R, 1>(ctx, P, U, rk, rkmode, gas, st); break;
+          case DG_SPLIT_DU: vrc = vol<R, 2>(ctx, P, U, rk, rkmode, gas, st); break;
+          case DG_SPLIT_KG: vrc = vol<R, 3>(ctx, P, U, rk, rkmode, gas, st); break;
+          default: vrc = vol<R, 4>(ctx, P, U, rk, rkmode, gas, st); break;
         }
       } else {
         gxh::set_error("split form needs N >= 2");
@@ -128,6 +135,118 @@ int rhs(dg_ctx* ctx, PrecData<R>& P, const double* U, gx::RKArgs rk, int rkmode,
   ctx->launches++;
   if (ev) cudaEventRecord(ev[4], st);
   GX_CUDA_TRY(cudaGetLastError(), "kernel launch");
+  return DG_OK;
+}
+
+// ---- tangent-linear operator: R = S = Dual<1>; mu_dot seeds the viscosity direction
+using D1 = gx::Dual<1>;
+
+int configure_t() {
+  if (lift_smem<D1>() + sizeof(gx::SBasis<NP, D1>) <= (size_t)smem_limit())
+    GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_lift<NP, D1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lift_smem<D1>()),
+                "k_lift shared-memory attribute");
+  int rc = cfg_vol<D1, -1, 0, D1>() | cfg_vol<D1, -1, 1, D1>();
+  if constexpr (NP >= 3) rc |= cfg_vol<D1, 3, 0, D1>() | cfg_vol<D1, 3, 1, D1>() | cfg_vol<D1, 4, 0, D1>() | cfg_vol<D1, 4, 1, D1>();
+  return rc ? DG_ERR_CUDA : DG_OK;
+}
+
+int rhs_t(dg_ctx* ctx, const D1* U, gx::RKArgsT<D1> rk, int rkmode, double mu_dot, cudaStream_t st) {
+  if (ctx->cfg.parabolic && lift_smem<D1>() + sizeof(gx::SBasis<NP, D1>) > (size_t)smem_limit()) {
+    gxh::set_error("tangent-linear lifting needs more shared memory per block than the device offers");
+    return DG_ERR_UNSUPPORTED;
+  }
+  gx::Gas<D1> gas = gxc::make_gas<D1>(ctx->cfg, 0.);
+  gas.mu.d[0] = mu_dot;
+  gas.lambda.d[0] = mu_dot * ctx->cfg.R * ctx->cfg.kappa / ((ctx->cfg.kappa - 1.) * ctx->cfg.Pr);
+  rhs_front<D1, D1>(ctx, ctx->t, U, gas, st, nullptr, true);
+  int vrc = DG_OK;
+  switch (ctx->cfg.split_dg) {
+    case DG_SPLIT_NONE: vrc = vol<D1, -1, D1>(ctx, ctx->t, U, rk, rkmode, gas, st); break;
+    case DG_SPLIT_KG:
+    case DG_SPLIT_PI:
+      if constexpr (NP >= 3) {
+        vrc = ctx->cfg.split_dg == DG_SPLIT_KG ? vol<D1, 3, D1>(ctx, ctx->t, U, rk, rkmode, gas, st)
+                                               : vol<D1, 4, D1>(ctx, ctx->t, U, rk, rkmode, gas, st);
+        break;
+      }
+      [[fallthrough]];
+    default:
+      gxh::set_error("tangent-linear operator: split forms PI and KG only");
+      return DG_ERR_UNSUPPORTED;
+  }
+  if (vrc != DG_OK) return vrc;
+  ctx->launches++;
+  GX_CUDA_TRY(cudaGetLastError(), "kernel launch");
+  return DG_OK;
+}
+
+// ---- adjoint
+constexpr size_t adj_vol_smem() { return sizeof(double) * (size_t)EPB * gx::adj_vol_words<NP>(); }
+bool adj_fits() { return adj_vol_smem() + sizeof(gx::SBasis<NP, double>) <= (size_t)smem_limit(); }
+
+template <int SPL, int PAR>
+int cfg_adj() {
+  if (!adj_fits()) return DG_OK;
+  GX_CUDA_TRY(cudaFuncSetAttribute(gx::ka_volume<NP, SPL, PAR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)adj_vol_smem()),
+              "ka_volume shared-memory attribute");
+  return DG_OK;
+}
+
+int configure_a() {
+  int rc = cfg_adj<-1, 0>() | cfg_adj<-1, 1>();
+  if constexpr (NP >= 3) rc |= cfg_adj<3, 0>() | cfg_adj<3, 1>() | cfg_adj<4, 0>() | cfg_adj<4, 1>();
+  return rc ? DG_ERR_CUDA : DG_OK;
+}
+
+template <int SPL>
+void adj_vol(dg_ctx* ctx, const double* U, gx::CotSrc cs, const gx::AdjLaunch& AL, double* part, cudaStream_t st) {
+  const int grid = (ctx->nElems + EPB - 1) / EPB;
+  const gx::DevBasis<double> b = gxc::dev_basis(ctx->d, NP);
+  PrecData<double>& P = ctx->d;
+  if (ctx->cfg.parabolic)
+    gx::ka_volume<NP, SPL, 1><<<grid, NT, adj_vol_smem(), st>>>(cs, U, P.Pvol.p, P.Gvol.p, P.Met.p, P.Fgeo.p, ctx->E2S.p,
+                                                               b, AL, ctx->GfB.p, ctx->UBv.p, ctx->JB.p, part);
+  else
+    gx::ka_volume<NP, SPL, 0><<<grid, NT, adj_vol_smem(), st>>>(cs, U, P.Pvol.p, P.Gvol.p, P.Met.p, P.Fgeo.p, ctx->E2S.p,
+                                                               b, AL, ctx->GfB.p, ctx->UBv.p, ctx->JB.p, part);
+}
+
+int adj(dg_ctx* ctx, const double* U, gx::CotSrc cs, int mode, double* Uout, double* Ubar, double* Kbar, double b_dt,
+        double mRKA, double* acc, cudaStream_t st) {
+  if (!adj_fits()) {
+    gxh::set_error("adjoint: this N needs more shared memory per block than the device offers");
+    return DG_ERR_UNSUPPORTED;
+  }
+  const dg_config& c = ctx->cfg;
+  const gx::Gas<double> gas = gxc::make_gas<double>(c, 0.);
+  rhs_front<double>(ctx, ctx->d, U, gas, st, nullptr, false);
+  gx::AdjLaunch AL;
+  AL.nElems = ctx->nElems; AL.nSides = ctx->nSides;
+  AL.gauss = c.node_type == DG_NODETYPE_GAUSS ? 1 : 0;
+  AL.riemann = c.riemann; AL.split = c.split_dg; AL.parabolic = c.parabolic;
+  AL.lift_mode = c.do_conservative_lifting ? 1 : 0;
+  AL.mu = c.mu0;
+  AL.lamc = c.R * c.kappa / ((c.kappa - 1.) * c.Pr);
+  AL.lambda = c.mu0 * AL.lamc;
+  AL.kappa = c.kappa; AL.sR = 1. / c.R;
+  const gx::DevBasis<double> b = gxc::dev_basis(ctx->d, NP);
+  const long long nf = (long long)ctx->nSides * NP * NP;
+  const int fgrid = (int)((nf + 127) / 128);
+  const int vgrid = (ctx->nElems + EPB - 1) / EPB;
+  gx::ka_face<NP><<<fgrid, 128, 0, st>>>(cs, ctx->d.Met.p, ctx->d.Uf.p, ctx->d.Pf.p, ctx->d.Gf.p, ctx->d.Fgeo.p,
+                                         ctx->S2E.p, b, gas, AL, ctx->UfB.p, ctx->GfB.p, ctx->part.p);
+  switch (c.split_dg) {
+    case DG_SPLIT_NONE: adj_vol<-1>(ctx, U, cs, AL, ctx->part.p + fgrid, st); break;
+    case DG_SPLIT_KG: if constexpr (NP >= 3) adj_vol<3>(ctx, U, cs, AL, ctx->part.p + fgrid, st); break;
+    default: if constexpr (NP >= 3) adj_vol<4>(ctx, U, cs, AL, ctx->part.p + fgrid, st); break;
+  }
+  gx::k_adj_sum<<<1, 256, 0, st>>>(ctx->part.p, fgrid + vgrid, acc);
+  const long long nn = (long long)ctx->nElems * NP * NP * NP;
+  gx::ka_final<NP><<<(int)((nn + 255) / 256), 256, 0, st>>>(ctx->UBv.p, ctx->d.Uf.p, ctx->UfB.p, ctx->JB.p, ctx->E2S.p,
+                                                           b, AL, mode, Uout, Ubar, Kbar, b_dt, mRKA);
+  ctx->launches += 4;
+  GX_CUDA_TRY(cudaGetLastError(), "adjoint kernel launch");
   return DG_OK;
 }
 
@@ -152,4 +271,5 @@ int cfl(dg_ctx* ctx, const double* U, double cflS, double dflS, double kpr, cuda
 
 #define GX_CAT2(a, b) a##b
 #define GX_CAT(a, b) GX_CAT2(a, b)
-extern const gxc::NPTable GX_CAT(gx_np_table_, GX_NP) = {configure<double>, configure<float>, rhs_d, rhs_f, cfl, stage_events};
+extern const gxc::NPTable GX_CAT(gx_np_table_, GX_NP) = {configure<double>, configure<float>, rhs_d, rhs_f, cfl,
+                                                         stage_events, configure_t, rhs_t, configure_a, adj};

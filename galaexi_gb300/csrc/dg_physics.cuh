@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include "../../include/galaexi_gb300.h"
+#include "dg_dual.cuh"
 
 namespace gx {
 
@@ -28,8 +29,8 @@ template <typename R> struct OffsetOf { static constexpr bool v = false; };
 template <> struct OffsetOf<float> { static constexpr bool v = true; };
 
 // ConsToPrim (idealgas/eos.f90:212-239) from the FP64 state: rho, u, v, w, p (p' in the mixed form), T, 1/rho
-template <typename R>
-__device__ __forceinline__ void cons_to_prim_d(const double u[5], const Gas<R>& g, R prim[6], R& srho) {
+template <typename R, typename S>
+__device__ __forceinline__ void cons_to_prim_d(const S u[5], const Gas<R>& g, R prim[6], R& srho) {
   if constexpr (!OffsetOf<R>::v) {
     srho = R(1) / (R)u[0];
     prim[0] = (R)u[0];

@@ -49,6 +49,11 @@ def _ptr(a):
     return ctypes.c_void_p(a.ctypes.data)
 
 
+def _tp(t):
+    """Device pointer of a torch tensor (None -> NULL)."""
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
+
+
 def basis(N, node_type):
     """InitInterpolationBasis + InitDGbasis: dict of the 1D operators (D, D_hat_T, ... column-major)."""
     n = N + 1
@@ -223,6 +228,77 @@ class DG:
             return dt.value, 1
         nat.check(rc, "dg_calc_timestep")
         return dt.value, 0
+
+    # -- integrals, tangent-linear and adjoint operators (FP64 form) ----------------------------
+    def integrals(self, U, stream=None):
+        """(mass, x-, y-, z-momentum, energy, kinetic energy) volume integrals of U in FP64."""
+        self._check_state(U)
+        out = (ctypes.c_double * 6)()
+        nat.check(nat.lib().dg_integrals(self._h, _tp(U), out, self._stream(stream)), "dg_integrals")
+        return list(out)
+
+    def kinetic_energy(self, U, grad=False, stream=None):
+        """J = integral of 0.5|m|^2/rho on the solution nodes; with grad=True also dJ/dU."""
+        self._check_state(U)
+        J = ctypes.c_double()
+        G = self._torch.empty_like(U) if grad else None
+        nat.check(nat.lib().dg_kinetic_energy(self._h, _tp(U), ctypes.byref(J), _tp(G), self._stream(stream)),
+                  "dg_kinetic_energy")
+        return (J.value, G) if grad else J.value
+
+    def rhs_jvp(self, U, Udot, mu_dot=0.0, stream=None):
+        """(Ut, Utdot): the operator and its exact directional derivative along (Udot, mu_dot)."""
+        self._check_state(U)
+        self._check_state(Udot)
+        Ut, Utd = self._torch.empty_like(U), self._torch.empty_like(U)
+        nat.check(nat.lib().dg_rhs_jvp(self._h, 0.0, _tp(U), _tp(Udot), float(mu_dot), _tp(Ut), _tp(Utd),
+                                       self._stream(stream)), "dg_rhs_jvp")
+        return Ut, Utd
+
+    def tlm_steps(self, dt, U, Udot, Ut_tmp, nSteps=1, mu_dot=0.0, stream=None):
+        """nSteps LSERK steps of U and its tangent Udot, in place."""
+        for x in (U, Udot, Ut_tmp):
+            self._check_state(x)
+        nat.check(nat.lib().dg_tlm_steps(self._h, 0.0, float(dt), int(nSteps), _tp(U), _tp(Udot), float(mu_dot),
+                                         _tp(Ut_tmp), self._stream(stream)), "dg_tlm_steps")
+
+    def rhs_vjp(self, U, Utbar, stream=None):
+        """(Ubar, mu_bar) = ((dR/dU)^T Utbar, <Utbar, dR/dmu>)."""
+        self._check_state(U)
+        self._check_state(Utbar)
+        Ub = self._torch.empty_like(U)
+        mb = ctypes.c_double()
+        nat.check(nat.lib().dg_rhs_vjp(self._h, 0.0, _tp(U), _tp(Utbar), _tp(Ub), ctypes.byref(mb),
+                                       self._stream(stream)), "dg_rhs_vjp")
+        return Ub, mb.value
+
+    def adjoint_forward(self, dt, nSteps, U0, budget_bytes, stream=None):
+        """Run and record nSteps steps from U0; returns (U_final, plan)."""
+        self._check_state(U0)
+        Uf = self._torch.empty_like(U0)
+        plan = ctypes.c_int()
+        nat.check(nat.lib().dg_adjoint_forward(self._h, 0.0, float(dt), int(nSteps), _tp(U0), _tp(Uf),
+                                               int(budget_bytes), ctypes.byref(plan), self._stream(stream)),
+                  "dg_adjoint_forward")
+        return Uf, plan.value
+
+    def adjoint_reverse(self, Ubar, stream=None):
+        """Ubar (in place): dJ/dU(t_end) -> dJ/dU(t0); returns dJ/dmu."""
+        self._check_state(Ubar)
+        mb = ctypes.c_double()
+        nat.check(nat.lib().dg_adjoint_reverse(self._h, _tp(Ubar), ctypes.byref(mb), self._stream(stream)),
+                  "dg_adjoint_reverse")
+        return mb.value
+
+    def adjoint_window(self, dt, nSteps, U0, budget_bytes, stream=None):
+        """Kinetic-energy objective after nSteps: (J, dJ/dU0, dJ/dmu, U_final)."""
+        self._check_state(U0)
+        G, Uf = self._torch.empty_like(U0), self._torch.empty_like(U0)
+        J, mb = ctypes.c_double(), ctypes.c_double()
+        nat.check(nat.lib().dg_adjoint_window(self._h, 0.0, float(dt), int(nSteps), _tp(U0), int(budget_bytes),
+                                              ctypes.byref(J), _tp(G), ctypes.byref(mb), _tp(Uf),
+                                              self._stream(stream)), "dg_adjoint_window")
+        return J.value, G, mb.value, Uf
 
     def gradients(self, stream=None):
         """Lifted gradients (GradUx, GradUy, GradUz) of the last RHS evaluation, each a float64 CUDA

@@ -184,6 +184,49 @@ int dg_check_state(dg_ctx* ctx, const double* d_U, long long* bad_count, void* s
  * DG_ERR_UNSUPPORTED for a non-parabolic operator, DG_ERR_ARG before the first RHS on the mesh. */
 int dg_get_gradients(dg_ctx* ctx, double* d_gradUx, double* d_gradUy, double* d_gradUz, void* stream);
 
+/* Volume integrals of the state in FP64 on the solution nodes (quadrature weights w_i w_j w_k / sJ,
+ * as the reference's analysis integrates, analyze.f90:383-484): out6 = {mass, x-, y-, z-momentum,
+ * total energy, kinetic energy 0.5|m|^2/rho}.  Synchronises the stream.  No counterpart as one call
+ * in the reference (its testcase analysis computes these on the host). */
+int dg_integrals(dg_ctx* ctx, const double* d_U, double* out6, void* stream);
+
+/* Kinetic-energy objective J = sum w_i w_j w_k / sJ * 0.5|m|^2/rho and, if d_dJdU is not null, its
+ * gradient dJ/dU (device array in the state layout).  Synchronises the stream. */
+int dg_kinetic_energy(dg_ctx* ctx, const double* d_U, double* J, double* d_dJdU, void* stream);
+
+/* ---- tangent-linear and adjoint operators (FP64 form; no counterpart in the reference) ---------
+ * Supported: Gauss or Gauss-Lobatto nodes, weak form or split form PI / KG, every Riemann solver,
+ * Euler or Navier-Stokes with BR1 lifting in strong form.  Others return DG_ERR_UNSUPPORTED.
+ *
+ * dg_rhs_jvp: Ut = R(U) (if d_Ut is not null) and Utdot = dR/dU . Udot + dR/dmu . mu_dot, the exact
+ * linearisation of the operator (forward-mode dual numbers through the same kernels).
+ * dg_tlm_steps: nSteps LSERK steps of U and of its tangent Udot (fixed dt). */
+int dg_rhs_jvp(dg_ctx* ctx, double t, const double* d_U, const double* d_Udot, double mu_dot, double* d_Ut,
+               double* d_Utdot, void* stream);
+int dg_tlm_steps(dg_ctx* ctx, double t, double dt, int nSteps, double* d_U, double* d_Udot, double mu_dot,
+                 double* d_Ut_tmp, void* stream);
+
+/* dg_rhs_vjp: d_Ubar = (dR/dU)^T d_Utbar at d_U, and *mu_bar = <d_Utbar, dR/dmu> (if not null). */
+int dg_rhs_vjp(dg_ctx* ctx, double t, const double* d_U, const double* d_Utbar, double* d_Ubar, double* mu_bar,
+               void* stream);
+
+/* Discrete adjoint of nSteps LSERK-W2 steps with fixed dt from d_U0.
+ * dg_adjoint_forward runs the window and records checkpoints in device memory of at most
+ * budget_bytes: every stage input if that fits (plan 1), else segment starts every k steps plus the
+ * stage inputs of one segment, recomputed during the reverse sweep (plan 2, one extra forward sweep),
+ * else segment starts plus the step starts of one segment plus one step's stage inputs (plan 3, two
+ * extra sweeps); *plan_out (if not null) receives the plan.  d_U_final (if not null) receives the
+ * end state.
+ * dg_adjoint_reverse: on entry d_Ubar holds dJ/dU(t_end); on exit dJ/dU(t0); *mu_bar = dJ/dmu.
+ * Consumes the recorded window.
+ * dg_adjoint_window: both, for J = the kinetic-energy integral of the end state (dg_kinetic_energy);
+ * writes J, dJ/dU0 and dJ/dmu. */
+int dg_adjoint_forward(dg_ctx* ctx, double t0, double dt, int nSteps, const double* d_U0, double* d_U_final,
+                       size_t budget_bytes, int* plan_out, void* stream);
+int dg_adjoint_reverse(dg_ctx* ctx, double* d_Ubar, double* mu_bar, void* stream);
+int dg_adjoint_window(dg_ctx* ctx, double t0, double dt, int nSteps, const double* d_U0, size_t budget_bytes,
+                      double* J, double* d_dJdU0, double* dJdmu, double* d_U_final, void* stream);
+
 /* Reference pressure of the mixed form (no counterpart in the reference).  With p_ref > 0 the FP32
  * bulk works with p' = p - p_ref (formed in FP64 from the FP64 state) in the momentum pressure terms
  * of the volume and surface fluxes.  The constant p_ref drops out of the operator for
