@@ -27,6 +27,7 @@
 // part).
 #pragma once
 #include "dg_kernels.cuh"
+#include "dg_riemann_vjp.cuh"
 
 namespace gx {
 
@@ -51,29 +52,6 @@ struct AdjLaunch {
   double mu, lambda, lamc;  // mu, lambda, lambda/mu (the thermal conductivity per unit viscosity)
   double kappa, sR;
 };
-
-// Transpose of ConsToPrim (idealgas/eos.f90:212-239) at the conservative state U, given cotangents of
-// rho, (u,v,w), p, T, 1/rho, and of the conservative E and momenta used directly; accumulates into Ub.
-__device__ __forceinline__ void prim_vjp(const double U[5], double kappaM1, double sR, double rb, double ub,
-                                         double vb, double wb, double pb, double Tb, double srhob, double Eb,
-                                         double m1b, double m2b, double m3b, double Ub[5]) {
-  const double srho = 1. / U[0];
-  const double vel[3] = {U[1] * srho, U[2] * srho, U[3] * srho};
-  const double p = kappaM1 * (U[4] - 0.5 * (U[1] * vel[0] + U[2] * vel[1] + U[3] * vel[2]));
-  // T = p * srho / R
-  pb += Tb * srho * sR;
-  srhob += Tb * p * sR;
-  // p = (kappa-1) (E - 0.5 m.v)
-  Eb += kappaM1 * pb;
-  const double hp = -0.5 * kappaM1 * pb;
-  m1b += hp * vel[0]; m2b += hp * vel[1]; m3b += hp * vel[2];
-  ub += hp * U[1]; vb += hp * U[2]; wb += hp * U[3];
-  // v = m * srho
-  m1b += ub * srho; m2b += vb * srho; m3b += wb * srho;
-  srhob += ub * U[1] + vb * U[2] + wb * U[3];
-  rb += -srhob * srho * srho;
-  Ub[0] += rb; Ub[1] += m1b; Ub[2] += m2b; Ub[3] += m3b; Ub[4] += Eb;
-}
 
 // Transpose of one directional BR1 viscous flux  f = normal_diff_flux(P, g, nv, mu, lambda)
 // (flux.f90:779-847) down to the cotangents of tau (6) and tq = tau.v + lambda grad T (3);
@@ -138,7 +116,7 @@ __device__ __forceinline__ void pair_sum_vjp(double rs, double us, double vs, do
 // ---------------------------------------------------------------------------------------------
 // ka_face: thread per face node
 // ---------------------------------------------------------------------------------------------
-template <int NP>
+template <int NP, bool HAND>
 __global__ void __launch_bounds__(128)
 ka_face(CotSrc cs, const double* __restrict__ Met, const double* __restrict__ Uf, const double* __restrict__ Pf,
         const double* __restrict__ Gf, const double* __restrict__ Fgeo, const int* __restrict__ S2E,
@@ -188,7 +166,21 @@ ka_face(CotSrc cs, const double* __restrict__ Met, const double* __restrict__ Uf
       ULv[v] = Uf[(size_t)side * 5 * n2 + v * n2 + pq];
       URv[v] = Uf[(S + side) * 5 * n2 + v * n2 + pq];
     }
-    {
+    if constexpr (HAND) {
+      const double nv[3] = {fg[0], fg[n2], fg[2 * n2]};
+      const double t1[3] = {fg[3 * n2], fg[4 * n2], fg[5 * n2]};
+      const double t2[3] = {fg[6 * n2], fg[7 * n2], fg[8 * n2]};
+      Ext<double> Le, Re;
+      make_ext(ULv, nv, t1, t2, gas.kappaM1, Le);
+      make_ext(URv, nv, t1, t2, gas.kappaM1, Re);
+      const double Fr[5] = {Fb[0], nv[0] * Fb[1] + nv[1] * Fb[2] + nv[2] * Fb[3],
+                            t1[0] * Fb[1] + t1[1] * Fb[2] + t1[2] * Fb[3], t2[0] * Fb[1] + t2[1] * Fb[2] + t2[2] * Fb[3],
+                            Fb[4]};
+      ExtB Lb = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0}, Rb = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+      riemann_solver_vjp(L.riemann, L.split, Le, Re, gas.kappa, Fr, Lb, Rb);
+      ext_vjp(ULv, Le, Lb, nv, t1, t2, gas.kappaM1, L.sR, ULb);
+      ext_vjp(URv, Re, Rb, nv, t1, t2, gas.kappaM1, L.sR, URb);
+    } else {
       using D10 = Dual<10>;
       D10 UL[5], UR[5], PL[6], PR[6], sL, sR_, F[5];
 #pragma unroll

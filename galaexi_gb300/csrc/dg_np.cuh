@@ -234,8 +234,12 @@ int adj(dg_ctx* ctx, const double* U, gx::CotSrc cs, int mode, double* Uout, dou
   const long long nf = (long long)ctx->nSides * NP * NP;
   const int fgrid = (int)((nf + 127) / 128);
   const int vgrid = (ctx->nElems + EPB - 1) / EPB;
-  gx::ka_face<NP><<<fgrid, 128, 0, st>>>(cs, ctx->d.Met.p, ctx->d.Uf.p, ctx->d.Pf.p, ctx->d.Gf.p, ctx->d.Fgeo.p,
-                                         ctx->S2E.p, b, gas, AL, ctx->UfB.p, ctx->GfB.p, ctx->part.p);
+  if (gx::riemann_vjp_supported_host(c.riemann, c.split_dg))
+    gx::ka_face<NP, true><<<fgrid, 128, 0, st>>>(cs, ctx->d.Met.p, ctx->d.Uf.p, ctx->d.Pf.p, ctx->d.Gf.p, ctx->d.Fgeo.p,
+                                                 ctx->S2E.p, b, gas, AL, ctx->UfB.p, ctx->GfB.p, ctx->part.p);
+  else
+    gx::ka_face<NP, false><<<fgrid, 128, 0, st>>>(cs, ctx->d.Met.p, ctx->d.Uf.p, ctx->d.Pf.p, ctx->d.Gf.p, ctx->d.Fgeo.p,
+                                                  ctx->S2E.p, b, gas, AL, ctx->UfB.p, ctx->GfB.p, ctx->part.p);
   switch (c.split_dg) {
     case DG_SPLIT_NONE: adj_vol<-1>(ctx, U, cs, AL, ctx->part.p + fgrid, st); break;
     case DG_SPLIT_KG: if constexpr (NP >= 3) adj_vol<3>(ctx, U, cs, AL, ctx->part.p + fgrid, st); break;
