@@ -56,6 +56,10 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-profile", action="store_true", help="skip the per-kernel event timing and peak kernels")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the mixed-precision comparisons and the adjoint measurement")
+    ap.add_argument("--adjoint-fd", type=int, default=0,
+                    help="central-difference check of the adjoint gradient along this many random directions")
     return ap.parse_args()
 
 
@@ -245,6 +249,11 @@ def run_ours(args, world, rank, local):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args.workload)
+    extras = {}
+    if not args.no_extras and args.precision == "fp64":
+        extras["mixed_vs_fp64"] = mixed_vs_fp64_tgv(args.workload, args.steps, stream)
+        extras["mixed_vs_fp64_curved_br2"] = mixed_vs_fp64_curved_br2(stream)
+        extras["adjoint"] = adjoint_tgv(stream, fd_dirs=args.adjoint_fd)
     if rank == 0:
         line = {"metric": "DOF-stage updates/s", "value": value, "unit": "DOF-stage/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -256,7 +265,174 @@ def run_ours(args, world, rank, local):
                            "dt": dt, "l2": "inputs larger than L2 (state 283 MB)", "parallelism": "replicas"},
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
                 "gpu_launches": launches, "bad_nodes_after": bad}
+        line.update(extras)
         print(json.dumps(line), flush=True)
+
+
+def timed(fn, stream):
+    """Run fn() between CUDA events on the stream; returns (ms, result)."""
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    r = fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1), r
+
+
+def mixed_vs_fp64_tgv(workload, steps, stream):
+    """Mixed form against the FP64 form on the TGV workload: same initial state, same dt, `steps`
+    LSERK steps each; kinetic-energy and L2 differences of the end states, DOF-stage/s ratio."""
+    import torch
+    import galaexi_gb300 as gx
+    w = WORKLOADS[workload]
+    mesh = gx.Mesh(w["N"], 2, w["ne"], w["ne"], w["ne"], (-math.pi,) * 3, (math.pi,) * 3)
+    U0 = torch.from_numpy(gx.tgv_state(mesh, mach=0.1, R=TGV_R)).cuda()
+    out, ops = {}, {}
+    for prec in ("fp64", "mixed"):
+        cfg = gx.config(N=w["N"], NodeType="gauss-lobatto", Riemann=w["Riemann"], SplitDG=w["SplitDG"],
+                        parabolic=w["parabolic"], mu0=w["mu0"], R=TGV_R, precision=prec)
+        ops[prec] = gx.DG(cfg, mesh)
+    dt, _ = ops["fp64"].CalcTimeStep(U0, CFL, DFL)
+    for prec, op in ops.items():
+        U, K = U0.clone(), torch.zeros_like(U0)
+        op.TimeStepByLSERKW2(0.0, dt, U, K)  # warm-up step (also fixes the mixed form's pressure offset)
+        U, K = U0.clone(), torch.zeros_like(U0)
+        ms, _ = timed(lambda: op.TimeStepByLSERKW2(0.0, dt, U, K, nSteps=steps), stream)
+        out[prec] = (ms, U, ops["fp64"].integrals(U))
+    ke64, kem = out["fp64"][2][5], out["mixed"][2][5]
+    res = {"workload": workload, "steps": steps, "dt": dt,
+           "speedup": out["fp64"][0] / out["mixed"][0],
+           "dof_stage_per_s_fp64": mesh.nDOF * 5 * steps / (out["fp64"][0] * 1e-3),
+           "dof_stage_per_s_mixed": mesh.nDOF * 5 * steps / (out["mixed"][0] * 1e-3),
+           "ke_rel_err": abs(kem - ke64) / abs(ke64),
+           "l2_rel": float((out["mixed"][1] - out["fp64"][1]).norm() / out["fp64"][1].norm()),
+           "mass_rel_diff": abs(out["mixed"][2][0] - out["fp64"][2][0]) / abs(out["fp64"][2][0]),
+           "reference": "FP64 path of this library (matches the oracle to <=1e-12 per evaluation)"}
+    for op in ops.values():
+        op.close()
+    return res
+
+
+def mixed_vs_fp64_curved_br2(stream, steps=500):
+    """Mixed form against the FP64 form on the curved-box BR2 case: Navier-Stokes, N=5 Gauss nodes,
+    weak form, HLLC, BR2 (etaBR2 = 2), 32^3 elements on [0,1]^3 with every node displaced by
+    0.05 sin(2 pi x) sin(2 pi y) sin(2 pi z), uniform flow rho=1, v=(0.3,0.2,0.1), p=1/1.4 plus
+    seeded Gaussian noise 1e-3 on each conserved variable, mu=1e-3; 500 steps."""
+    import numpy as np
+    import torch
+    import galaexi_gb300 as gx
+    N, ne = 5, 32
+    mesh = gx.Mesh(N, 1, ne, ne, ne, (0.0,) * 3, (1.0,) * 3, deform=0.05)
+    U = gx.fill_ini(mesh, 1, [1.0, 0.3, 0.2, 0.1, 1.0 / 1.4])
+    rng = np.random.default_rng(20261203)
+    U = U + 1e-3 * rng.standard_normal(U.size).reshape(U.shape)
+    U0 = torch.from_numpy(U).cuda()
+    ops = {}
+    for prec in ("fp64", "mixed"):
+        cfg = gx.config(N=N, NodeType="gauss", Riemann="hllc", parabolic=True, mu0=1e-3, Lifting="br2", etaBR2=2.0,
+                        precision=prec)
+        ops[prec] = gx.DG(cfg, mesh)
+    # CFLscale 0.9; DFLscale 0.45: the BR2 penalty (etaBR2 = 2) raises the viscous spectral radius
+    # above the BR1 value the DFL alpha tables are made for -- with DFLscale 0.6 the oracle itself
+    # diverges on this case within 10 steps at matching viscous/convective ratio, 0.45 is stable
+    dt, _ = ops["fp64"].CalcTimeStep(U0, 0.9, 0.45)
+    I0 = ops["fp64"].integrals(U0)
+    out = {}
+    for prec, op in ops.items():
+        Uw, K = U0.clone(), torch.zeros_like(U0)
+        op.TimeStepByLSERKW2(0.0, dt, Uw, K)
+        Ur, K = U0.clone(), torch.zeros_like(U0)
+        ms, _ = timed(lambda: op.TimeStepByLSERKW2(0.0, dt, Ur, K, nSteps=steps), stream)
+        out[prec] = (ms, Ur, ops["fp64"].integrals(Ur))
+    res = {"workload": "curved_n5_gauss_32cube_weak_hllc_br2", "steps": steps, "dt": dt, "cfl": 0.9, "dfl": 0.45,
+           "speedup": out["fp64"][0] / out["mixed"][0],
+           "dof_stage_per_s_fp64": mesh.nDOF * 5 * steps / (out["fp64"][0] * 1e-3),
+           "dof_stage_per_s_mixed": mesh.nDOF * 5 * steps / (out["mixed"][0] * 1e-3),
+           "l2_rel": float((out["mixed"][1] - out["fp64"][1]).norm() / out["fp64"][1].norm()),
+           "mass_drift_fp64": (out["fp64"][2][0] - I0[0]) / I0[0],
+           "mass_drift_mixed": (out["mixed"][2][0] - I0[0]) / I0[0],
+           "energy_drift_fp64": (out["fp64"][2][4] - I0[4]) / I0[4],
+           "energy_drift_mixed": (out["mixed"][2][4] - I0[4]) / I0[4],
+           "ke_rel_err": abs(out["mixed"][2][5] - out["fp64"][2][5]) / abs(out["fp64"][2][5]),
+           "reference": "FP64 path of this library (matches the oracle to <=1e-12 per evaluation)"}
+    for op in ops.values():
+        op.close()
+    return res
+
+
+def adjoint_tgv(stream, steps=200, fd_dirs=0):
+    """Discrete adjoint on the N=5, 16^3 TGV (split PI, Roe, BR1, FP64): J = kinetic-energy integral
+    after `steps` LSERK steps at fixed dt; gradient w.r.t. the initial state and mu.  Reports the
+    adjoint (record + reverse) to forward wall-time ratio and, with fd_dirs > 0, central differences
+    (eps = 1e-6) along seeded random unit directions (default_rng(4))."""
+    import numpy as np
+    import torch
+    import galaexi_gb300 as gx
+    N, ne, mu = 5, 16, 1 / 1600.0
+    cfg = gx.config(N=N, NodeType="gauss-lobatto", Riemann="roe", SplitDG="pi", parabolic=True, mu0=mu, R=TGV_R)
+    mesh = gx.Mesh(N, 2, ne, ne, ne, (-math.pi,) * 3, (math.pi,) * 3)
+    U0 = torch.from_numpy(gx.tgv_state(mesh, mach=0.1, R=TGV_R)).cuda()
+    op = gx.DG(cfg, mesh)
+    dt, _ = op.CalcTimeStep(U0, CFL, DFL)
+    budget = 180 << 30
+
+    def fwd(o=op, U_init=U0):
+        U, K = U_init.clone(), torch.zeros_like(U_init)
+        o.TimeStepByLSERKW2(0.0, dt, U, K, nSteps=steps)
+        return U
+
+    fwd()
+    op.adjoint_window(dt, 2, U0, budget)
+    ms_f, Uf = timed(fwd, stream)
+    ms_a, (J, G, dJdmu, _) = timed(lambda: op.adjoint_window(dt, steps, U0, budget), stream)
+    plan = 1 if 5 * steps * U0.numel() * 8 <= budget else 2  # the window's checkpoint rule (plan 1: all stage inputs)
+    res = {"workload": "tgv_n5_16cube_split_pi_roe_br1_adjoint", "steps": steps, "dt": dt, "nDOF": mesh.nDOF,
+           "forward_ms": ms_f, "adjoint_ms": ms_a, "adjoint_over_forward": ms_a / ms_f,
+           "checkpoint_plan": plan, "checkpoint_budget_gb": budget / 2 ** 30,
+           "J": J, "dJ_dmu": dJdmu, "grad_norm": float(G.norm())}
+    if fd_dirs > 0:
+        rng = np.random.default_rng(4)
+        dirs = []
+        for _ in range(fd_dirs):
+            v = torch.from_numpy(rng.standard_normal(tuple(U0.shape))).cuda()
+            dirs.append(v / v.norm())
+        # central differences at eps = 1e-6 (and 1e-4 to show the round-off share of the difference)
+        for eps in (1e-6, 1e-4):
+            errs = []
+            for v in dirs:
+                Jp = op.kinetic_energy(fwd(op, U0 + eps * v))
+                Jm = op.kinetic_energy(fwd(op, U0 - eps * v))
+                fd = (Jp - Jm) / (2 * eps)
+                ad = float((G * v).sum())
+                errs.append(abs(fd - ad) / abs(ad))
+            res["fd_max_rel_err_eps%.0e" % eps] = max(errs)
+        res["fd_directions"] = fd_dirs
+        # exact directional derivatives from the tangent-linear model (dual numbers through the same
+        # 200 steps): <dJ/dU(t_end), Udot(t_end)> against <dJ/dU0, v>
+        errs = []
+        for v in dirs[:4]:
+            U, Ud, K = U0.clone(), v.clone(), torch.zeros_like(U0)
+            op.tlm_steps(dt, U, Ud, K, nSteps=steps)
+            _, Gend = op.kinetic_energy(U, grad=True)
+            tl = float((Gend * Ud).sum())
+            ad = float((G * v).sum())
+            errs.append(abs(tl - ad) / abs(ad))
+        res["tlm_max_rel_err"] = max(errs)
+        res["tlm_directions"] = min(4, fd_dirs)
+        ops = {}
+        eps = 1e-6
+        for sgn in (1, -1):
+            c2 = gx.config(N=N, NodeType="gauss-lobatto", Riemann="roe", SplitDG="pi", parabolic=True,
+                           mu0=mu + sgn * eps, R=TGV_R)
+            o2 = gx.DG(c2, mesh)
+            ops[sgn] = o2.kinetic_energy(fwd(o2, U0))
+            o2.close()
+        fdm = (ops[1] - ops[-1]) / (2 * eps)
+        res["fd_mu_rel_err"] = abs(fdm - dJdmu) / abs(dJdmu)
+    op.close()
+    return res
 
 
 def profile_roofline(args, op, U, dt, stream, nDOF):

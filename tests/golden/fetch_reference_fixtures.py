@@ -13,6 +13,9 @@ tree is absent:
   ProlongToFace_{G,GL}3D.bin   prolonged face data
   SurfIntFlux.bin              random face flux                       (unitTests/SurfInt.f90)
   SurfInt_{G,GL}3D.bin         surface-integral result
+  TGV_Re1600_Split_TGVAnalysis_Reference.csv
+                               Taylor-Green vortex analysis of the split-form regression run
+                               (regressioncheck/checks/tgv/split/), one row every 10 time steps
 
 Usage:  python tests/golden/fetch_reference_fixtures.py [/path/to/reference]
 """
@@ -33,11 +36,19 @@ FILES = [
 ]
 
 
+REGRESSION = [
+    ("regressioncheck/checks/tgv/split", "TGV_Re1600_Split_TGVAnalysis_Reference.csv"),
+]
+
+
 def main(ref_root):
     here = os.path.dirname(os.path.abspath(__file__))
     for name in FILES:
         src = os.path.join(ref_root, "unitTests", name)
         shutil.copyfile(src, os.path.join(here, name))
+        print("copied", name)
+    for sub, name in REGRESSION:
+        shutil.copyfile(os.path.join(ref_root, sub, name), os.path.join(here, name))
         print("copied", name)
 
 
