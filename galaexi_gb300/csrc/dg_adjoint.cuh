@@ -16,8 +16,9 @@
 //                                    flux, gradient cotangents (volume + face traces), transposed
 //                                    lifting volume integral, ConsToPrim -> U cotangent (volume part),
 //                                    and the per-element share of the lifting jump cotangent
-//   ka_final  thread per node        transposed ProlongToFace of the face cotangents (incl. the lifting
-//                                    jumps through ConsToPrim of the face states), and the reverse RK
+//   ka_jump   thread per face node   the lifting jump cotangents of both elements through ConsToPrim of
+//                                    the face states, added to the face cotangents (Navier-Stokes)
+//   ka_final  thread per node        transposed ProlongToFace of the face cotangents, and the reverse RK
 //                                    stage  Ubar += dR^T(K_bar + b dt Ubar),  K_bar = -RKA (K_bar + b dt Ubar)
 // The viscosity derivative <Ut_bar, dR/dmu> is accumulated on the way (R is linear in mu at fixed
 // Prandtl number): per-block partial sums, reduced in a fixed order by k_adj_sum.
@@ -587,16 +588,45 @@ ka_volume(CotSrc cs, const double* __restrict__ U, const double* __restrict__ Pv
 }
 
 // ---------------------------------------------------------------------------------------------
+// ka_jump: thread per face node; the lifting surface term 0.5 SE (P_slave - P_master) n transposed
+// through ConsToPrim of both face states, added to the face-state cotangents in place
+// ---------------------------------------------------------------------------------------------
+static __global__ void __launch_bounds__(256)
+ka_jump(const double* __restrict__ Uf, const double* __restrict__ JB, AdjLaunch L, int n2, double* __restrict__ UfB) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)L.nSides * n2) return;
+  const int side = (int)(t / n2), pq = (int)(t - (long long)side * n2);
+  const size_t S = L.nSides;
+  double jb[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v)
+    jb[v] = JB[(size_t)side * 5 * n2 + v * n2 + pq] + JB[(S + side) * 5 * n2 + v * n2 + pq];
+#pragma unroll
+  for (int slot = 0; slot < 2; ++slot) {
+    const double sg = slot == 0 ? -1. : 1.;
+    double uf[5], fb[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      uf[v] = Uf[((size_t)slot * S + side) * 5 * n2 + v * n2 + pq];
+      fb[v] = UfB[((size_t)slot * S + side) * 5 * n2 + v * n2 + pq];
+    }
+    prim_vjp(uf, L.kappa - 1., L.sR, sg * jb[0], sg * jb[1], sg * jb[2], sg * jb[3], 0., sg * jb[4], 0., 0., 0., 0.,
+             0., fb);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) UfB[((size_t)slot * S + side) * 5 * n2 + v * n2 + pq] = fb[v];
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
 // ka_final: thread per node; transposed ProlongToFace of the face cotangents, then output
 // mode 0: Ubar_out = dR^T Ut_bar;  mode 1 (reverse RK stage): K = Kbar + b dt Ubar,
 //   Ubar += dR^T K,  Kbar = mRKA K   (Ut_bar = K was the cotangent source of the stage)
 // ---------------------------------------------------------------------------------------------
 template <int NP>
 __global__ void __launch_bounds__(256)
-ka_final(const double* __restrict__ UBv, const double* __restrict__ Uf, const double* __restrict__ UfB,
-         const double* __restrict__ JB, const int* __restrict__ E2S, DevBasis<double> basis, AdjLaunch L,
-         int mode, double* __restrict__ Uout, double* __restrict__ Ubar, double* __restrict__ Kbar, double b_dt,
-         double mRKA) {
+ka_final(const double* __restrict__ UBv, const double* __restrict__ UfB, const int* __restrict__ E2S,
+         DevBasis<double> basis, AdjLaunch L, int mode, double* __restrict__ Uout, double* __restrict__ Ubar,
+         double* __restrict__ Kbar, double b_dt, double mRKA) {
   constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, N = NP - 1;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)L.nElems * n3) return;
@@ -627,23 +657,8 @@ ka_final(const double* __restrict__ UBv, const double* __restrict__ Uf, const do
     int p, q;
     s2v2_inv(N, a, b, flip, ls, p, q);
     const int pq = p + n * q;
-    double fb[5];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) fb[v] = UfB[((size_t)slot * S + side) * 5 * n2 + v * n2 + pq];
-    if (L.parabolic) {
-      // lifting surface term 0.5 SE (P_slave - P_master) n: the face primitives' cotangents
-      double jb[5];
-      const double sg = slot == 0 ? -1. : 1.;
-#pragma unroll
-      for (int v = 0; v < 5; ++v)
-        jb[v] = sg * (JB[(size_t)side * 5 * n2 + v * n2 + pq] + JB[(S + side) * 5 * n2 + v * n2 + pq]);
-      double uf[5];
-#pragma unroll
-      for (int v = 0; v < 5; ++v) uf[v] = Uf[((size_t)slot * S + side) * 5 * n2 + v * n2 + pq];
-      prim_vjp(uf, L.kappa - 1., L.sR, jb[0], jb[1], jb[2], jb[3], 0., jb[4], 0., 0., 0., 0., 0., fb);
-    }
-#pragma unroll
-    for (int v = 0; v < 5; ++v) Ub[v] += Lv * fb[v];
+    for (int v = 0; v < 5; ++v) Ub[v] += Lv * UfB[((size_t)slot * S + side) * 5 * n2 + v * n2 + pq];
   }
   if (mode == 0) {
 #pragma unroll

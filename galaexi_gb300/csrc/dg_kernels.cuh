@@ -187,6 +187,8 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
   const int e0 = blockIdx.x * EPB;
   const int nloc = min(EPB, L.nElems - e0);
   const int liftc[5] = {0, 1, 2, 3, 5};
+  const bool facepass = !L.gauss && !L.br2;
+  const R sigflux = (L.lift_mode == 2) ? R(1) : R(-1);
   for (int t = threadIdx.x; t < nloc * 5 * n3; t += blockDim.x) {
     int el = t / (5 * n3), r = t - el * 5 * n3;
     int c = r / n3, node = r - c * n3;
@@ -251,11 +253,18 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
 #pragma unroll
         for (int v = 0; v < 5; ++v) Gs[el][d * 5 + v][node] = g[d][v];
     }
+    if (facepass) {
+      // Gauss-Lobatto BR1: the surface part is added below by face-node threads
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int v = 0; v < 5; ++v) Gs[el][d * 5 + v][node] = g[d][v];
+      continue;
+    }
     // surface part (SurfInt_Device_Single_Flux, surfint.t90:591-725) of the BR1 flux
     // 0.5*SurfElem*(sig*U_master + U_slave) (Lifting_FillFlux, lifting_fillflux.t90:39-103) times the
     // normal (Lifting_FillFlux_NormVec, :212-256) times L_hat and the Jacobian; the scalar factors of
     // one face are folded into one weight.
-    const R sigflux = (L.lift_mode == 2) ? R(1) : R(-1);
 #pragma unroll
     for (int ls = 1; ls <= 6; ++ls) {
       int a, b, l;
@@ -301,6 +310,51 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
       }
   }
   __syncthreads();
+  if (facepass) {
+    // surface part on Gauss-Lobatto nodes, one thread per face node, one normal direction per pass
+    // (the two faces of a direction share no node); only face nodes do surface work, so no warp
+    // executes the side bodies of nodes that are not on that face
+#pragma unroll 1
+    for (int dir = 0; dir < 3; ++dir) {
+      for (int t = threadIdx.x; t < nloc * 2 * n2; t += blockDim.x) {
+        const int el = t / (2 * n2), r = t - el * 2 * n2;
+        const bool minus = r < n2;
+        const int ab = minus ? r : r - n2;
+        const int a = ab % n, b = ab / n;
+        const int ls = dir == 0 ? (minus ? L_XI_MINUS : L_XI_PLUS)
+                                : (dir == 1 ? (minus ? L_ETA_MINUS : L_ETA_PLUS) : (minus ? L_ZETA_MINUS : L_ZETA_PLUS));
+        const int node = face_node(n, ls, a, b, minus ? 0 : N);
+        const int e = e0 + el;
+        const R Lhat = minus ? sb.Lhm[0] : sb.Lhp[N];
+        const int side = E2S[(e * 6 + ls - 1) * 2 + 0];
+        const int flip = E2S[(e * 6 + ls - 1) * 2 + 1];
+        int p, q;
+        s2v2_inv(N, a, b, flip, ls, p, q);
+        const int pq = p + n * q;
+        const R* pm = Pf + (size_t)side * 6 * n2 + pq;
+        const R* ps = Pf + ((size_t)L.nSides + side) * 6 * n2 + pq;
+        const R* fg = Fgeo + (size_t)side * 10 * n2 + pq;
+        const R sj = Met[((size_t)e * 10 + 9) * n3 + node];
+        const R sig = (L.lift_mode == 2) ? ((flip == 0) ? R(1) : R(-1)) : R(1);
+        const R wgt = sig * Lhat * R(0.5) * fg[9 * n2] * sj;
+        const R nvv[3] = {wgt * fg[0], wgt * fg[n2], wgt * fg[2 * n2]};
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+          const int c = liftc[v];
+          const R fl = sigflux * pm[c * n2] + ps[c * n2];
+#pragma unroll
+          for (int d = 0; d < 3; ++d) Gs[el][d * 5 + v][node] = Gs[el][d * 5 + v][node] + fl * nvv[d];
+        }
+      }
+      __syncthreads();
+    }
+    for (int t = threadIdx.x; t < nloc * n3; t += blockDim.x) {
+      const int el = t / n3, node = t - el * n3;
+      R* G = Gvol + (size_t)(e0 + el) * 15 * n3 + node;
+#pragma unroll
+      for (int c = 0; c < 15; ++c) G[c * n3] = Gs[el][c][node];
+    }
+  }
   // ProlongToFaceLifting
   for (int t = threadIdx.x; t < nloc * 6 * n2; t += blockDim.x) {
     int el = t / (6 * n2), r = t - el * 6 * n2;

@@ -246,9 +246,13 @@ int adj(dg_ctx* ctx, const double* U, gx::CotSrc cs, int mode, double* Uout, dou
     default: if constexpr (NP >= 3) adj_vol<4>(ctx, U, cs, AL, ctx->part.p + fgrid, st); break;
   }
   gx::k_adj_sum<<<1, 256, 0, st>>>(ctx->part.p, fgrid + vgrid, acc);
+  if (c.parabolic) {
+    gx::ka_jump<<<(int)((nf + 255) / 256), 256, 0, st>>>(ctx->d.Uf.p, ctx->JB.p, AL, NP * NP, ctx->UfB.p);
+    ctx->launches++;
+  }
   const long long nn = (long long)ctx->nElems * NP * NP * NP;
-  gx::ka_final<NP><<<(int)((nn + 255) / 256), 256, 0, st>>>(ctx->UBv.p, ctx->d.Uf.p, ctx->UfB.p, ctx->JB.p, ctx->E2S.p,
-                                                           b, AL, mode, Uout, Ubar, Kbar, b_dt, mRKA);
+  gx::ka_final<NP><<<(int)((nn + 255) / 256), 256, 0, st>>>(ctx->UBv.p, ctx->UfB.p, ctx->E2S.p, b, AL, mode, Uout,
+                                                           Ubar, Kbar, b_dt, mRKA);
   ctx->launches += 4;
   GX_CUDA_TRY(cudaGetLastError(), "adjoint kernel launch");
   return DG_OK;
