@@ -481,6 +481,11 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
   R* A = reinterpret_cast<R*>(smem_raw);             // [EPB][NA][n3]
   R* AccD = A + (size_t)EPB * NA * n3;               // [EPB][3][5][n3]  (split form only)
   load_basis(sb, basis);
+  if constexpr (SPLIT == DG_SPLIT_PI) {
+    // PI pair fluxes are evaluated as 8F (see phase B): fold the 1/8 into DVolSurf (exact scaling)
+    __syncthreads();
+    for (int t = threadIdx.x; t < NP * NP; t += blockDim.x) sb.DVS[t] = sb.DVS[t] * R(0.125);
+  }
   const int e0 = blockIdx.x * EPB;
   const int nloc = min(EPB, L.nElems - e0);
   const int tid = threadIdx.x;
@@ -578,7 +583,7 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
       Ae[5 * n3 + node] = uu;
       Ae[6 * n3 + node] = vv;
       Ae[7 * n3 + node] = ww;
-      Ae[8 * n3 + node] = pm;
+      Ae[8 * n3 + node] = (SPLIT == DG_SPLIT_PI) ? R(4) * pm : pm;  // PI: 4p (exact scaling)
       Ae[9 * n3 + node] = R(0);
 #pragma unroll
       for (int c = 0; c < 9; ++c) Ae[(10 + c) * n3 + node] = M[c * n3];
@@ -619,7 +624,21 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
           B_.pm = Al[8 * n3 + nb];
           const R Ms0 = ma0 + Al[mc * n3 + nb], Ms1 = ma1 + Al[(mc + 1) * n3 + nb], Ms2 = ma2 + Al[(mc + 2) * n3 + nb];
           R F[5];
-          split_pair_flux<SPLIT, R>(A_, B_, Ms0, Ms1, Ms2, R(2) * gas.pref, F);
+          if constexpr (SPLIT == DG_SPLIT_PI) {
+            // 8 x the PI flux of split_pair_flux, with the density row at 4 x (its accumulators are
+            // doubled at the end); every factor is a power of two, so the rounding is unchanged
+            const R rs = A_.rho + B_.rho, us = A_.u + B_.u, vs = A_.v + B_.v, ws = A_.w + B_.w;
+            const R ps4 = A_.pm + B_.pm;
+            const R Vs = Ms0 * us + Ms1 * vs + Ms2 * ws;
+            const R q8 = rs * Vs;
+            F[0] = q8;
+            F[1] = q8 * us + ps4 * Ms0;
+            F[2] = q8 * vs + ps4 * Ms1;
+            F[3] = q8 * ws + ps4 * Ms2;
+            F[4] = q8 * (A_.aux + B_.aux);
+          } else {
+            split_pair_flux<SPLIT, R>(A_, B_, Ms0, Ms1, Ms2, R(2) * gas.pref, F);
+          }
           const R dba = sb.DVS[b + n * a], dab = sb.DVS[a + n * b];  // DVolSurf(l=b,i=a), DVolSurf(l=a,i=b)
 #pragma unroll
           for (int v = 0; v < 5; ++v) {
@@ -635,17 +654,63 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
     if (active) {
       const R* Ad = AccD + (size_t)el * 15 * n3;
 #pragma unroll
-      for (int v = 0; v < 5; ++v) vacc[v] = vacc[v] + (Ad[v * n3 + node] + Ad[(5 + v) * n3 + node] + Ad[(10 + v) * n3 + node]);
+      for (int v = 0; v < 5; ++v) {
+        R sv = Ad[v * n3 + node] + Ad[(5 + v) * n3 + node] + Ad[(10 + v) * n3 + node];
+        if (SPLIT == DG_SPLIT_PI && v == 0) sv = sv * R(2);
+        vacc[v] = vacc[v] + sv;
+      }
     }
   }
 
   // ---- phase C: surface integral, -1, Jacobian, output / RK stage
-  if (!active) return;
   R ut[5];
 #pragma unroll
   for (int v = 0; v < 5; ++v) ut[v] = R(0);
+  if (!L.gauss) {
+    // Gauss-Lobatto: only face nodes receive surface terms; add them by face-node threads, one
+    // normal direction per pass (the two faces of a direction share no node), into the staging area
+    __syncthreads();  // every read of the staging area is complete
+    for (int t = threadIdx.x; t < nloc * 5 * n3; t += blockDim.x) {
+      const int el2 = t / (5 * n3), r = t - el2 * 5 * n3;
+      A[(size_t)el2 * NA * n3 + r] = R(0);
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int dir = 0; dir < 3; ++dir) {
+      for (int t = threadIdx.x; t < nloc * 2 * n2; t += blockDim.x) {
+        const int el2 = t / (2 * n2), r = t - el2 * 2 * n2;
+        const bool minus = r < n2;
+        const int ab = minus ? r : r - n2;
+        const int a = ab % n, b = ab / n;
+        const int ls = dir == 0 ? (minus ? L_XI_MINUS : L_XI_PLUS)
+                                : (dir == 1 ? (minus ? L_ETA_MINUS : L_ETA_PLUS) : (minus ? L_ZETA_MINUS : L_ZETA_PLUS));
+        const int fnode = face_node(n, ls, a, b, minus ? 0 : N);
+        const int e2 = e0 + el2;
+        const R Lhat = minus ? sb.Lhm[0] : sb.Lhp[N];
+        const int side = E2S[(e2 * 6 + ls - 1) * 2 + 0];
+        const int flip = E2S[(e2 * 6 + ls - 1) * 2 + 1];
+        int p, q;
+        s2v2_inv(N, a, b, flip, ls, p, q);
+        const R* fx = Flux + (size_t)side * 5 * n2 + p + n * q;
+        R* Su = A + (size_t)el2 * NA * n3 + fnode;
+        if (flip == 0) {
+#pragma unroll
+          for (int v = 0; v < 5; ++v) Su[v * n3] = Su[v * n3] + fx[v * n2] * Lhat;
+        } else {
+#pragma unroll
+          for (int v = 0; v < 5; ++v) Su[v * n3] = Su[v * n3] - fx[v * n2] * Lhat;
+        }
+      }
+      __syncthreads();
+    }
+    if (!active) return;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) ut[v] = Ae[v * n3 + node];
+  }
+  if (!active) return;
 #pragma unroll
   for (int ls = 1; ls <= 6; ++ls) {
+    if (!L.gauss) break;
     int a, b, l;
     switch (ls) {
       case L_XI_MINUS: case L_XI_PLUS: a = j; b = k; l = i; break;
