@@ -37,8 +37,8 @@ ALG_BYTES_N7 = 510.0  # compulsory HBM bytes per DOF-stage of a fully fused impl
 # ncu on the 16^3 case of the same kernels (profiles/dgsem_fp64_kernels_tgv_n7_16cube.md): DRAM bytes
 # and executed FP64 thread-instructions (DFMA+DADD+DMUL) per DOF for one k_volume launch; traffic
 # grows with the number of elements, so it is scaled to a launch by nDOF
-KVOL_DRAM_BYTES_PER_DOF = (669.970688e6 + 144.893696e6) / 2097152
-KVOL_FP64_INSTR_PER_DOF = 548.3
+KVOL_DRAM_BYTES_PER_DOF = (669.912832e6 + 144.459520e6) / 2097152
+KVOL_FP64_INSTR_PER_DOF = 519.0
 FP64_ISSUE_PER_CYCLE = 304  # sm__sass_thread_inst_executed_op_dfma_pred_on.sum.peak_sustained (152 SMs x 2)
 TGV_R = 71.42857
 CFL = 0.8  # CFLscale / DFLscale of the reference's TGV regression (regressioncheck/checks/tgv/split/parameter.ini)
@@ -60,6 +60,9 @@ def parse():
                     help="skip the mixed-precision comparisons and the adjoint measurement")
     ap.add_argument("--adjoint-fd", type=int, default=0,
                     help="central-difference check of the adjoint gradient along this many random directions")
+    ap.add_argument("--adjoint-steps", type=int, default=200)
+    ap.add_argument("--only", default=None, choices=["adjoint", "mixed_tgv", "mixed_curved"],
+                    help="run one of the extra measurements alone and print its JSON (profiling runs)")
     return ap.parse_args()
 
 
@@ -253,7 +256,7 @@ def run_ours(args, world, rank, local):
     if not args.no_extras and args.precision == "fp64":
         extras["mixed_vs_fp64"] = mixed_vs_fp64_tgv(args.workload, args.steps, stream)
         extras["mixed_vs_fp64_curved_br2"] = mixed_vs_fp64_curved_br2(stream)
-        extras["adjoint"] = adjoint_tgv(stream, fd_dirs=args.adjoint_fd)
+        extras["adjoint"] = adjoint_tgv(stream, steps=args.adjoint_steps, fd_dirs=args.adjoint_fd)
     if rank == 0:
         line = {"metric": "DOF-stage updates/s", "value": value, "unit": "DOF-stage/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -484,6 +487,19 @@ def profile_roofline(args, op, U, dt, stream, nDOF):
 def main():
     args = parse()
     world, rank, local = dist_init(args)
+    if args.only:
+        import torch
+        torch.cuda.set_device(local)
+        stream = torch.cuda.current_stream()
+        if args.only == "adjoint":
+            res = adjoint_tgv(stream, steps=args.adjoint_steps, fd_dirs=args.adjoint_fd)
+        elif args.only == "mixed_tgv":
+            res = mixed_vs_fp64_tgv(args.workload, args.steps, stream)
+        else:
+            res = mixed_vs_fp64_curved_br2(stream, steps=args.steps)
+        if rank == 0:
+            print(json.dumps({"only": args.only, **res}), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args, world, rank)
     else:
