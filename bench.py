@@ -61,7 +61,7 @@ def parse():
     ap.add_argument("--adjoint-fd", type=int, default=0,
                     help="central-difference check of the adjoint gradient along this many random directions")
     ap.add_argument("--adjoint-steps", type=int, default=200)
-    ap.add_argument("--only", default=None, choices=["adjoint", "mixed_tgv", "mixed_curved"],
+    ap.add_argument("--only", default=None, choices=["adjoint", "mixed_tgv", "mixed_curved", "scale64"],
                     help="run one of the extra measurements alone and print its JSON (profiling runs)")
     return ap.parse_args()
 
@@ -365,6 +365,75 @@ def mixed_vs_fp64_curved_br2(stream, steps=500):
     return res
 
 
+def scale_c5(stream, steps=100, adj_steps=50, budget_gb=180):
+    """The 64^3 scale case (134 M DOF, N=7 GL, split PI, Roe, BR1): FP64 and mixed for `steps` LSERK
+    steps from the TGV state, then the adjoint of an `adj_steps` window (kinetic-energy objective)
+    with checkpoints in at most `budget_gb` of device memory (less if the operator, ~61 GB at this
+    size, and the adjoint's work states and scratch leave less free)."""
+    import torch
+    import galaexi_gb300 as gx
+    w = WORKLOADS["tgv_n7_64cube_split_pi_roe_br1"]
+    N, ne = w["N"], w["ne"]
+    mesh = gx.Mesh(N, 2, ne, ne, ne, (-math.pi,) * 3, (math.pi,) * 3)
+    U0 = torch.from_numpy(gx.tgv_state(mesh, mach=0.1, R=TGV_R)).cuda()
+    res = {"workload": "tgv_n7_64cube_split_pi_roe_br1", "nDOF": mesh.nDOF, "steps": steps}
+    ends = {}
+    dt = None
+    for prec in ("fp64", "mixed"):
+        cfg = gx.config(N=N, NodeType="gauss-lobatto", Riemann=w["Riemann"], SplitDG=w["SplitDG"],
+                        parabolic=True, mu0=w["mu0"], R=TGV_R, precision=prec)
+        op = gx.DG(cfg, mesh)
+        if dt is None:
+            dt, _ = op.CalcTimeStep(U0, CFL, DFL)
+        U, K = U0.clone(), torch.zeros_like(U0)
+        op.TimeStepByLSERKW2(0.0, dt, U, K)
+        U, K = U0.clone(), torch.zeros_like(U0)
+        ms, _ = timed(lambda: op.TimeStepByLSERKW2(0.0, dt, U, K, nSteps=steps), stream)
+        res["dof_stage_per_s_" + prec] = mesh.nDOF * 5 * steps / (ms * 1e-3)
+        res["ms_per_step_" + prec] = ms / steps
+        ends[prec] = (U, op.integrals(U) if prec == "fp64" else None)
+        if prec == "mixed":
+            I64 = ends["fp64"][1]
+            Im = gx.DG(gx.config(N=N, NodeType="gauss-lobatto", Riemann=w["Riemann"], SplitDG=w["SplitDG"],
+                                 parabolic=True, mu0=w["mu0"], R=TGV_R), mesh)
+            Imix = Im.integrals(U)
+            Im.close()
+            res["mixed_ke_rel_err"] = abs(Imix[5] - I64[5]) / abs(I64[5])
+            res["mixed_l2_rel"] = float((U - ends["fp64"][0]).norm() / ends["fp64"][0].norm())
+        op.close()
+        del K
+    res["mixed_speedup"] = res["dof_stage_per_s_mixed"] / res["dof_stage_per_s_fp64"]
+    del ends
+    torch.cuda.empty_cache()
+    cfg = gx.config(N=N, NodeType="gauss-lobatto", Riemann=w["Riemann"], SplitDG=w["SplitDG"], parabolic=True,
+                    mu0=w["mu0"], R=TGV_R)
+    op = gx.DG(cfg, mesh)
+
+    def fwd():
+        U, K = U0.clone(), torch.zeros_like(U0)
+        op.TimeStepByLSERKW2(0.0, dt, U, K, nSteps=adj_steps)
+        return U
+
+    ms_f, _ = timed(fwd, stream)
+    torch.cuda.empty_cache()
+    # checkpoint budget: at most budget_gb, and what is left of the device after the operator, the
+    # adjoint's work states and scratch (about 12 states at N=7) and a margin
+    free, _ = torch.cuda.mem_get_info()
+    state = U0.numel() * 8
+    budget = int(min(budget_gb * 2 ** 30, free - 12 * state - 8 * 2 ** 30))
+    Uf, plan = None, None
+    t_rec, (Uf, plan) = timed(lambda: op.adjoint_forward(dt, adj_steps, U0, budget), stream)
+    J, G = op.kinetic_energy(Uf, grad=True)
+    del Uf
+    t_rev, mub = timed(lambda: op.adjoint_reverse(G), stream)
+    res.update({"adjoint_steps": adj_steps, "adjoint_budget_gb": budget / 2 ** 30, "adjoint_plan": plan,
+                "state_gb": U0.numel() * 8 / 2 ** 30, "forward_window_ms": ms_f, "adjoint_record_ms": t_rec,
+                "adjoint_reverse_ms": t_rev, "adjoint_over_forward": (t_rec + t_rev) / ms_f, "J": J, "dJ_dmu": mub,
+                "grad_norm": float(G.norm())})
+    op.close()
+    return res
+
+
 def adjoint_tgv(stream, steps=200, fd_dirs=0):
     """Discrete adjoint on the N=5, 16^3 TGV (split PI, Roe, BR1, FP64): J = kinetic-energy integral
     after `steps` LSERK steps at fixed dt; gradient w.r.t. the initial state and mu.  Reports the
@@ -493,6 +562,8 @@ def main():
         stream = torch.cuda.current_stream()
         if args.only == "adjoint":
             res = adjoint_tgv(stream, steps=args.adjoint_steps, fd_dirs=args.adjoint_fd)
+        elif args.only == "scale64":
+            res = scale_c5(stream, steps=args.steps, adj_steps=args.adjoint_steps)
         elif args.only == "mixed_tgv":
             res = mixed_vs_fp64_tgv(args.workload, args.steps, stream)
         else:

@@ -51,6 +51,7 @@ struct AdjLaunch {
   int nElems, nSides;
   int gauss, riemann, split, parabolic, lift_mode;
   double mu, lambda, lamc;  // mu, lambda, lambda/mu (the thermal conductivity per unit viscosity)
+  double inv_mu;            // 1/mu, or 0 for mu = 0
   double kappa, sR;
 };
 
@@ -225,18 +226,25 @@ ka_face(CotSrc cs, const double* __restrict__ Met, const double* __restrict__ Uf
 #pragma unroll
         for (int c = 0; c < 15; ++c) gb[c] = 0.;
         visc_dir_vjp(nv, fb, taub, tqb);
+        // d F / d mu = F_visc / mu (the viscous flux is linear in mu at fixed Prandtl number), so
+        // <fb, dF/dmu> = (taub . tau + tqb . tq) / mu before taub is closed
+        const double fvis = taub[0] * tau[0] + taub[1] * tau[1] + taub[2] * tau[2] + taub[3] * tau[3] +
+                            taub[4] * tau[4] + taub[5] * tau[5] + tqb[0] * tq[0] + tqb[1] * tq[1] + tqb[2] * tq[2];
+        if (L.inv_mu > 0.) {
+          mub += fvis * L.inv_mu;
+        } else {
+          double fd1[5];
+          const double P6[6] = {psrc[0], vel[0], vel[1], vel[2], psrc[4 * n2], psrc[5 * n2]};
+          normal_diff_flux(P6, gg, gg + 5, gg + 10, nv, 1., L.lamc, fd1);
+#pragma unroll
+          for (int v = 1; v < 5; ++v) mub += fb[v] * fd1[v];
+        }
         visc_close_vjp(tau, vel, L.mu, L.lambda, taub, tqb, gb, velb);
         double* gout = GfB + ((size_t)slot * S + side) * 15 * n2 + pq;
 #pragma unroll
         for (int c = 0; c < 15; ++c) gout[c * n2] = gb[c];
         prim_vjp(slot == 0 ? ULv : URv, gas.kappaM1, L.sR, 0., velb[0], velb[1], velb[2], 0., 0., 0., 0., 0., 0., 0.,
                  slot == 0 ? ULb : URb);
-        // d F / d mu: the viscous flux at unit viscosity (lambda/mu fixed)
-        double fd1[5];
-        const double P6[6] = {psrc[0], vel[0], vel[1], vel[2], psrc[4 * n2], psrc[5 * n2]};
-        normal_diff_flux(P6, gg, gg + 5, gg + 10, nv, 1., L.lamc, fd1);
-#pragma unroll
-        for (int v = 1; v < 5; ++v) mub += fb[v] * fd1[v];
       }
     }
 #pragma unroll
@@ -380,12 +388,13 @@ ka_volume(CotSrc cs, const double* __restrict__ U, const double* __restrict__ Pv
       for (int d = 0; d < 3; ++d)
 #pragma unroll
         for (int v = 0; v < 5; ++v) flb[d][v] = 0.;
+      constexpr int v0 = (SPLIT < 0) ? 0 : 1;  // the viscous fluxes have no density row
 #pragma unroll
       for (int l = 0; l < n; ++l) {
         const double ci = sb.DhatT[i + n * l], cj = sb.DhatT[j + n * l], ck = sb.DhatT[k + n * l];
         const int ni = l + n * (j + n * k), nj = i + n * (l + n * k), nk = i + n * (j + n * l);
 #pragma unroll
-        for (int v = 0; v < 5; ++v) {
+        for (int v = v0; v < 5; ++v) {
           flb[0][v] += ci * Aa[v * n3 + ni];
           flb[1][v] += cj * Aa[v * n3 + nj];
           flb[2][v] += ck * Aa[v * n3 + nk];
@@ -421,16 +430,17 @@ ka_volume(CotSrc cs, const double* __restrict__ U, const double* __restrict__ Pv
         double tau[6], tq[3];
         visc_stress(gg, gg + 5, gg + 10, vel, L.mu, L.lambda, tau, tq);
         double taub[6] = {0, 0, 0, 0, 0, 0}, tqb[3] = {0, 0, 0}, velb[3] = {0, 0, 0};
-        double tau1[6], tq1[3];
-        visc_stress(gg, gg + 5, gg + 10, vel, 1., L.lamc, tau1, tq1);
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          visc_dir_vjp(Ms[d], flb[d], taub, tqb);
-          // d/dmu of the viscous contravariant flux: -Ms[d] . (tau1 rows, tq1)
-          mub -= flb[d][1] * (Ms[d][0] * tau1[0] + Ms[d][1] * tau1[3] + Ms[d][2] * tau1[4]) +
-                 flb[d][2] * (Ms[d][0] * tau1[3] + Ms[d][1] * tau1[1] + Ms[d][2] * tau1[5]) +
-                 flb[d][3] * (Ms[d][0] * tau1[4] + Ms[d][1] * tau1[5] + Ms[d][2] * tau1[2]) +
-                 flb[d][4] * (Ms[d][0] * tq1[0] + Ms[d][1] * tq1[1] + Ms[d][2] * tq1[2]);
+        for (int d = 0; d < 3; ++d) visc_dir_vjp(Ms[d], flb[d], taub, tqb);
+        // d/dmu of the viscous contravariant fluxes = the fluxes / mu: (taub . tau + tqb . tq) / mu
+        if (L.inv_mu > 0.) {
+          mub += (taub[0] * tau[0] + taub[1] * tau[1] + taub[2] * tau[2] + taub[3] * tau[3] + taub[4] * tau[4] +
+                  taub[5] * tau[5] + tqb[0] * tq[0] + tqb[1] * tq[1] + tqb[2] * tq[2]) * L.inv_mu;
+        } else {
+          double tau1[6], tq1[3];
+          visc_stress(gg, gg + 5, gg + 10, vel, 1., L.lamc, tau1, tq1);
+          mub += taub[0] * tau1[0] + taub[1] * tau1[1] + taub[2] * tau1[2] + taub[3] * tau1[3] + taub[4] * tau1[4] +
+                 taub[5] * tau1[5] + tqb[0] * tq1[0] + tqb[1] * tq1[1] + tqb[2] * tq1[2];
         }
         visc_close_vjp(tau, vel, L.mu, L.lambda, taub, tqb, gb, velb);
         ub_ += velb[0]; vb += velb[1]; wb += velb[2];

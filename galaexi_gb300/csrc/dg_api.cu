@@ -325,7 +325,7 @@ int integrals(dg_ctx* ctx, const double* d_U, double out[6], cudaStream_t st) {
   }
   if (!ctx->acc.p && !ctx->acc.alloc(8)) { set_error("cudaMalloc"); return DG_ERR_ALLOC; }
   CUDA_TRY(cudaMemsetAsync(ctx->acc.p, 0, 8 * sizeof(double), st), "clear");
-  k_integrals<<<grid, 256, 0, st>>>(d_U, ctx->MetD.p, ctx->wq.p, ctx->n, ctx->nElems, ctx->part.p);
+  k_integrals<<<grid, 256, 0, st>>>(d_U, ctx->metd, ctx->wq.p, ctx->n, ctx->nElems, ctx->part.p);
   for (int c = 0; c < 6; ++c) gx::k_adj_sum<<<1, 256, 0, st>>>(ctx->part.p + (size_t)c * grid, grid, ctx->acc.p + c);
   ctx->launches += 7;
   CUDA_TRY(cudaGetLastError(), "integrals launch");
@@ -504,8 +504,15 @@ int dg_set_mesh(dg_ctx* ctx, int nElems, int nSides, int nBCSides, const double*
     }
   }
   if (rc != DG_OK) return rc;
-  if (!ctx->MetD.alloc(met.size()) || !ctx->E2S.alloc(he2s.size())) { set_error("cudaMalloc mesh"); return DG_ERR_ALLOC; }
-  CUDA_TRY(cudaMemcpy(ctx->MetD.p, met.data(), met.size() * sizeof(double), cudaMemcpyHostToDevice), "upload metrics");
+  if (!ctx->E2S.alloc(he2s.size())) { set_error("cudaMalloc mesh"); return DG_ERR_ALLOC; }
+  if (ctx->cfg.precision == DG_PRECISION_FP64) {
+    ctx->MetD.release();
+    ctx->metd = ctx->d.Met.p;  // same layout and precision: no second copy
+  } else {
+    if (!ctx->MetD.alloc(met.size())) { set_error("cudaMalloc mesh"); return DG_ERR_ALLOC; }
+    CUDA_TRY(cudaMemcpy(ctx->MetD.p, met.data(), met.size() * sizeof(double), cudaMemcpyHostToDevice), "upload metrics");
+    ctx->metd = ctx->MetD.p;
+  }
   CUDA_TRY(cudaMemcpy(ctx->E2S.p, he2s.data(), he2s.size() * sizeof(int), cudaMemcpyHostToDevice), "upload E2S");
   // SideToElem on the device, from the validated ElemToSide: master elem/side, slave elem/side, flip
   std::vector<int> hs2e((size_t)nSides * 5, 0);
@@ -640,7 +647,7 @@ int dg_kinetic_energy(dg_ctx* ctx, const double* d_U, double* J, double* d_dJdU,
   if (int rc = integrals(ctx, d_U, out, st)) return rc;
   *J = out[5];
   if (d_dJdU) {
-    k_ke_grad<<<grid_for((size_t)ctx->nElems * ctx->n3), 256, 0, st>>>(d_U, ctx->MetD.p, ctx->wq.p, ctx->n,
+    k_ke_grad<<<grid_for((size_t)ctx->nElems * ctx->n3), 256, 0, st>>>(d_U, ctx->metd, ctx->wq.p, ctx->n,
                                                                      ctx->nElems, d_dJdU);
     ctx->launches++;
     CUDA_TRY(cudaGetLastError(), "k_ke_grad launch");

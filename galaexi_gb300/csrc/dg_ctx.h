@@ -88,7 +88,8 @@ struct dg_ctx {
   gxh::Basis1D B;
   gxc::PrecData<double> d;
   gxc::PrecData<float> f;
-  gxc::DBuf<double> MetD;  // FP64 packed metrics [e][10][n3] for the CFL reduction
+  gxc::DBuf<double> MetD;  // FP64 packed metrics [e][10][n3] for the CFL reduction (mixed form only)
+  const double* metd = nullptr;  // FP64 packed metrics: d.Met in the FP64 form, MetD in the mixed form
   gxc::DBuf<int> E2S;      // [e][6][2]: 0-based side, flip
   gxc::DBuf<double> red;   // dt reduction result (2)
   gxc::DBuf<unsigned long long> bad;

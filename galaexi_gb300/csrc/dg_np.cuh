@@ -229,6 +229,7 @@ int adj(dg_ctx* ctx, const double* U, gx::CotSrc cs, int mode, double* Uout, dou
   AL.mu = c.mu0;
   AL.lamc = c.R * c.kappa / ((c.kappa - 1.) * c.Pr);
   AL.lambda = c.mu0 * AL.lamc;
+  AL.inv_mu = c.mu0 > 0. ? 1. / c.mu0 : 0.;
   AL.kappa = c.kappa; AL.sR = 1. / c.R;
   const gx::DevBasis<double> b = gxc::dev_basis(ctx->d, NP);
   const long long nf = (long long)ctx->nSides * NP * NP;
@@ -268,7 +269,7 @@ int stage_events(dg_ctx* ctx, double* U, gx::RKArgs rk, cudaStream_t st, cudaEve
 
 int cfl(dg_ctx* ctx, const double* U, double cflS, double dflS, double kpr, cudaStream_t st) {
   const int threads = ((NP * NP * NP + 31) / 32) * 32;
-  gx::k_cfl<NP><<<ctx->nElems, threads, 0, st>>>(U, ctx->MetD.p, ctx->nElems, ctx->cfg.kappa, ctx->cfg.mu0,
+  gx::k_cfl<NP><<<ctx->nElems, threads, 0, st>>>(U, ctx->metd, ctx->nElems, ctx->cfg.kappa, ctx->cfg.mu0,
                                                  ctx->cfg.parabolic, kpr, cflS, dflS, ctx->red.p, ctx->bad.p);
   ctx->launches++;
   GX_CUDA_TRY(cudaGetLastError(), "k_cfl launch");
