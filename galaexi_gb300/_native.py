@@ -76,6 +76,8 @@ _SIGS = {
     "dg_check_state": (_I, [_P, _P, ctypes.POINTER(ctypes.c_longlong), _P]),
     "dg_kernel_launch_count": (ctypes.c_longlong, [_P]),
     "dg_get_gradients": (_I, [_P, _P, _P, _P, _P]),
+    "dg_mesh_hopr_sizes": (_I, [ctypes.c_char_p, _IP, _IP, _IP, _IP]),
+    "dg_mesh_hopr": (_I, [ctypes.c_char_p, _I, _I] + [_P] * 12),
     "dg_integrals": (_I, [_P, _P, _P, _P]),
     "dg_kinetic_energy": (_I, [_P, _P, _P, _P, _P]),
     "dg_rhs_jvp": (_I, [_P, _D, _P, _P, _D, _P, _P, _P]),

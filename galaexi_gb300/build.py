@@ -19,7 +19,8 @@ CUFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xco
 
 
 def sources():
-    srcs = ["dg_api.cu", "dg_host.cpp", "dg_noalloc.cu"] + ["dg_np%d.cu" % np_ for np_ in range(2, 11)]
+    srcs = ["dg_api.cu", "dg_host.cpp", "dg_hdf5.cpp", "dg_hopr.cpp", "dg_noalloc.cu"] + [
+        "dg_np%d.cu" % np_ for np_ in range(2, 11)]
     return [os.path.join(CSRC, s) for s in srcs]
 
 

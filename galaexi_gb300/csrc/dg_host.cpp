@@ -174,7 +174,7 @@ void basis_1d(int N, int node_type, Basis1D& B) {
 }
 
 // interpolation matrix V(i,j) = l_j(y_i) from nodes x (degree N) to points y (m+1 points)
-static void vandermonde(int N, const double* x, const double* wb, int M, const double* y, std::vector<double>& V) {
+void vandermonde(int N, const double* x, const double* wb, int M, const double* y, std::vector<double>& V) {
   V.assign((size_t)(M + 1) * (N + 1), 0.);
   std::vector<double> L(N + 1);
   for (int i = 0; i <= M; ++i) {
@@ -323,7 +323,7 @@ extern "C" int dg_mesh_cartesian_sizes(int nx, int ny, int nz, int* nElems, int*
 // The slave flips (1 for xi/zeta sides, 2 for eta sides) are the ones for which
 // SideToVol2(p,q,flip,slave side) lands on the same physical point as the master's (p,q).
 // ---------------------------------------------------------------------------------------------
-namespace {
+namespace gxh {
 enum { ZETA_MINUS = 1, ETA_MINUS = 2, XI_PLUS = 3, ETA_PLUS = 4, XI_MINUS = 5, ZETA_PLUS = 6 };
 const int NormalDirs[7] = {0, 3, 2, 1, 2, 1, 3};            // mesh_vars.f90:112 (1-based locSide)
 const int TangDirs[7] = {0, 1, 3, 2, 3, 2, 1};              // mesh_vars.f90:114
@@ -342,8 +342,121 @@ struct Mapping {
   }
 };
 
-inline size_t vidx(int n, int i, int j, int k, int e) { return (size_t)i + n * (j + n * (k + (size_t)n * e)); }
-}  // namespace
+
+// Metric terms of one element from its coordinates X (3 per node, i fastest) at the
+// Chebyshev-Gauss-Lobatto points of degree N: conservative curl form (metrics.f90:451-485), then
+// interpolation to the solution nodes (metrics.f90:497-507); sJ = 1/det(dX/dxi) at the solution
+// nodes; JaFace[loc-1][a][b][nn][dd] the metric terms on the six face planes at the solution face
+// nodes (volume face coordinates a, b).
+void curl_metrics(int N, const Basis1D& C, const std::vector<double>& Vcl, const double* X, int e, double* Mf,
+                  double* Mg, double* Mh, double* sJ, double* JaFace) {
+  const int n = N + 1, n2 = n * n;
+  std::vector<double> dX((size_t)9 * n * n2), Rcl((size_t)9 * n * n2), Ja((size_t)9 * n * n2);
+  std::vector<double> JaN((size_t)9 * n * n2), dXN((size_t)9 * n * n2);
+  auto I3 = [&](int i, int j, int k) { return (size_t)i + n * (j + (size_t)n * k); };
+  auto to_nodes = [&](const std::vector<double>& src, std::vector<double>& dst) {
+    std::vector<double> a(src.size()), b(src.size());
+    for (int c = 0; c < 9; ++c)
+      for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
+        double s = 0.; for (int l = 0; l < n; ++l) s += Vcl[i + n * l] * src[c + 9 * I3(l, j, k)]; a[c + 9 * I3(i, j, k)] = s;
+      }
+    for (int c = 0; c < 9; ++c)
+      for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
+        double s = 0.; for (int l = 0; l < n; ++l) s += Vcl[j + n * l] * a[c + 9 * I3(i, l, k)]; b[c + 9 * I3(i, j, k)] = s;
+      }
+    for (int c = 0; c < 9; ++c)
+      for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
+        double s = 0.; for (int l = 0; l < n; ++l) s += Vcl[k + n * l] * b[c + 9 * I3(i, j, l)]; dst[c + 9 * I3(i, j, k)] = s;
+      }
+  };
+  // dX(dd, nn) = d X_nn / d xi_dd
+  for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
+    double* d = &dX[9 * I3(i, j, k)];
+    for (int t = 0; t < 9; ++t) d[t] = 0.;
+    for (int l = 0; l < n; ++l)
+      for (int nn = 0; nn < 3; ++nn) {
+        d[0 * 3 + nn] += C.D[i + n * l] * X[nn + 3 * I3(l, j, k)];
+        d[1 * 3 + nn] += C.D[j + n * l] * X[nn + 3 * I3(i, l, k)];
+        d[2 * 3 + nn] += C.D[k + n * l] * X[nn + 3 * I3(i, j, l)];
+      }
+  }
+  // R(dd, nn) = 1/2 (X_{nn+2} dX_{nn+1}/dxi_dd - X_{nn+1} dX_{nn+2}/dxi_dd)
+  for (size_t t = 0; t < (size_t)n * n2; ++t)
+    for (int dd = 0; dd < 3; ++dd)
+      for (int nn = 0; nn < 3; ++nn) {
+        const int n1 = (nn + 1) % 3, n2_ = (nn + 2) % 3;
+        Rcl[t * 9 + dd * 3 + nn] = 0.5 * (X[n2_ + 3 * t] * dX[t * 9 + dd * 3 + n1] - X[n1 + 3 * t] * dX[t * 9 + dd * 3 + n2_]);
+      }
+  // Ja(dd, nn) = -(d/dxi_{dd+1} R(dd+2, nn) - d/dxi_{dd+2} R(dd+1, nn))
+  for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
+    double* J = &Ja[9 * I3(i, j, k)];
+    for (int t = 0; t < 9; ++t) J[t] = 0.;
+    for (int q = 0; q < n; ++q)
+      for (int nn = 0; nn < 3; ++nn) {
+        J[0 * 3 + nn] += -C.D[j + n * q] * Rcl[9 * I3(i, q, k) + 2 * 3 + nn] + C.D[k + n * q] * Rcl[9 * I3(i, j, q) + 1 * 3 + nn];
+        J[1 * 3 + nn] += -C.D[k + n * q] * Rcl[9 * I3(i, j, q) + 0 * 3 + nn] + C.D[i + n * q] * Rcl[9 * I3(q, j, k) + 2 * 3 + nn];
+        J[2 * 3 + nn] += -C.D[i + n * q] * Rcl[9 * I3(q, j, k) + 1 * 3 + nn] + C.D[j + n * q] * Rcl[9 * I3(i, q, k) + 0 * 3 + nn];
+      }
+  }
+  to_nodes(Ja, JaN);
+  to_nodes(dX, dXN);
+  for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
+    const size_t t = I3(i, j, k), g = vidx(n, i, j, k, e);
+    const double* J = &JaN[9 * t];
+    for (int d = 0; d < 3; ++d) { Mf[d + 3 * g] = J[0 * 3 + d]; Mg[d + 3 * g] = J[1 * 3 + d]; Mh[d + 3 * g] = J[2 * 3 + d]; }
+    const double* a = &dXN[9 * t];
+    const double det = a[0] * (a[4] * a[8] - a[5] * a[7]) - a[1] * (a[3] * a[8] - a[5] * a[6]) +
+                       a[2] * (a[3] * a[7] - a[4] * a[6]);
+    sJ[g] = 1. / det;
+  }
+  // face metrics: JaCL on the face planes (xi = -+1 are CL end points), interpolated in 2D
+  for (int loc = 1; loc <= 6; ++loc)
+    for (int b = 0; b < n; ++b)
+      for (int a = 0; a < n; ++a) {
+        double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (int qb = 0; qb < n; ++qb)
+          for (int qa = 0; qa < n; ++qa) {
+            size_t src;
+            const int pl = (loc == XI_MINUS || loc == ETA_MINUS || loc == ZETA_MINUS) ? 0 : N;
+            if (loc == XI_MINUS || loc == XI_PLUS) src = I3(pl, qa, qb);
+            else if (loc == ETA_MINUS || loc == ETA_PLUS) src = I3(qa, pl, qb);
+            else src = I3(qa, qb, pl);
+            const double wgt = Vcl[a + n * qa] * Vcl[b + n * qb];
+            for (int c = 0; c < 9; ++c) acc[c] += wgt * Ja[9 * src + c];
+          }
+        for (int c = 0; c < 9; ++c) JaFace[((size_t)(loc - 1) * n2 + a + n * b) * 9 + c] = acc[c];
+      }
+}
+
+// SurfMetricsFromJa (metrics.f90:752-789) for a master side (flip 0) of local side loc: the side
+// node (p,q) sits at the volume face coordinates CGNS_SideToVol2(p,q,loc) (mappings.f90:388-425).
+void surface_metrics(int N, int loc, const double* JaFace, size_t side, double* nvec, double* t1vec, double* t2vec,
+                     double* surfelem) {
+  const int n = N + 1, n2 = n * n;
+  const int nd = NormalDirs[loc] - 1, td = TangDirs[loc] - 1;
+  const double sgn = NormalSigns[loc];
+  for (int q = 0; q <= N; ++q)
+    for (int p = 0; p <= N; ++p) {
+      int a = p, b = q;
+      if (loc == XI_MINUS || loc == ZETA_MINUS) { a = q; b = p; }
+      else if (loc == ETA_PLUS) a = N - p;
+      const double* J = &JaFace[((size_t)(loc - 1) * n2 + a + n * b) * 9];
+      const size_t f = (size_t)p + n * (q + (size_t)n * side);
+      double se = std::sqrt(J[nd * 3 + 0] * J[nd * 3 + 0] + J[nd * 3 + 1] * J[nd * 3 + 1] + J[nd * 3 + 2] * J[nd * 3 + 2]);
+      double nv[3], t1[3], t2[3];
+      for (int c = 0; c < 3; ++c) nv[c] = sgn * J[nd * 3 + c] / se;
+      const double dot = J[td * 3 + 0] * nv[0] + J[td * 3 + 1] * nv[1] + J[td * 3 + 2] * nv[2];
+      for (int c = 0; c < 3; ++c) t1[c] = J[td * 3 + c] - dot * nv[c];
+      const double tn = std::sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
+      for (int c = 0; c < 3; ++c) t1[c] = t1[c] / tn;
+      t2[0] = nv[1] * t1[2] - nv[2] * t1[1];
+      t2[1] = nv[2] * t1[0] - nv[0] * t1[2];
+      t2[2] = nv[0] * t1[1] - nv[1] * t1[0];
+      surfelem[f] = se;
+      for (int c = 0; c < 3; ++c) { nvec[c + 3 * f] = nv[c]; t1vec[c + 3 * f] = t1[c]; t2vec[c + 3 * f] = t2[c]; }
+    }
+}
+}  // namespace gxh
 
 extern "C" int dg_mesh_cartesian(int N, int node_type, int nx, int ny, int nz, const double* x0, const double* x1,
                                  double deform_amp, double* elem_xgp, double* Mf, double* Mg, double* Mh, double* sJ,
@@ -426,119 +539,23 @@ extern "C" int dg_mesh_cartesian(int N, int node_type, int nx, int ny, int nz, c
     basis_1d(N, 99, C);  // Chebyshev-Gauss-Lobatto
     std::vector<double> Vcl;  // CL -> solution nodes
     vandermonde(N, C.x.data(), C.wb.data(), N, B.x.data(), Vcl);
-    std::vector<double> X((size_t)3 * n * n2), dX((size_t)9 * n * n2), Rcl((size_t)9 * n * n2), Ja((size_t)9 * n * n2);
-    std::vector<double> JaN((size_t)9 * n * n2), dXN((size_t)9 * n * n2), tmp((size_t)9 * n * n2);
+    std::vector<double> X((size_t)3 * n * n2);
     auto I3 = [&](int i, int j, int k) { return (size_t)i + n * (j + (size_t)n * k); };
-    // interpolate a 9-component CL field to the solution nodes (tensor product)
-    auto to_nodes = [&](const std::vector<double>& src, std::vector<double>& dst) {
-      std::vector<double> a(src.size()), b(src.size());
-      for (int c = 0; c < 9; ++c)
-        for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
-          double s = 0.; for (int l = 0; l < n; ++l) s += Vcl[i + n * l] * src[c + 9 * I3(l, j, k)]; a[c + 9 * I3(i, j, k)] = s;
-        }
-      for (int c = 0; c < 9; ++c)
-        for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
-          double s = 0.; for (int l = 0; l < n; ++l) s += Vcl[j + n * l] * a[c + 9 * I3(i, l, k)]; b[c + 9 * I3(i, j, k)] = s;
-        }
-      for (int c = 0; c < 9; ++c)
-        for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
-          double s = 0.; for (int l = 0; l < n; ++l) s += Vcl[k + n * l] * b[c + 9 * I3(i, j, l)]; dst[c + 9 * I3(i, j, k)] = s;
-        }
-    };
     for (int e = 0; e < nElems; ++e) {
       int e3[3] = {e % nx, (e / nx) % ny, e / (nx * ny)};
       for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
         const double xi[3] = {C.x[i], C.x[j], C.x[k]};
         map(e3, xi, &X[3 * I3(i, j, k)]);
       }
-      // dX(dd, nn) = d X_nn / d xi_dd
-      for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
-        double* d = &dX[9 * I3(i, j, k)];
-        for (int t = 0; t < 9; ++t) d[t] = 0.;
-        for (int l = 0; l < n; ++l)
-          for (int nn = 0; nn < 3; ++nn) {
-            d[0 * 3 + nn] += C.D[i + n * l] * X[nn + 3 * I3(l, j, k)];
-            d[1 * 3 + nn] += C.D[j + n * l] * X[nn + 3 * I3(i, l, k)];
-            d[2 * 3 + nn] += C.D[k + n * l] * X[nn + 3 * I3(i, j, l)];
-          }
-      }
-      // R(dd, nn) = 1/2 (X_{nn+2} dX_{nn+1}/dxi_dd - X_{nn+1} dX_{nn+2}/dxi_dd)
-      for (size_t t = 0; t < (size_t)n * n2; ++t)
-        for (int dd = 0; dd < 3; ++dd)
-          for (int nn = 0; nn < 3; ++nn) {
-            const int n1 = (nn + 1) % 3, n2_ = (nn + 2) % 3;
-            Rcl[t * 9 + dd * 3 + nn] = 0.5 * (X[n2_ + 3 * t] * dX[t * 9 + dd * 3 + n1] - X[n1 + 3 * t] * dX[t * 9 + dd * 3 + n2_]);
-          }
-      // Ja(dd, nn) = -(d/dxi_{dd+1} R(dd+2, nn) - d/dxi_{dd+2} R(dd+1, nn))
-      for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
-        double* J = &Ja[9 * I3(i, j, k)];
-        for (int t = 0; t < 9; ++t) J[t] = 0.;
-        for (int q = 0; q < n; ++q)
-          for (int nn = 0; nn < 3; ++nn) {
-            J[0 * 3 + nn] += -C.D[j + n * q] * Rcl[9 * I3(i, q, k) + 2 * 3 + nn] + C.D[k + n * q] * Rcl[9 * I3(i, j, q) + 1 * 3 + nn];
-            J[1 * 3 + nn] += -C.D[k + n * q] * Rcl[9 * I3(i, j, q) + 0 * 3 + nn] + C.D[i + n * q] * Rcl[9 * I3(q, j, k) + 2 * 3 + nn];
-            J[2 * 3 + nn] += -C.D[i + n * q] * Rcl[9 * I3(q, j, k) + 1 * 3 + nn] + C.D[j + n * q] * Rcl[9 * I3(i, q, k) + 0 * 3 + nn];
-          }
-      }
-      to_nodes(Ja, JaN);
-      to_nodes(dX, dXN);
-      for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
-        const size_t t = I3(i, j, k), g = vidx(n, i, j, k, e);
-        const double* J = &JaN[9 * t];
-        for (int d = 0; d < 3; ++d) { Mf[d + 3 * g] = J[0 * 3 + d]; Mg[d + 3 * g] = J[1 * 3 + d]; Mh[d + 3 * g] = J[2 * 3 + d]; }
-        const double* a = &dXN[9 * t];
-        const double det = a[0] * (a[4] * a[8] - a[5] * a[7]) - a[1] * (a[3] * a[8] - a[5] * a[6]) +
-                           a[2] * (a[3] * a[7] - a[4] * a[6]);
-        sJ[g] = 1. / det;
-      }
-      // face metrics: JaCL on the face planes (xi = -+1 are CL end points), interpolated in 2D
-      for (int loc = 1; loc <= 6; ++loc)
-        for (int b = 0; b < n; ++b)
-          for (int a = 0; a < n; ++a) {
-            double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-            for (int qb = 0; qb < n; ++qb)
-              for (int qa = 0; qa < n; ++qa) {
-                size_t src;
-                const int pl = (loc == XI_MINUS || loc == ETA_MINUS || loc == ZETA_MINUS) ? 0 : N;
-                if (loc == XI_MINUS || loc == XI_PLUS) src = I3(pl, qa, qb);
-                else if (loc == ETA_MINUS || loc == ETA_PLUS) src = I3(qa, pl, qb);
-                else src = I3(qa, qb, pl);
-                const double wgt = Vcl[a + n * qa] * Vcl[b + n * qb];
-                for (int c = 0; c < 9; ++c) acc[c] += wgt * Ja[9 * src + c];
-              }
-            for (int c = 0; c < 9; ++c) JaFace[(((size_t)e * 6 + (loc - 1)) * n2 + a + n * b) * 9 + c] = acc[c];
-          }
+      curl_metrics(N, C, Vcl, X.data(), e, Mf, Mg, Mh, sJ, &JaFace[(size_t)e * 6 * n2 * 9]);
     }
   }
-  // SurfMetricsFromJa (metrics.f90:752-789) on master sides; master side node (p,q) sits at the
-  // volume face coordinates SideToVol2(p,q,0,loc) (CGNS_SideToVol2, mappings.f90:376-409).
+  // SurfMetricsFromJa (metrics.f90:752-789) on the master sides (every element is master of its
+  // three plus sides)
   for (int e = 0; e < nElems; ++e) {
     const int locs[3] = {XI_PLUS, ETA_PLUS, ZETA_PLUS};
-    for (int d = 0; d < 3; ++d) {
-      const int loc = locs[d];
-      const int side = 3 * e + d;
-      const int nd = NormalDirs[loc] - 1, td = TangDirs[loc] - 1;
-      const double sgn = NormalSigns[loc];
-      for (int q = 0; q <= N; ++q)
-        for (int p = 0; p <= N; ++p) {
-          int a = p, b = q;
-          if (loc == ETA_PLUS) a = N - p;  // CGNS_SideToVol2 for the three plus sides
-          const double* J = &JaFace[(((size_t)e * 6 + (loc - 1)) * n2 + a + n * b) * 9];
-          const size_t f = (size_t)p + n * (q + (size_t)n * side);
-          double se = std::sqrt(J[nd * 3 + 0] * J[nd * 3 + 0] + J[nd * 3 + 1] * J[nd * 3 + 1] + J[nd * 3 + 2] * J[nd * 3 + 2]);
-          double nv[3], t1[3], t2[3];
-          for (int c = 0; c < 3; ++c) nv[c] = sgn * J[nd * 3 + c] / se;
-          const double dot = J[td * 3 + 0] * nv[0] + J[td * 3 + 1] * nv[1] + J[td * 3 + 2] * nv[2];
-          for (int c = 0; c < 3; ++c) t1[c] = J[td * 3 + c] - dot * nv[c];
-          const double tn = std::sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
-          for (int c = 0; c < 3; ++c) t1[c] = t1[c] / tn;
-          t2[0] = nv[1] * t1[2] - nv[2] * t1[1];
-          t2[1] = nv[2] * t1[0] - nv[0] * t1[2];
-          t2[2] = nv[0] * t1[1] - nv[1] * t1[0];
-          surfelem[f] = se;
-          for (int c = 0; c < 3; ++c) { nvec[c + 3 * f] = nv[c]; t1vec[c + 3 * f] = t1[c]; t2vec[c + 3 * f] = t2[c]; }
-        }
-    }
+    for (int d = 0; d < 3; ++d)
+      surface_metrics(N, locs[d], &JaFace[(size_t)e * 6 * n2 * 9], (size_t)(3 * e + d), nvec, t1vec, t2vec, surfelem);
   }
   return DG_OK;
 }

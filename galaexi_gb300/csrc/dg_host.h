@@ -20,4 +20,15 @@ inline double D_at(const Basis1D& B, int i, int l) { return B.D[i + (B.N + 1) * 
 void basis_1d(int N, int node_type, Basis1D& B);
 void set_error(const std::string& s);
 
+// Lagrange interpolation matrix V(j,i) = l_i(y_j) from the N+1 nodes x (barycentric weights wb) to
+// the M+1 points y, column-major (0:M, 0:N)
+void vandermonde(int N, const double* x, const double* wb, int M, const double* y, std::vector<double>& V);
+inline size_t vidx(int n, int i, int j, int k, int e) { return (size_t)i + n * (j + n * (k + (size_t)n * e)); }
+// element metric terms from coordinates at the CGL points of degree N (dg_host.cpp)
+void curl_metrics(int N, const Basis1D& C, const std::vector<double>& Vcl, const double* X, int e, double* Mf,
+                  double* Mg, double* Mh, double* sJ, double* JaFace);
+// normal, tangents and surface element of a master side from the element's face metric terms
+void surface_metrics(int N, int loc, const double* JaFace, size_t side, double* nvec, double* t1vec, double* t2vec,
+                     double* surfelem);
+
 }  // namespace gxh

@@ -83,7 +83,40 @@ class Mesh:
         self.nElems, self.nSides = ne.value, ns.value
         self.nx, self.ny, self.nz = nx, ny, nz
         self.x0, self.x1, self.deform = tuple(x0), tuple(x1), deform
-        n = N + 1
+        self.nBCSides, self.NGeo = 0, None
+        self._alloc()
+        a0 = np.asarray(x0, dtype=np.float64)
+        a1 = np.asarray(x1, dtype=np.float64)
+        nat.check(L.dg_mesh_cartesian(N, node_type, nx, ny, nz, _ptr(a0), _ptr(a1), float(deform),
+                                      _ptr(self.Elem_xGP), _ptr(self.Metrics_fTilde), _ptr(self.Metrics_gTilde),
+                                      _ptr(self.Metrics_hTilde), _ptr(self.sJ), _ptr(self.NormVec),
+                                      _ptr(self.TangVec1), _ptr(self.TangVec2), _ptr(self.SurfElem),
+                                      _ptr(self.ElemToSide), _ptr(self.SideToElem)), "dg_mesh_cartesian")
+
+    @classmethod
+    def from_hopr(cls, path, N, node_type):
+        """A HOPR mesh file (HDF5) read as ReadMesh + CalcMetrics do (dg_mesh_hopr); BC sides come
+        first, BCIndex holds their index into the file's BCNames/BCType."""
+        L = nat.lib()
+        ne, ns, nb, ng = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        p = str(path).encode()
+        nat.check(L.dg_mesh_hopr_sizes(p, ctypes.byref(ne), ctypes.byref(ns), ctypes.byref(nb), ctypes.byref(ng)),
+                  "dg_mesh_hopr_sizes")
+        self = cls.__new__(cls)
+        self.N, self.node_type = N, node_type
+        self.nElems, self.nSides, self.nBCSides, self.NGeo = ne.value, ns.value, nb.value, ng.value
+        self.path = str(path)
+        self._alloc()
+        self.BCIndex = np.zeros(max(1, self.nBCSides), dtype=np.int32)
+        nat.check(L.dg_mesh_hopr(p, N, node_type, _ptr(self.Elem_xGP), _ptr(self.Metrics_fTilde),
+                                 _ptr(self.Metrics_gTilde), _ptr(self.Metrics_hTilde), _ptr(self.sJ), _ptr(self.NormVec),
+                                 _ptr(self.TangVec1), _ptr(self.TangVec2), _ptr(self.SurfElem), _ptr(self.ElemToSide),
+                                 _ptr(self.SideToElem), _ptr(self.BCIndex)), "dg_mesh_hopr")
+        self.BCIndex = self.BCIndex[:self.nBCSides]
+        return self
+
+    def _alloc(self):
+        n = self.N + 1
         E, S = self.nElems, self.nSides
         self.Elem_xGP = np.zeros((E, n, n, n, 3))
         self.Metrics_fTilde = np.zeros((E, n, n, n, 3))
@@ -96,13 +129,6 @@ class Mesh:
         self.SurfElem = np.zeros((S, n, n))
         self.ElemToSide = np.zeros((E, 6, 3), dtype=np.int32)
         self.SideToElem = np.zeros((S, 5), dtype=np.int32)
-        a0 = np.asarray(x0, dtype=np.float64)
-        a1 = np.asarray(x1, dtype=np.float64)
-        nat.check(L.dg_mesh_cartesian(N, node_type, nx, ny, nz, _ptr(a0), _ptr(a1), float(deform),
-                                      _ptr(self.Elem_xGP), _ptr(self.Metrics_fTilde), _ptr(self.Metrics_gTilde),
-                                      _ptr(self.Metrics_hTilde), _ptr(self.sJ), _ptr(self.NormVec),
-                                      _ptr(self.TangVec1), _ptr(self.TangVec2), _ptr(self.SurfElem),
-                                      _ptr(self.ElemToSide), _ptr(self.SideToElem)), "dg_mesh_cartesian")
 
     @property
     def nDOF(self):

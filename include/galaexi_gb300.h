@@ -248,6 +248,17 @@ long long dg_kernel_launch_count(const dg_ctx* ctx);
 /* Description of the last error on the calling thread. */
 const char* dg_last_error(void);
 
+/* ---- HOPR mesh files (HDF5): ReadMesh + BuildCoords + CalcMetrics (mesh_readin.f90:204-470,
+ * metrics.f90:85-789) without MPI and mortars --------------------------------------------------
+ * dg_mesh_hopr_sizes: element/side counts of the file (BC sides counted in nSides; periodic sides
+ * are connected sides, not BC sides).  dg_mesh_hopr: the arrays of dg_mesh_cartesian for N and the
+ * node type, computed from the file's NGeo node coordinates; BC sides come first (1..nBCSides) and
+ * BCIndex[0..nBCSides-1] (if not null) receives their BC index into the file's BCNames/BCType. */
+int dg_mesh_hopr_sizes(const char* path, int* nElems, int* nSides, int* nBCSides, int* NGeo);
+int dg_mesh_hopr(const char* path, int N, int node_type, double* elem_xgp, double* metrics_f, double* metrics_g,
+                 double* metrics_h, double* sJ, double* nvec, double* t1, double* t2, double* surfelem,
+                 int* elem_to_side, int* side_to_elem, int* BCIndex);
+
 /* ---- host-side mesh and state set-up (stand-ins for HOPR + ReadMesh) ------ */
 
 /* Basis of the reference (InitInterpolationBasis + InitDGbasis): arrays of

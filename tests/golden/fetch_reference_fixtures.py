@@ -16,6 +16,7 @@ tree is absent:
   TGV_Re1600_Split_TGVAnalysis_Reference.csv
                                Taylor-Green vortex analysis of the split-form regression run
                                (regressioncheck/checks/tgv/split/), one row every 10 time steps
+  CART_HEX_PERIODIC_008_mesh.h5  the HOPR mesh of that run (8^3 periodic hexahedra on [0,2pi]^3)
 
 Usage:  python tests/golden/fetch_reference_fixtures.py [/path/to/reference]
 """
@@ -38,6 +39,7 @@ FILES = [
 
 REGRESSION = [
     ("regressioncheck/checks/tgv/split", "TGV_Re1600_Split_TGVAnalysis_Reference.csv"),
+    ("regressioncheck/checks/tgv/split", "CART_HEX_PERIODIC_008_mesh.h5"),
 ]
 
 
