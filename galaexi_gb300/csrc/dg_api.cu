@@ -127,6 +127,7 @@ int alloc_prec(dg_ctx* ctx, gxc::PrecData<R>& P, const std::vector<double>& met,
 int check_ctx(dg_ctx* ctx, bool need_mesh) {
   if (!ctx) { set_error("null context"); return DG_ERR_ARG; }
   if (need_mesh && !ctx->mesh_ok) { set_error("dg_set_mesh has not been called"); return DG_ERR_ARG; }
+  if (need_mesh && !ctx->bc_ok) { set_error("the mesh has BC sides: call dg_set_boundaries first"); return DG_ERR_ARG; }
   return DG_OK;
 }
 
@@ -270,6 +271,7 @@ int need_fp64(dg_ctx* ctx, const char* what) {
 
 int tlm_setup(dg_ctx* ctx) {
   if (int rc = need_fp64(ctx, "tangent-linear operator")) return rc;
+  if (ctx->nBCSides) { set_error("tangent-linear operator: periodic meshes only"); return DG_ERR_UNSUPPORTED; }
   if (ctx->cfg.split_dg != DG_SPLIT_NONE && ctx->cfg.split_dg != DG_SPLIT_PI && ctx->cfg.split_dg != DG_SPLIT_KG) {
     set_error("tangent-linear operator: split forms PI and KG only"); return DG_ERR_UNSUPPORTED;
   }
@@ -293,6 +295,7 @@ int tlm_setup(dg_ctx* ctx) {
 
 int adj_setup(dg_ctx* ctx) {
   if (int rc = need_fp64(ctx, "adjoint")) return rc;
+  if (ctx->nBCSides) { set_error("adjoint: periodic meshes only"); return DG_ERR_UNSUPPORTED; }
   const dg_config& c = ctx->cfg;
   if (c.split_dg != DG_SPLIT_NONE && c.split_dg != DG_SPLIT_PI && c.split_dg != DG_SPLIT_KG) {
     set_error("adjoint: split forms PI and KG only"); return DG_ERR_UNSUPPORTED;
@@ -437,6 +440,7 @@ int dg_ctx_destroy(dg_ctx* ctx) {
   ctx->red.release();
   ctx->bad.release();
   ctx->S2E.release(); ctx->wq.release();
+  ctx->bctype.release(); ctx->bcstate.release(); ctx->bcref_d.release(); ctx->bcref_f.release();
   ctx->t.release(); ctx->Ud.release(); ctx->Utd.release();
   ctx->UfB.release(); ctx->GfB.release(); ctx->JB.release(); ctx->UBv.release(); ctx->part.release();
   ctx->acc.release(); ctx->W.release(); ctx->K.release(); ctx->tape.store.release();
@@ -451,7 +455,7 @@ int dg_set_mesh(dg_ctx* ctx, int nElems, int nSides, int nBCSides, const double*
   if (nElems < 1 || nSides < 1 || !Mf || !Mg || !Mh || !sJ || !nv || !t1 || !t2 || !se || !e2s || !s2e) {
     set_error("dg_set_mesh: bad argument"); return DG_ERR_ARG;
   }
-  if (nBCSides != 0) { set_error("boundary sides are not supported"); return DG_ERR_UNSUPPORTED; }
+  if (nBCSides < 0 || nBCSides > nSides) { set_error("dg_set_mesh: bad nBCSides"); return DG_ERR_ARG; }
   const int n = ctx->n, n2 = ctx->n2, n3 = ctx->n3;
   // validate connectivity: every side has one master (flip 0) and one slave (flip 1..4)
   std::vector<int> seen((size_t)nSides * 2, 0);
@@ -465,7 +469,11 @@ int dg_set_mesh(dg_ctx* ctx, int nElems, int nSides, int nBCSides, const double*
       he2s[(e * 6 + ls) * 2 + 1] = flip;
     }
   for (size_t t = 0; t < seen.size(); ++t)
-    if (seen[t] != 1) { set_error("every side needs exactly one master and one slave element"); return DG_ERR_ARG; }
+    if (seen[t] != ((t & 1) && (int)(t / 2) < nBCSides ? 0 : 1)) {
+      set_error("every inner side needs one master and one slave element, every BC side (the first nBCSides) one "
+                "master");
+      return DG_ERR_ARG;
+    }
   (void)s2e;
   // pack metrics [e][10][n3] and face geometry [side][10][n2]
   std::vector<double> met((size_t)nElems * 10 * n3), fgeo((size_t)nSides * 10 * n2);
@@ -526,6 +534,9 @@ int dg_set_mesh(dg_ctx* ctx, int nElems, int nSides, int nBCSides, const double*
   if (!ctx->S2E.alloc(hs2e.size()) || !ctx->wq.alloc(n)) { set_error("cudaMalloc mesh"); return DG_ERR_ALLOC; }
   CUDA_TRY(cudaMemcpy(ctx->S2E.p, hs2e.data(), hs2e.size() * sizeof(int), cudaMemcpyHostToDevice), "upload S2E");
   CUDA_TRY(cudaMemcpy(ctx->wq.p, ctx->B.w.data(), n * sizeof(double), cudaMemcpyHostToDevice), "upload weights");
+  ctx->nBCSides = nBCSides;
+  ctx->bc_ok = nBCSides == 0;
+  ctx->bctype.release(); ctx->bcstate.release(); ctx->bcref_d.release(); ctx->bcref_f.release();
   ctx->t_ok = false;
   ctx->tape.ok = false;
   ctx->t.release(); ctx->Ud.release(); ctx->Utd.release();
@@ -533,6 +544,55 @@ int dg_set_mesh(dg_ctx* ctx, int nElems, int nSides, int nBCSides, const double*
   ctx->W.release(); ctx->K.release(); ctx->tape.store.release();
   ctx->mesh_ok = true;
   ctx->grad_ok = false;
+  return DG_OK;
+}
+
+int dg_set_boundaries(dg_ctx* ctx, const int* bc_type, const int* bc_state, int nRefState, const double* refstate) {
+  if (!ctx || !ctx->mesh_ok) { set_error("dg_set_boundaries: call dg_set_mesh first"); return DG_ERR_ARG; }
+  const int nb = ctx->nBCSides;
+  if (nb == 0) { ctx->bc_ok = true; return DG_OK; }
+  if (!bc_type || !bc_state || nRefState < 1 || !refstate) { set_error("dg_set_boundaries: bad argument"); return DG_ERR_ARG; }
+  std::vector<int> st(nb);
+  for (int s = 0; s < nb; ++s) {
+    const int t = bc_type[s];
+    if (t != 2 && t != 3 && t != 4 && t != 9 && t != 91 && t != 23 && t != 24 && t != 25 && t != 27) {
+      set_error("dg_set_boundaries: BC type " + std::to_string(t) + " is not supported"); return DG_ERR_UNSUPPORTED;
+    }
+    st[s] = bc_state[s] - 1;  // 1-based as in BoundaryType(BC_STATE)
+    const bool needs_state = t != 3 && t != 9 && t != 91;
+    if (needs_state && (st[s] < 0 || st[s] >= nRefState)) { set_error("dg_set_boundaries: BC state out of range"); return DG_ERR_ARG; }
+    if (st[s] < 0 || st[s] >= nRefState) st[s] = 0;
+  }
+  // RefStatePrim as InitEquation (equation.f90:136-147) builds it: T = p * (1/rho) / R
+  std::vector<double> rd((size_t)nRefState * 6);
+  std::vector<float> rf((size_t)nRefState * 6);
+  for (int r = 0; r < nRefState; ++r) {
+    const double* q = refstate + 5 * (size_t)r;
+    for (int c = 0; c < 5; ++c) rd[6 * r + c] = q[c];
+    rd[6 * r + 5] = q[4] * (1. / q[0]) / ctx->cfg.R;
+  }
+  // type 27 states: (Tt, alpha, beta, -, pt), angles in degrees -> the inflow direction a(1:3)
+  // (InitBC, getboundaryflux.f90:199-208), once per state
+  std::vector<char> done(nRefState, 0);
+  for (int s = 0; s < nb; ++s) {
+    if (bc_type[s] != 27 || done[st[s]]) continue;
+    done[st[s]] = 1;
+    double* q = &rd[6 * (size_t)st[s]];
+    const double pi = 3.141592653589793238462643383279502884197;
+    const double ta = std::tan(pi / 180. * q[1]), tb = std::tan(pi / 180. * q[2]);
+    q[1] = 1. / std::sqrt(1. + ta * ta + tb * tb);
+    q[2] = ta / std::sqrt(1. + ta * ta + tb * tb);
+    q[3] = tb / std::sqrt(1. + ta * ta + tb * tb);
+  }
+  for (size_t i = 0; i < rd.size(); ++i) rf[i] = (float)rd[i];
+  if (!ctx->bctype.alloc(nb) || !ctx->bcstate.alloc(nb) || !ctx->bcref_d.alloc(rd.size()) || !ctx->bcref_f.alloc(rf.size())) {
+    set_error("cudaMalloc boundaries"); return DG_ERR_ALLOC;
+  }
+  CUDA_TRY(cudaMemcpy(ctx->bctype.p, bc_type, nb * sizeof(int), cudaMemcpyHostToDevice), "upload BC types");
+  CUDA_TRY(cudaMemcpy(ctx->bcstate.p, st.data(), nb * sizeof(int), cudaMemcpyHostToDevice), "upload BC states");
+  CUDA_TRY(cudaMemcpy(ctx->bcref_d.p, rd.data(), rd.size() * sizeof(double), cudaMemcpyHostToDevice), "upload RefStates");
+  CUDA_TRY(cudaMemcpy(ctx->bcref_f.p, rf.data(), rf.size() * sizeof(float), cudaMemcpyHostToDevice), "upload RefStates");
+  ctx->bc_ok = true;
   return DG_OK;
 }
 

@@ -84,7 +84,13 @@ struct AdjTape {
 struct dg_ctx {
   dg_config cfg;
   int N = 0, n = 0, n2 = 0, n3 = 0;
-  int nElems = 0, nSides = 0;
+  int nElems = 0, nSides = 0, nBCSides = 0;
+  // boundary sides (the first nBCSides sides): BC type and 0-based reference state per side, and
+  // the reference states [state][6] in FP64 and FP32
+  gxc::DBuf<int> bctype, bcstate;
+  gxc::DBuf<double> bcref_d;
+  gxc::DBuf<float> bcref_f;
+  bool bc_ok = false;
   gxh::Basis1D B;
   gxc::PrecData<double> d;
   gxc::PrecData<float> f;
@@ -121,6 +127,10 @@ inline gx::Launch make_launch(const dg_ctx* ctx) {
   L.lift_mode = ctx->cfg.do_weak_lifting ? 2 : (ctx->cfg.do_conservative_lifting ? 1 : 0);
   L.br2 = ctx->cfg.lifting == DG_LIFTING_BR2 ? 1 : 0;
   L.eta_br2 = ctx->cfg.eta_br2;
+  L.nBCSides = ctx->nBCSides;
+  L.bctype = ctx->bctype.p;
+  L.bcstate = ctx->bcstate.p;
+  L.bcref = ctx->cfg.precision == DG_PRECISION_FP64 ? (const void*)ctx->bcref_d.p : (const void*)ctx->bcref_f.p;
   return L;
 }
 

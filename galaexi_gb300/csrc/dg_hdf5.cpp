@@ -35,7 +35,15 @@ bool File::open(const std::string& path, std::string& err) {
   if (got != d_.size()) { err = "short read of " + path; return false; }
   try {
     static const uint8_t sig[8] = {0x89, 'H', 'D', 'F', '\r', '\n', 0x1a, '\n'};
-    if (d_.size() < 96 || std::memcmp(d_.data(), sig, 8) != 0) { err = path + " is not an HDF5 file"; return false; }
+    // the superblock sits at 0 or, after a user block (FLEXI stores its parameter file there), at
+    // 512, 1024, 2048, ...; file addresses are relative to it (base address = its position)
+    uint64_t base = 0;
+    while (base + 96 <= d_.size() && std::memcmp(d_.data() + base, sig, 8) != 0) base = base ? 2 * base : 512;
+    if (base + 96 > d_.size()) { err = path + " is not an HDF5 file"; return false; }
+    if (base) {
+      if (u(base + 24, 8) != base) { err = "HDF5 base address other than the superblock position is not supported"; return false; }
+      d_.erase(d_.begin(), d_.begin() + (long)base);
+    }
     if (d_[8] != 0) { err = "HDF5 superblock version " + std::to_string(d_[8]) + " is not supported (need 0)"; return false; }
     if (d_[13] != 8 || d_[14] != 8) { err = "HDF5 offsets/lengths other than 8 bytes are not supported"; return false; }
     // root group symbol table entry at 56: name offset, object header, cache type, reserved, scratch

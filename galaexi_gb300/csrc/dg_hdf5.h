@@ -1,6 +1,6 @@
 // Minimal HDF5 reader for the datasets and attributes of HOPR mesh files and FLEXI state files.
 //
-// Covers the file-format subset these files use: superblock version 0 (8-byte offsets and
+// Covers the file-format subset these files use: an optional user block, superblock version 0 (8-byte offsets and
 // lengths), object headers version 1 with continuation blocks, old-style groups (symbol-table
 // message, v1 B-tree of group nodes, local heap), dataspace messages v1/v2, fixed-point,
 // floating-point and fixed-length string datatypes, contiguous and compact data layouts (layout

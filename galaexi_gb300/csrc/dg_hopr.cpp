@@ -11,7 +11,9 @@
 // the master element (SurfMetricsFromJa, metrics.f90:752-789).  Side numbering: BC sides first
 // (1..nBCSides), then the connected sides in order of first appearance.  Mortar meshes are not
 // supported.
+#include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <map>
 #include <string>
 #include <vector>
@@ -347,6 +349,64 @@ extern "C" int dg_mesh_hopr_sizes(const char* path, int* nElems, int* nSides, in
   *nSides = H.nSides;
   *nBCSides = H.nBCSides;
   *NGeo = H.NGeo;
+  return DG_OK;
+}
+
+extern "C" int dg_h5_read(const char* path, const char* name, int attribute, int* ndims, long long* dims, double* out,
+                          long long cap, char* str, int str_len) {
+  if (!path || !name || !ndims || !dims) { set_error("dg_h5_read: null argument"); return DG_ERR_ARG; }
+  gxh5::File f;
+  std::string err;
+  if (!f.open(path, err)) { set_error(err); return DG_ERR_ARG; }
+  gxh5::Array a;
+  if (!(attribute ? f.attribute(name, a, err) : f.dataset(name, a, err))) { set_error(err); return DG_ERR_ARG; }
+  if (a.dims.size() > 8) { set_error("dg_h5_read: more than 8 dimensions"); return DG_ERR_UNSUPPORTED; }
+  *ndims = (int)a.dims.size();
+  for (size_t d = 0; d < a.dims.size(); ++d) dims[d] = (long long)a.dims[d];
+  if (a.cls == 3) {
+    if (str && str_len > 1) {
+      const std::vector<std::string> v = a.as_strings();
+      std::memset(str, 0, str_len);
+      if (!v.empty()) std::memcpy(str, v[0].data(), std::min((size_t)str_len - 1, v[0].size()));
+    }
+    return DG_OK;
+  }
+  if (out) {
+    if ((unsigned long long)cap < a.count()) { set_error("dg_h5_read: output too small"); return DG_ERR_ARG; }
+    const std::vector<double> v = a.as_double();
+    std::memcpy(out, v.data(), v.size() * sizeof(double));
+  }
+  return DG_OK;
+}
+
+extern "C" int dg_mesh_hopr_bcs(const char* path, int* nBCs, char* names, int name_len, int* bc_type) {
+  if (!path || !nBCs) { set_error("dg_mesh_hopr_bcs: null argument"); return DG_ERR_ARG; }
+  gxh5::File f;
+  std::string err;
+  if (!f.open(path, err)) { set_error(err); return DG_ERR_ARG; }
+  *nBCs = 0;
+  if (!f.has_dataset("BCType")) return DG_OK;
+  gxh5::Array t, nm;
+  if (!f.dataset("BCType", t, err) || !f.dataset("BCNames", nm, err)) { set_error(err); return DG_ERR_ARG; }
+  if (t.dims.size() != 2 || t.dims[1] != 4) { set_error("BCType must be (nBCs,4)"); return DG_ERR_ARG; }
+  const std::vector<std::string> bn = nm.as_strings();
+  if (bn.size() != t.dims[0]) { set_error("BCNames and BCType differ in length"); return DG_ERR_ARG; }
+  *nBCs = (int)t.dims[0];
+  if (bc_type) {
+    const std::vector<long long> v = t.as_int();
+    for (size_t i = 0; i < v.size(); ++i) bc_type[i] = (int)v[i];
+  }
+  if (names) {
+    if (name_len < 2) { set_error("dg_mesh_hopr_bcs: name_len too small"); return DG_ERR_ARG; }
+    for (int b = 0; b < *nBCs; ++b) {
+      // names are fixed-length, blank padded: trimmed as Fortran TRIM does
+      std::string x = bn[b];
+      while (!x.empty() && (x.back() == ' ' || x.back() == '\0')) x.pop_back();
+      char* dst = names + (size_t)b * name_len;
+      std::memset(dst, 0, name_len);
+      std::memcpy(dst, x.data(), std::min((size_t)name_len - 1, x.size()));
+    }
+  }
   return DG_OK;
 }
 

@@ -19,6 +19,7 @@
 // The caller's U / Ut / Ut_tmp keep the reference layout (5,0:N,0:N,0:N,nElems), FP64.
 #pragma once
 #include "dg_physics.cuh"
+#include "dg_bc.cuh"
 
 namespace gx {
 
@@ -97,6 +98,12 @@ struct Launch {
   int lift_mode;    // 0: strong non-conservative, 1: strong conservative, 2: weak
   int br2;          // 1: BR2 face traces (lifting_br2.t90:191-310), strong form only
   double eta_br2;   // BR2 penalty etaBR2
+  // boundary sides: the first nBCSides sides; per side BC type and reference-state index, and the
+  // reference states (compute type, [state][6]); see dg_bc.cuh
+  int nBCSides;
+  const int* bctype;
+  const int* bcstate;
+  const void* bcref;
 };
 
 template <int NP> struct EPBof { static constexpr int v = (NP * NP * NP >= 128) ? 1 : (256 / (NP * NP * NP)); };
@@ -174,10 +181,37 @@ k_prolong(const S* __restrict__ U, const int* __restrict__ E2S, const double* __
 // k_lift: Lifting_BR1 (lifting_br1.t90:47-167): volume part + surface part + sJ, then
 // ProlongToFaceLifting.  Lifted variables (rho,u,v,w,T) = PRIM_LIFT (eos.h:143).
 // =====================================================================================
+// Outer state of the lifting flux at a face node: the slave primitives (rho,u,v,w,T), or on a BC
+// side the ghost state that reproduces the boundary lifting flux (Lifting_GetBoundaryFlux_Kernel,
+// getboundaryflux.f90:945-1019)
+template <typename R>
+__device__ __forceinline__ void lift_outer_state(const Launch& L, const Gas<R>& gas, int side, const R* pm,
+                                                 const R* ps, const R* fg, int n2, R out[5]) {
+  const int liftc[5] = {0, 1, 2, 3, 5};
+  if (side >= L.nBCSides) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) out[v] = ps[liftc[v] * n2];
+    return;
+  }
+  R Pm[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) Pm[c] = pm[c * n2];
+  Pm[4] = p_abs(Pm[4], gas);
+  const R nv[3] = {fg[0], fg[n2], fg[2 * n2]};
+  const R t1[3] = {fg[3 * n2], fg[4 * n2], fg[5 * n2]};
+  const R t2[3] = {fg[6 * n2], fg[7 * n2], fg[8 * n2]};
+  const int bt = L.bctype[side];
+  const R* ref = static_cast<const R*>(L.bcref) + 6 * L.bcstate[side];
+  R Pb[6];
+  bc_state(bt, Pm, ref, nv, t1, t2, gas.kappa, gas.R_gas, Pb);
+  bc_lift_ghost(bt, Pm, Pb, out);
+}
+
 template <int NP, typename R>
 __global__ void __launch_bounds__(EPBof<NP>::v * NP * NP * NP)
 k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restrict__ Pf, const R* __restrict__ Fgeo,
-       const int* __restrict__ E2S, DevBasis<R> basis, Launch L, R* __restrict__ Gvol, R* __restrict__ Gf) {
+       const int* __restrict__ E2S, DevBasis<R> basis, Launch L, Gas<R> gas_lift, R* __restrict__ Gvol,
+       R* __restrict__ Gf) {
   constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, EPB = EPBof<NP>::v, N = NP - 1;
   __shared__ SBasis<NP, R> sb;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -288,13 +322,15 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
       const R* pm = Pf + (size_t)side * 6 * n2 + pq;
       const R* ps = Pf + ((size_t)L.nSides + side) * 6 * n2 + pq;
       const R* fg = Fgeo + (size_t)side * 10 * n2 + pq;
+      R psv[5];
+      lift_outer_state(L, gas_lift, side, pm, ps, fg, n2, psv);
       const R sig = (L.lift_mode == 2) ? ((flip == 0) ? R(1) : R(-1)) : R(1);
       const R wgt = sig * Lhat * R(0.5) * fg[9 * n2] * sj;
       const R nvv[3] = {wgt * fg[0], wgt * fg[n2], wgt * fg[2 * n2]};
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
         const int c = liftc[v];
-        const R fl = sigflux * pm[c * n2] + ps[c * n2];
+        const R fl = sigflux * pm[c * n2] + psv[v];
 #pragma unroll
         for (int d = 0; d < 3; ++d) g[d][v] = g[d][v] + fl * nvv[d];
       }
@@ -334,6 +370,8 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
         const R* pm = Pf + (size_t)side * 6 * n2 + pq;
         const R* ps = Pf + ((size_t)L.nSides + side) * 6 * n2 + pq;
         const R* fg = Fgeo + (size_t)side * 10 * n2 + pq;
+        R psv[5];
+        lift_outer_state(L, gas_lift, side, pm, ps, fg, n2, psv);
         const R sj = Met[((size_t)e * 10 + 9) * n3 + node];
         const R sig = (L.lift_mode == 2) ? ((flip == 0) ? R(1) : R(-1)) : R(1);
         const R wgt = sig * Lhat * R(0.5) * fg[9 * n2] * sj;
@@ -341,7 +379,7 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
 #pragma unroll
         for (int v = 0; v < 5; ++v) {
           const int c = liftc[v];
-          const R fl = sigflux * pm[c * n2] + ps[c * n2];
+          const R fl = sigflux * pm[c * n2] + psv[v];
 #pragma unroll
           for (int d = 0; d < 3; ++d) Gs[el][d * 5 + v][node] = Gs[el][d * 5 + v][node] + fl * nvv[d];
         }
@@ -374,6 +412,7 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
     const R* pm = nullptr;
     const R* ps = nullptr;
     const R* fg = nullptr;
+    R psv[5];
     if (L.br2) {
       const R* Lv = is_minus(ls) ? sb.Lm : sb.Lp;
       const R* Lh = is_minus(ls) ? sb.Lhm : sb.Lhp;
@@ -384,6 +423,7 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
       bw = R(L.eta_br2) * R(0.5) * fg[9 * n2] * bw;
       pm = Pf + (size_t)side * 6 * n2 + pq;
       ps = Pf + ((size_t)L.nSides + side) * 6 * n2 + pq;
+      lift_outer_state(L, gas_lift, side, pm, ps, fg, n2, psv);
     }
     for (int c = 0; c < 15; ++c) {
       R s;
@@ -397,7 +437,7 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
       }
       if (L.br2) {
         const int d = c / 5, v = c - 5 * d;
-        s = s + bw * (ps[liftc[v] * n2] - pm[liftc[v] * n2]) * fg[d * n2];
+        s = s + bw * (psv[v] - pm[liftc[v] * n2]) * fg[d * n2];
       }
       gf[c * n2] = s;
     }
@@ -432,6 +472,59 @@ k_face(const R* __restrict__ Uf, const R* __restrict__ Pf, const R* __restrict__
   const R t2[3] = {fg[6 * n2], fg[7 * n2], fg[8 * n2]};
   const R se = fg[9 * n2];
   R F[5];
+  if (side < L.nBCSides) {
+    // GetBoundaryFlux_GPU (getboundaryflux.f90:542-838)
+    const int bt = L.bctype[side];
+    const R* ref = static_cast<const R*>(L.bcref) + 6 * L.bcstate[side];
+    R Pm[6], Pb[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) Pm[c] = PL[c];
+    Pm[4] = p_abs(PL[4], gas);
+    bc_state(bt, Pm, ref, nv, t1, t2, gas.kappa, gas.R_gas, Pb);
+    R gx[5], gy[5], gz[5], fd[5];
+    if (L.parabolic) {
+      const R* gm = Gf + (size_t)side * 15 * n2 + pq;
+#pragma unroll
+      for (int v = 0; v < 5; ++v) { gx[v] = gm[v * n2]; gy[v] = gm[(5 + v) * n2]; gz[v] = gm[(10 + v) * n2]; }
+    }
+    if (bc_riemann_type(bt)) {
+      // Riemann solver between the inner state and the boundary state (both via PrimToCons)
+      R Uc[5], Ub[5], Ps[6];
+      prim_to_cons_face(Pm, gas, Uc);
+      prim_to_cons_face(Pb, gas, Ub);
+#pragma unroll
+      for (int c = 0; c < 6; ++c) Ps[c] = Pb[c];
+      Ps[4] = OffsetOf<R>::v ? Pb[4] - gas.pref : Pb[4];
+      riemann_face(L.riemann, L.split, Uc, Ub, PL, Ps, nv, t1, t2, gas, F);
+      if (L.parabolic) {
+        normal_diff_flux(PL, gx, gy, gz, nv, gas.mu, gas.lambda, fd);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) F[v] = F[v] + R(0.5) * fd[v];
+        normal_diff_flux(Pb, gx, gy, gz, nv, gas.mu, gas.lambda, fd);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) F[v] = F[v] + R(0.5) * fd[v];
+      }
+    } else {
+      // walls: pressure flux, plus the viscous flux of the wall state
+      const R pw = OffsetOf<R>::v ? Pb[4] - gas.pref : Pb[4];
+      F[0] = R(0);
+      F[1] = pw * nv[0];
+      F[2] = pw * nv[1];
+      F[3] = pw * nv[2];
+      F[4] = R(0);
+      if (L.parabolic) {
+        if (bt == 9 || bt == 91) bc_wall_gradients(bt, nv, t1, t2, gx, gy, gz);
+        normal_diff_flux(Pb, gx, gy, gz, nv, gas.mu, gas.lambda, fd);
+        if (bt == 3) fd[4] = R(0);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) F[v] = F[v] + fd[v];
+      }
+    }
+    R* out = Flux + (size_t)side * 5 * n2 + pq;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) out[v * n2] = F[v] * se;
+    return;
+  }
   riemann_face(L.riemann, L.split, UL, UR, PL, PR, nv, t1, t2, gas, F);
   if (L.parabolic) {
     // ViscousFlux_Kernel_CUDA (riemann.f90:638-700): F = F + 0.5*f(L); F = F + 0.5*f(R)

@@ -94,7 +94,7 @@ void rhs_front(dg_ctx* ctx, PrecData<R>& P, const S* U, const gx::Gas<R>& gas, c
   ctx->launches++;
   if (ev) cudaEventRecord(ev[1], st);
   if (ctx->cfg.parabolic) {
-    gx::k_lift<NP, R><<<grid, NT, lift_smem<R>(), st>>>(P.Pvol.p, P.Met.p, P.Pf.p, P.Fgeo.p, ctx->E2S.p, b, L,
+    gx::k_lift<NP, R><<<grid, NT, lift_smem<R>(), st>>>(P.Pvol.p, P.Met.p, P.Pf.p, P.Fgeo.p, ctx->E2S.p, b, L, gas,
                                                         P.Gvol.p, P.Gf.p);
     ctx->launches++;
   }

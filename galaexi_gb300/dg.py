@@ -65,6 +65,24 @@ def basis(N, node_type):
     return out
 
 
+def read_h5(path, name, attribute=False):
+    """A dataset or root attribute of an HDF5 file (dg_h5_read): a numpy float64 array in the file's
+    (C) shape, or a str for string data."""
+    L = nat.lib()
+    nd = ctypes.c_int()
+    dims = np.zeros(8, dtype=np.int64)
+    p, nm = str(path).encode(), str(name).encode()
+    buf = ctypes.create_string_buffer(1024)
+    nat.check(L.dg_h5_read(p, nm, int(attribute), ctypes.byref(nd), _ptr(dims), None, 0, buf, 1024), "dg_h5_read")
+    shape = tuple(int(d) for d in dims[:nd.value])
+    if buf.value:
+        return buf.value.decode()
+    out = np.zeros(shape if shape else (1,))
+    nat.check(L.dg_h5_read(p, nm, int(attribute), ctypes.byref(nd), _ptr(dims), _ptr(out), out.size, None, 0),
+              "dg_h5_read")
+    return out
+
+
 class Mesh:
     """Periodic hexahedral box with the reference's connectivity and metric arrays.
 
@@ -113,7 +131,32 @@ class Mesh:
                                  _ptr(self.TangVec1), _ptr(self.TangVec2), _ptr(self.SurfElem), _ptr(self.ElemToSide),
                                  _ptr(self.SideToElem), _ptr(self.BCIndex)), "dg_mesh_hopr")
         self.BCIndex = self.BCIndex[:self.nBCSides]
+        nbc = ctypes.c_int()
+        nat.check(L.dg_mesh_hopr_bcs(p, ctypes.byref(nbc), None, 0, None), "dg_mesh_hopr_bcs")
+        NL = 256
+        names = ctypes.create_string_buffer(max(1, nbc.value) * NL)
+        self.BCType = np.zeros((max(1, nbc.value), 4), dtype=np.int32)
+        nat.check(L.dg_mesh_hopr_bcs(p, ctypes.byref(nbc), names, NL, _ptr(self.BCType)), "dg_mesh_hopr_bcs")
+        self.BCType = self.BCType[:nbc.value]
+        self.BCNames = [names.raw[b * NL:(b + 1) * NL].split(b"\0", 1)[0].decode() for b in range(nbc.value)]
         return self
+
+    def boundaries(self, refstates, boundary_types=None):
+        """(bc_type, bc_state, refstates) for DG(..., boundaries=...): the file's BCType with the
+        parameter file's BoundaryName / BoundaryType overrides (ReadBCs, mesh_readin.f90:98-169: an
+        exact name match replaces type and state; an unknown name is an error), per BC side.
+        refstates: the RefState rows (rho, u, v, w, p), type 27 rows (Tt, alpha, beta, -, pt)."""
+        bct = self.BCType.copy()
+        for name, (typ, state) in (boundary_types or {}).items():
+            hit = [b for b, bn in enumerate(self.BCNames) if bn == name]
+            if not hit:
+                raise ValueError(f"Boundary condition specified in parameter file has not been found: {name}")
+            for b in hit:
+                if (typ == 1) != (bct[b, 0] == 1):
+                    raise ValueError(f"boundary {name}: remapping between periodic and non-periodic is not supported")
+                bct[b, 0], bct[b, 2] = typ, state
+        idx = self.BCIndex - 1
+        return bct[idx, 0].astype(np.int32), bct[idx, 2].astype(np.int32), np.asarray(refstates, dtype=np.float64)
 
     def _alloc(self):
         n = self.N + 1
@@ -156,9 +199,11 @@ class DG:
     U, Ut, Ut_tmp are torch float64 CUDA tensors of shape (nElems, n, n, n, 5) (reference layout).
     """
 
-    def __init__(self, cfg, mesh, pressure_offset=None):
+    def __init__(self, cfg, mesh, pressure_offset=None, boundaries=None):
         """pressure_offset: reference pressure of the mixed form (dg_set_pressure_offset); None picks
-        the volume-mean pressure of the first state this operator sees (mixed form only)."""
+        the volume-mean pressure of the first state this operator sees (mixed form only).
+        boundaries: for meshes with BC sides, (bc_type, bc_state, refstates): per BC side type and
+        1-based RefState index, and the RefStates (n x 5 primitives) -- see dg_set_boundaries."""
         import torch  # device memory and streams only
         self._pref = pressure_offset
         self._torch = torch
@@ -169,10 +214,19 @@ class DG:
         nat.check(L.dg_ctx_create(ctypes.byref(cfg), ctypes.byref(h)), "dg_ctx_create")
         self._h = h
         m = mesh
-        nat.check(L.dg_set_mesh(h, m.nElems, m.nSides, 0, _ptr(m.Metrics_fTilde), _ptr(m.Metrics_gTilde),
+        nat.check(L.dg_set_mesh(h, m.nElems, m.nSides, getattr(m, "nBCSides", 0), _ptr(m.Metrics_fTilde),
+                                _ptr(m.Metrics_gTilde),
                                 _ptr(m.Metrics_hTilde), _ptr(m.sJ), _ptr(m.NormVec), _ptr(m.TangVec1),
                                 _ptr(m.TangVec2), _ptr(m.SurfElem), _ptr(m.ElemToSide), _ptr(m.SideToElem)),
                   "dg_set_mesh")
+        if getattr(m, "nBCSides", 0):
+            if boundaries is None:
+                raise ValueError("mesh has BC sides: pass boundaries=(bc_type, bc_state, refstates)")
+            bt, bs, rs = boundaries
+            self._bc = (np.ascontiguousarray(bt, dtype=np.int32), np.ascontiguousarray(bs, dtype=np.int32),
+                        np.ascontiguousarray(rs, dtype=np.float64).reshape(-1, 5))
+            nat.check(L.dg_set_boundaries(h, _ptr(self._bc[0]), _ptr(self._bc[1]), self._bc[2].shape[0],
+                                          _ptr(self._bc[2])), "dg_set_boundaries")
         if pressure_offset is not None:
             nat.check(L.dg_set_pressure_offset(h, float(pressure_offset)), "dg_set_pressure_offset")
 

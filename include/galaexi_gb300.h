@@ -115,14 +115,26 @@ int dg_ctx_destroy(dg_ctx* ctx);
 /* Upload mesh data (host pointers, layouts above) and size all scratch.
  * Replaces the device copies of InitMesh (src/mesh/mesh.f90:307-451) and
  * InitCalctimestep (calctimestep.f90:51-92).  Periodic and inner faces are
- * resolved in-kernel; boundary sides (nBCSides > 0) are not supported yet
- * and return DG_ERR_UNSUPPORTED. */
+ * resolved in-kernel.  As in the reference's side order, the first nBCSides sides
+ * are boundary sides with a master element only; a mesh with nBCSides > 0 needs
+ * dg_set_boundaries before the operator is used. */
 int dg_set_mesh(dg_ctx* ctx, int nElems, int nSides, int nBCSides,
                 const double* metrics_f, const double* metrics_g, const double* metrics_h,
                 const double* sJ,
                 const double* normvec, const double* tangvec1, const double* tangvec2,
                 const double* surfelem,
                 const int* elem_to_side, const int* side_to_elem);
+
+/* Boundary conditions of the BC sides: the reference's BCSides(BC_TYPE, BC_STATE) per side and
+ * its RefStates (InitBC, equations/navierstokes/idealgas/getboundaryflux.f90:87-256).
+ * bc_type[s], bc_state[s] for s < nBCSides: type 2 (Dirichlet, RefState), 3 (adiabatic wall),
+ * 4 (isothermal wall, RefState temperature), 9 / 91 (slip walls), 23 (outflow, RefState u = Mach
+ * number), 24 / 25 (pressure / subsonic outflow, RefState p), 27 (subsonic inflow); bc_state is
+ * the 1-based RefState index (ignored for 3, 9, 91).  refstate: nRefState x 5 RefState rows as in
+ * the parameter file, (rho, u, v, w, p); a state used by type 27 is (Tt, alpha, beta, -, pt) with
+ * the angles in degrees and is turned into the inflow direction as InitBC does.
+ * Other BC types return DG_ERR_UNSUPPORTED. */
+int dg_set_boundaries(dg_ctx* ctx, const int* bc_type, const int* bc_state, int nRefState, const double* refstate);
 
 /* Ut = DGTimeDerivative_weakForm(U) at time t (src/dg/dg.f90:255-425).
  * d_U, d_Ut: device FP64 arrays (5,0:N,0:N,0:N,nElems); stream: cudaStream_t or NULL. */
@@ -255,6 +267,16 @@ const char* dg_last_error(void);
  * node type, computed from the file's NGeo node coordinates; BC sides come first (1..nBCSides) and
  * BCIndex[0..nBCSides-1] (if not null) receives their BC index into the file's BCNames/BCType. */
 int dg_mesh_hopr_sizes(const char* path, int* nElems, int* nSides, int* nBCSides, int* NGeo);
+/* The file's boundary table (ReadBCs, mesh_readin.f90:78-189): *nBCs, and if not null the names
+ * (nBCs x name_len bytes, NUL-terminated, trailing blanks trimmed) and BCType rows (nBCs x 4:
+ * type, curve index, state, periodic vector index). */
+int dg_mesh_hopr_bcs(const char* path, int* nBCs, char* names, int name_len, int* bc_type);
+/* A dataset (attribute = 0) or root attribute (attribute = 1) of an HDF5 file such as a FLEXI state
+ * file (DG_Solution, Time, N, NodeType, MeshFile; ReadState, restart.f90): *ndims and dims[0..7]
+ * (slowest first); numbers as doubles into out (if not null; cap >= element count); a string's first
+ * element into str (str_len bytes, NUL-terminated). */
+int dg_h5_read(const char* path, const char* name, int attribute, int* ndims, long long* dims, double* out,
+               long long cap, char* str, int str_len);
 int dg_mesh_hopr(const char* path, int N, int node_type, double* elem_xgp, double* metrics_f, double* metrics_g,
                  double* metrics_h, double* sJ, double* nvec, double* t1, double* t2, double* surfelem,
                  int* elem_to_side, int* side_to_elem, int* BCIndex);

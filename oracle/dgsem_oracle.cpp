@@ -305,6 +305,11 @@ struct Ctx {
   int s2v2_inv(int c, int a, int b, int flip, int locSide) const {
     return S2V2_inv[c + 2 * (a + n * (b + n * (flip + 5 * (locSide - 1))))];
   }
+  // boundary sides 0..nBCSides-1 (InitBC, getboundaryflux.f90:87-256): type, 0-based RefState index,
+  // RefStatePrim (rho, u, v, w, p, T) per state
+  int nBCSides = 0;
+  std::vector<int> bctype, bcstate;
+  std::vector<double> refprim;
   // index helpers (0-based element / side)
   size_t vol(int i, int j, int k, int e) const { return (size_t)i + n * (j + n * (k + (size_t)n * e)); }
   size_t fac(int p, int q, int s) const { return (size_t)p + n * (q + (size_t)n * s); }
@@ -869,6 +874,257 @@ static void EvalTransformedDiffFlux3D(const double* P, const double* gx, const d
 }
 
 // ---------------------------------------------------------------------------------------
+// Boundary conditions: equations/navierstokes/idealgas/getboundaryflux.f90
+// ---------------------------------------------------------------------------------------
+// PRESSURE_RIEMANN_PURE  idealgas/eos.f90:605-628 (U_Prim in the side-normal frame)
+static double PRESSURE_RIEMANN_PURE(const double* U_Prim, double Kappa) {
+  double P_RP;
+  if (U_Prim[VEL1] <= 0.) {  // rarefaction
+    const double kappaFac = 2. * Kappa / (Kappa - 1.);
+    P_RP = U_Prim[PRES] *
+           std::pow(std::max(0.0001, (1. + 0.5 * (Kappa - 1.) * U_Prim[VEL1] / std::sqrt(Kappa * U_Prim[PRES] / U_Prim[DENS]))),
+                    kappaFac);
+  } else {  // shock
+    const double ar = 2. / ((Kappa + 1.) * U_Prim[DENS]);
+    const double br = (Kappa - 1.) / (Kappa + 1.) * U_Prim[PRES];
+    P_RP = U_Prim[PRES] + U_Prim[VEL1] / ar * 0.5 *
+                              (U_Prim[VEL1] + std::sqrt(U_Prim[VEL1] * U_Prim[VEL1] + 4. * ar * (U_Prim[PRES] + br)));
+  }
+  return P_RP;
+}
+
+// GetBoundaryState  getboundaryflux.f90:262-487
+static void GetBoundaryState(int BCType, double* UPrim_Out, const double* UPrim_master, const double* RefStatePrim,
+                             const double* NormVec, const double* TangVec1, const double* TangVec2, double kappa,
+                             double R) {
+  if (BCType == 2) {
+    for (int c = 0; c < 6; ++c) UPrim_Out[c] = RefStatePrim[c];
+    return;
+  }
+  auto dot3 = [](const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+  double B[6];
+  B[DENS] = UPrim_master[DENS];
+  B[VEL1] = dot3(&UPrim_master[VEL1], NormVec);
+  B[VEL2] = dot3(&UPrim_master[VEL1], TangVec1);
+  B[VEL3] = dot3(&UPrim_master[VEL1], TangVec2);
+  B[PRES] = UPrim_master[PRES];
+  B[TEMP] = UPrim_master[TEMP];
+  switch (BCType) {
+    case 3:
+    case 4:  // adiabatic / isothermal wall
+      B[PRES] = PRESSURE_RIEMANN_PURE(B, kappa);
+      B[VEL1] = 0.; B[VEL2] = 0.; B[VEL3] = 0.;
+      B[TEMP] = BCType == 3 ? UPrim_master[TEMP] : RefStatePrim[TEMP];
+      B[DENS] = B[PRES] / (B[TEMP] * R);
+      break;
+    case 9:
+    case 91:  // slip wall
+      B[PRES] = PRESSURE_RIEMANN_PURE(B, kappa);
+      B[VEL1] = 0.;
+      B[DENS] = UPrim_master[DENS];
+      B[TEMP] = B[PRES] / (B[DENS] * R);
+      break;
+    case 23: {  // outflow Mach number
+      const double MaOut = RefStatePrim[1];
+      const double c = std::sqrt(kappa * B[PRES] / B[DENS]);
+      const double Ma = B[VEL1] / c;
+      double pb;
+      if (Ma < 1) {
+        const double pt = B[PRES] * (std::pow(1 + 0.5 * (kappa - 1) * Ma * Ma, kappa / (kappa - 1.)));
+        pb = pt * (std::pow(1 + 0.5 * (kappa - 1) * MaOut * MaOut, -kappa / (kappa - 1.)));
+      } else {
+        pb = B[PRES] + 0.5 * B[DENS] * dot3(&B[VEL1], &B[VEL1]);
+      }
+      B[DENS] = kappa * pb / (c * c);
+      B[PRES] = pb;
+      B[TEMP] = B[PRES] / (R * B[DENS]);
+      break;
+    }
+    case 24: {  // pressure outflow
+      const double c = std::sqrt(kappa * B[PRES] / B[DENS]);
+      const double Ma = B[VEL1] / c;
+      if (Ma < 1) {
+        const double pb = RefStatePrim[4];
+        B[DENS] = kappa * pb / (c * c);
+        B[PRES] = pb;
+        B[TEMP] = B[PRES] / (R * B[DENS]);
+      }
+      break;
+    }
+    case 25: {  // subsonic outflow
+      const double c = std::sqrt(kappa * B[PRES] / B[DENS]);
+      const double Ma = B[VEL1] / c;
+      const double pb = Ma < 1 ? RefStatePrim[4] : B[PRES] + 0.5 * B[DENS] * dot3(&B[VEL1], &B[VEL1]);
+      if (B[VEL1] < 0.) {
+        B[VEL1] = std::fabs(B[VEL1]);
+        B[VEL2] = 0.;
+        B[VEL3] = 0.;
+      }
+      B[DENS] = kappa * pb / (c * c);
+      B[PRES] = RefStatePrim[4];
+      B[TEMP] = B[PRES] / (R * B[DENS]);
+      break;
+    }
+    case 27: {  // subsonic inflow
+      const double Tt = RefStatePrim[0], pt = RefStatePrim[4];
+      const double* a = &RefStatePrim[1];
+      const double A = -1. * dot3(a, NormVec);
+      const double c = std::sqrt(kappa * B[PRES] / B[DENS]);
+      const double Rplus = -B[VEL1] - 2. * c / (kappa - 1.);
+      const double tmp1 = A * A + 2. / (kappa - 1.);
+      const double tmp2 = 2 * Rplus;
+      const double tmp3 = (kappa - 1.) / 2. * (Rplus * Rplus) - kappa * R * Tt * (A * A);
+      const double cb = std::max((-tmp2 + std::sqrt(tmp2 * tmp2 - 4 * tmp1 * tmp3)) / (2 * tmp1),
+                                 (-tmp2 - std::sqrt(tmp2 * tmp2 - 4 * tmp1 * tmp3)) / (2 * tmp1));
+      const double Tb = cb * cb / (kappa * R);
+      const double Ma = std::sqrt(2. / (kappa - 1.) * (Tt / Tb - 1.));
+      const double pb = pt * std::pow(1. + 0.5 * (kappa - 1.) * (Ma * Ma), -kappa / (kappa - 1.));
+      const double U = Ma * std::sqrt(kappa * R * Tb);
+      B[DENS] = pb / (R * Tb);
+      B[VEL1] = U * dot3(a, NormVec);
+      B[VEL2] = U * dot3(a, TangVec1);
+      B[VEL3] = U * dot3(a, TangVec2);
+      B[PRES] = pb;
+      B[TEMP] = Tb;
+      break;
+    }
+  }
+  UPrim_Out[DENS] = B[DENS];
+  for (int d = 0; d < 3; ++d) UPrim_Out[VEL1 + d] = B[VEL1] * NormVec[d] + B[VEL2] * TangVec1[d] + B[VEL3] * TangVec2[d];
+  UPrim_Out[PRES] = B[PRES];
+  UPrim_Out[TEMP] = B[TEMP];
+}
+
+// PrimToCons  idealgas/eos.f90:467-489
+static void PrimToCons(const double* prim, double* cons, double Kappa) {
+  cons[DENS] = prim[DENS];
+  cons[MOM1] = prim[VEL1] * prim[DENS];
+  cons[MOM2] = prim[VEL2] * prim[DENS];
+  cons[MOM3] = prim[VEL3] * prim[DENS];
+  cons[ENER] = prim[PRES] / (Kappa - 1.) + 0.5 * (cons[MOM1] * prim[VEL1] + cons[MOM2] * prim[VEL2] + cons[MOM3] * prim[VEL3]);
+}
+
+// EvalDiffFlux3D  flux.f90:702-760
+static void EvalDiffFlux3D(const double* P, const double* gx, const double* gy, const double* gz, double* f, double* g,
+                           double* h, double mu, double lambda) {
+  const double s23 = 2. / 3., s43 = 4. / 3.;
+  const double tau_xx = mu * (s43 * gx[1] - s23 * gy[2] - s23 * gz[3]);
+  const double tau_yy = mu * (-s23 * gx[1] + s43 * gy[2] - s23 * gz[3]);
+  const double tau_zz = mu * (-s23 * gx[1] - s23 * gy[2] + s43 * gz[3]);
+  const double tau_xy = mu * (gy[1] + gx[2]);
+  const double tau_xz = mu * (gz[1] + gx[3]);
+  const double tau_yz = mu * (gz[2] + gy[3]);
+  f[DENS] = 0.; f[MOM1] = -tau_xx; f[MOM2] = -tau_xy; f[MOM3] = -tau_xz;
+  f[ENER] = -tau_xx * P[VEL1] - tau_xy * P[VEL2] - tau_xz * P[VEL3] - lambda * gx[4];
+  g[DENS] = 0.; g[MOM1] = -tau_xy; g[MOM2] = -tau_yy; g[MOM3] = -tau_yz;
+  g[ENER] = -tau_xy * P[VEL1] - tau_yy * P[VEL2] - tau_yz * P[VEL3] - lambda * gy[4];
+  h[DENS] = 0.; h[MOM1] = -tau_xz; h[MOM2] = -tau_yz; h[MOM3] = -tau_zz;
+  h[ENER] = -tau_xz * P[VEL1] - tau_yz * P[VEL2] - tau_zz * P[VEL3] - lambda * gz[4];
+}
+
+// GetBoundaryFlux_GPU  getboundaryflux.f90:542-838, one face point; Flux before the SurfElem factor
+static void GetBoundaryFlux(const Ctx& C, const double* UPrim_master, const double* gx, const double* gy,
+                            const double* gz, const double* nv, const double* t1, const double* t2, int BCType,
+                            const double* RefStatePrim, double* Flux) {
+  const dg_config& cfg = C.cfg;
+  const double Kappa = cfg.kappa, mu = cfg.mu0, lambda = cfg.mu0 * cfg.R * cfg.kappa / ((cfg.kappa - 1.) * cfg.Pr);
+  double UPrim_boundary[6];
+  GetBoundaryState(BCType, UPrim_boundary, UPrim_master, RefStatePrim, nv, t1, t2, Kappa, cfg.R);
+  if (BCType == 2 || BCType == 23 || BCType == 24 || BCType == 25 || BCType == 27) {
+    double UCons_master[5], UCons_boundary[5];
+    PrimToCons(UPrim_master, UCons_master, Kappa);
+    PrimToCons(UPrim_boundary, UCons_boundary, Kappa);
+    Riemann(cfg, Flux, UCons_master, UCons_boundary, UPrim_master, UPrim_boundary, nv, t1, t2);
+    if (cfg.parabolic) {
+      // ViscousFlux  riemann.f90:489-546 with the master gradients on both sides
+      double fL[5], gL[5], hL[5], fR[5], gR[5], hR[5];
+      EvalDiffFlux3D(UPrim_master, gx, gy, gz, fL, gL, hL, mu, lambda);
+      EvalDiffFlux3D(UPrim_boundary, gx, gy, gz, fR, gR, hR, mu, lambda);
+      for (int v = 0; v < 5; ++v)
+        Flux[v] = Flux[v] + 0.5 * (nv[0] * (fL[v] + fR[v]) + nv[1] * (gL[v] + gR[v]) + nv[2] * (hL[v] + hR[v]));
+    }
+    return;
+  }
+  // walls: F = (0, p n, 0)
+  Flux[DENS] = 0.;
+  for (int d = 0; d < 3; ++d) Flux[MOM1 + d] = UPrim_boundary[PRES] * nv[d];
+  Flux[ENER] = 0.;
+  if (!cfg.parabolic) return;
+  double Fd[5], Gd[5], Hd[5];
+  if (BCType == 3 || BCType == 4) {
+    EvalDiffFlux3D(UPrim_boundary, gx, gy, gz, Fd, Gd, Hd, mu, lambda);
+    if (BCType == 3) { Fd[ENER] = 0.; Gd[ENER] = 0.; Hd[ENER] = 0.; }
+  } else if (BCType == 9) {
+    // BCGradMat = I - n n^T applied to all gradients
+    double M[3][3];
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) M[a][b] = (a == b ? 1. : 0.) - nv[a] * nv[b];
+    M[1][0] = M[0][1]; M[2][0] = M[0][2]; M[1][2] = M[2][1];
+    double fx[5], fy[5], fz[5];
+    for (int v = 0; v < 5; ++v) {
+      fx[v] = M[0][0] * gx[v] + M[0][1] * gy[v] + M[0][2] * gz[v];
+      fy[v] = M[1][0] * gx[v] + M[1][1] * gy[v] + M[1][2] * gz[v];
+      fz[v] = M[2][0] * gx[v] + M[2][1] * gy[v] + M[2][2] * gz[v];
+    }
+    EvalDiffFlux3D(UPrim_boundary, fx, fy, fz, Fd, Gd, Hd, mu, lambda);
+  } else {  // 91
+    double M[3][3];
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) M[a][b] = (a == b ? 1. : 0.) - nv[a] * nv[b];
+    M[1][0] = M[0][1]; M[2][0] = M[0][2]; M[1][2] = M[2][1];
+    const double* G[3] = {gx, gy, gz};
+    double fl[3][5] = {{0}};  // the density gradient is not used by EvalDiffFlux3D
+    for (int d = 0; d < 3; ++d) fl[d][4] = M[d][0] * gx[4] + M[d][1] * gy[4] + M[d][2] * gz[4];
+    // gradients of the wall-aligned velocities
+    double vN[3], vT1[3], vT2[3];
+    for (int d = 0; d < 3; ++d) {
+      vN[d] = nv[0] * G[d][1] + nv[1] * G[d][2] + nv[2] * G[d][3];
+      vT1[d] = t1[0] * G[d][1] + t1[1] * G[d][2] + t1[2] * G[d][3];
+      vT2[d] = t2[0] * G[d][1] + t2[1] * G[d][2] + t2[2] * G[d][3];
+    }
+    // derivatives along n, t1, t2; normal-tangential couplings set to zero
+    const double n_vN = nv[0] * vN[0] + nv[1] * vN[1] + nv[2] * vN[2];
+    const double n_vT1 = 0., n_vT2 = 0., t1_vN = 0., t2_vN = 0.;
+    const double t1_vT1 = t1[0] * vT1[0] + t1[1] * vT1[1] + t1[2] * vT1[2];
+    const double t1_vT2 = t1[0] * vT2[0] + t1[1] * vT2[1] + t1[2] * vT2[2];
+    const double t2_vT1 = t2[0] * vT1[0] + t2[1] * vT1[1] + t2[2] * vT1[2];
+    const double t2_vT2 = t2[0] * vT2[0] + t2[1] * vT2[1] + t2[2] * vT2[2];
+    double xN[3], xT1[3], xT2[3];
+    for (int d = 0; d < 3; ++d) {
+      xN[d] = nv[d] * n_vN + t1[d] * t1_vN + t2[d] * t2_vN;
+      xT1[d] = nv[d] * n_vT1 + t1[d] * t1_vT1 + t2[d] * t2_vT1;
+      xT2[d] = nv[d] * n_vT2 + t1[d] * t1_vT2 + t2[d] * t2_vT2;
+    }
+    for (int d = 0; d < 3; ++d)
+      for (int c = 0; c < 3; ++c) fl[d][1 + c] = nv[c] * xN[d] + t1[c] * xT1[d] + t2[c] * xT2[d];
+    EvalDiffFlux3D(UPrim_boundary, fl[0], fl[1], fl[2], Fd, Gd, Hd, mu, lambda);
+  }
+  for (int v = 0; v < 5; ++v) Flux[v] = Flux[v] + nv[0] * Fd[v] + nv[1] * Gd[v] + nv[2] * Hd[v];
+}
+
+// Lifting_GetBoundaryFlux_Kernel  getboundaryflux.f90:945-1019, one face point, SurfElem included
+static void Lifting_GetBoundaryFlux(const Ctx& C, const double* UPrim_master, const double* nv, const double* t1,
+                                    const double* t2, double SurfElem, int BCType, const double* RefStatePrim,
+                                    bool doWeakLifting, double* Flux) {
+  double UPrim_boundary[6], Flux_loc[5];
+  GetBoundaryState(BCType, UPrim_boundary, UPrim_master, RefStatePrim, nv, t1, t2, C.cfg.kappa, C.cfg.R);
+  if (BCType == 2 || BCType == 23 || BCType == 24 || BCType == 25 || BCType == 27) {
+    for (int iv = 0; iv < 5; ++iv) Flux_loc[iv] = 0.5 * (UPrim_master[PRIM_LIFT[iv]] + UPrim_boundary[PRIM_LIFT[iv]]);
+  } else if (BCType == 3 || BCType == 4) {
+    Flux_loc[0] = UPrim_boundary[DENS];
+    Flux_loc[1] = 0.; Flux_loc[2] = 0.; Flux_loc[3] = 0.;
+    Flux_loc[4] = UPrim_boundary[TEMP];
+  } else {  // 9, 91
+    Flux_loc[0] = UPrim_master[DENS];
+    for (int d = 0; d < 3; ++d) Flux_loc[1 + d] = UPrim_boundary[VEL1 + d];
+    Flux_loc[4] = UPrim_master[TEMP];
+  }
+  if (!doWeakLifting)
+    for (int iv = 0; iv < 5; ++iv) Flux_loc[iv] = Flux_loc[iv] - UPrim_master[PRIM_LIFT[iv]];
+  for (int iv = 0; iv < 5; ++iv) Flux[iv] = Flux_loc[iv] * SurfElem;
+}
+
+// ---------------------------------------------------------------------------------------
 // Operator pieces
 // ---------------------------------------------------------------------------------------
 // EvalElemFaceG/GL_Device (prolongtoface.t90:168-344): thread per (elem, locSide, p, q)
@@ -1059,18 +1315,28 @@ static void Lifting_VolInt(const Ctx& C, Work& W, bool weak) {
   }
 }
 
-// Lifting_BR1  src/dg/lifting/lifting_br1.t90:47-167 (no BC sides, no MPI)
+// Lifting_BR1  src/dg/lifting/lifting_br1.t90:47-167 (no MPI)
 static void Lifting_BR1(const Ctx& C, Work& W) {
   const int N = C.B.N, n = C.n;
   const size_t nF = (size_t)C.n2 * C.M.nSides;
   const bool weak = C.cfg.do_weak_lifting != 0;
-  // Lifting_FillFlux  lifting_fillflux.t90:39-103
+  // Lifting_FillFlux_BC (lifting_fillflux.t90:109-140) on the BC sides, Lifting_FillFlux
+  // (lifting_fillflux.t90:39-103) on the inner sides
   double sig = weak ? 1. : -1.;
+  const long long nFbc = (long long)C.n2 * C.nBCSides;
 #pragma omp parallel for schedule(static)
-  for (long long fidx = 0; fidx < (long long)nF; ++fidx)
+  for (long long fidx = 0; fidx < (long long)nF; ++fidx) {
+    if (fidx < nFbc) {
+      const int s = (int)(fidx / C.n2);
+      Lifting_GetBoundaryFlux(C, &W.UPrim_master[6 * fidx], &C.M.nv[3 * fidx], &C.M.t1[3 * fidx], &C.M.t2[3 * fidx],
+                              C.M.SurfElem[fidx], C.bctype[s], &C.refprim[6 * C.bcstate[s]], weak,
+                              &W.liftflux[5 * fidx]);
+      continue;
+    }
     for (int iv = 0; iv < 5; ++iv)
       W.liftflux[iv + 5 * fidx] = 0.5 * C.M.SurfElem[fidx] *
                                   (sig * W.UPrim_master[PRIM_LIFT[iv] + 6 * fidx] + W.UPrim_slave[PRIM_LIFT[iv] + 6 * fidx]);
+  }
   // Lifting_FillFlux_NormVec  lifting_fillflux.t90:212-256 (stored in gradU*_master)
 #pragma omp parallel for schedule(static)
   for (long long fidx = 0; fidx < (long long)nF; ++fidx)
@@ -1092,23 +1358,34 @@ static void Lifting_BR1(const Ctx& C, Work& W) {
   (void)n;
 }
 
-// Lifting_BR2 + Lifting_SurfInt_BR2  src/dg/lifting/lifting_br2.t90:43-310 (always strong form; no BC
-// sides, no MPI, no mortars).  The volume gradient gets the same surface lifting as BR1; the face
+// Lifting_BR2 + Lifting_SurfInt_BR2  src/dg/lifting/lifting_br2.t90:43-310 (always strong form; no MPI,
+// no mortars).  The volume gradient gets the same surface lifting as BR1; the face
 // traces are the prolonged volume-only gradient plus etaBR2 times the lifting of that face's own jump.
 static void Lifting_BR2(const Ctx& C, Work& W) {
   const int N = C.B.N;
   const size_t nF = (size_t)C.n2 * C.M.nSides, nDOF = (size_t)C.n3 * C.M.nElems;
   const bool gauss = C.B.node_type == DG_NODETYPE_GAUSS;
-  // Lifting_FillFlux (strong: 0.5*SurfElem*(U_slave - U_master)) and the normal components
+  // Lifting_FillFlux (strong: 0.5*SurfElem*(U_slave - U_master); BC sides: the strong boundary
+  // lifting flux of Lifting_GetBoundaryFlux) and the normal components
   std::vector<double> FX(5 * nF), FY(5 * nF), FZ(5 * nF);
+  const long long nFbc = (long long)C.n2 * C.nBCSides;
 #pragma omp parallel for schedule(static)
-  for (long long f = 0; f < (long long)nF; ++f)
+  for (long long f = 0; f < (long long)nF; ++f) {
+    double bfl[5];
+    if (f < nFbc) {
+      const int s = (int)(f / C.n2);
+      Lifting_GetBoundaryFlux(C, &W.UPrim_master[6 * f], &C.M.nv[3 * f], &C.M.t1[3 * f], &C.M.t2[3 * f],
+                              C.M.SurfElem[f], C.bctype[s], &C.refprim[6 * C.bcstate[s]], false, bfl);
+    }
     for (int iv = 0; iv < 5; ++iv) {
-      const double fl = 0.5 * C.M.SurfElem[f] * (-1. * W.UPrim_master[PRIM_LIFT[iv] + 6 * f] + W.UPrim_slave[PRIM_LIFT[iv] + 6 * f]);
+      const double fl = f < nFbc ? bfl[iv]
+                                 : 0.5 * C.M.SurfElem[f] * (-1. * W.UPrim_master[PRIM_LIFT[iv] + 6 * f] +
+                                                            W.UPrim_slave[PRIM_LIFT[iv] + 6 * f]);
       FX[iv + 5 * f] = fl * C.M.nv[0 + 3 * f];
       FY[iv + 5 * f] = fl * C.M.nv[1 + 3 * f];
       FZ[iv + 5 * f] = fl * C.M.nv[2 + 3 * f];
     }
+  }
   Lifting_VolInt(C, W, false);
   // ApplyJacobianLifting
 #pragma omp parallel for schedule(static)
@@ -1192,10 +1469,12 @@ static void DGTimeDerivative(const Ctx& C, Work& W, const double* U, double* Ut)
 #pragma omp parallel for schedule(static)
   for (long long id = 0; id < (long long)nDOF; ++id) ConsToPrim(&W.UPrim[6 * id], &U[5 * id], Kappa, R);
   // 5. GetPrimitiveStateSurface (version 1: prims of prolonged conservative traces)
+  // (BC sides, the first nBCSides, have no slave element)
+  const long long nFbc = (long long)C.n2 * C.nBCSides;
 #pragma omp parallel for schedule(static)
   for (long long f = 0; f < (long long)nF; ++f) {
     ConsToPrim(&W.UPrim_master[6 * f], &W.U_master[5 * f], Kappa, R);
-    ConsToPrim(&W.UPrim_slave[6 * f], &W.U_slave[5 * f], Kappa, R);
+    if (f >= nFbc) ConsToPrim(&W.UPrim_slave[6 * f], &W.U_slave[5 * f], Kappa, R);
   }
   // 6. Lifting
   if (cfg.parabolic) {
@@ -1255,10 +1534,24 @@ static void DGTimeDerivative(const Ctx& C, Work& W, const double* U, double* Ut)
         for (int v = 0; v < 5; ++v) Ut[v + 5 * id] = cfg.parabolic ? Ut[v + 5 * id] + tmp[v] : tmp[v];
       }
   }
-  // 11. FillFlux  fillflux.f90:45-172 (inner sides): Riemann, viscous flux, SurfElem, copy to slave
+  // 11. FillFlux  fillflux.f90:45-172: BC sides (GetBoundaryFlux), inner sides (Riemann, viscous
+  // flux), then SurfElem and the copy to the slave side
 #pragma omp parallel for schedule(static)
   for (long long f = 0; f < (long long)nF; ++f) {
     double* Fm = &W.Flux_master[5 * f];
+    if (f < nFbc) {
+      const int s = (int)(f / C.n2);
+      const double* gx = cfg.parabolic ? &W.gx_m[5 * f] : nullptr;
+      const double* gy = cfg.parabolic ? &W.gy_m[5 * f] : nullptr;
+      const double* gz = cfg.parabolic ? &W.gz_m[5 * f] : nullptr;
+      GetBoundaryFlux(C, &W.UPrim_master[6 * f], gx, gy, gz, &C.M.nv[3 * f], &C.M.t1[3 * f], &C.M.t2[3 * f],
+                      C.bctype[s], &C.refprim[6 * C.bcstate[s]], Fm);
+      for (int v = 0; v < 5; ++v) {
+        Fm[v] = Fm[v] * C.M.SurfElem[f];
+        W.Flux_slave[v + 5 * f] = Fm[v];
+      }
+      continue;
+    }
     Riemann(cfg, Fm, &W.U_master[5 * f], &W.U_slave[5 * f], &W.UPrim_master[6 * f], &W.UPrim_slave[6 * f],
             &C.M.nv[3 * f], &C.M.t1[3 * f], &C.M.t2[3 * f]);
     if (cfg.parabolic) {
@@ -1540,6 +1833,43 @@ orc_handle* orc_create(const dg_config* cfg, int nElems, int nSides, const doubl
 }
 
 void orc_destroy(orc_handle* h) { delete h; }
+
+// Boundary conditions of the first nBCSides sides: BC type and 1-based RefState index per side, RefState
+// rows (rho, u, v, w, p) as in the parameter file.  RefStatePrim(TEMP) as InitEquation
+// (equation.f90:136-147); type 27 states (Tt, alpha, beta, -, pt) turned into the inflow direction as
+// InitBC (getboundaryflux.f90:199-208).
+int orc_set_boundaries(orc_handle* h, int nBCSides, const int* bc_type, const int* bc_state, int nRefState,
+                       const double* refstate) {
+  Ctx& C = h->C;
+  C.nBCSides = nBCSides;
+  C.bctype.assign(bc_type, bc_type + nBCSides);
+  C.bcstate.resize(nBCSides);
+  C.refprim.assign((size_t)6 * std::max(1, nRefState), 0.);
+  for (int r = 0; r < nRefState; ++r) {
+    for (int c = 0; c < 5; ++c) C.refprim[6 * r + c] = refstate[5 * r + c];
+    C.refprim[6 * r + TEMP] = C.refprim[6 * r + PRES] * (1. / C.refprim[6 * r + DENS]) / C.cfg.R;
+  }
+  std::vector<char> done(std::max(1, nRefState), 0);
+  for (int s = 0; s < nBCSides; ++s) {
+    const int t = bc_type[s];
+    if (t != 2 && t != 3 && t != 4 && t != 9 && t != 91 && t != 23 && t != 24 && t != 25 && t != 27) return -1;
+    int st = bc_state[s] - 1;
+    if (st < 0 || st >= nRefState) {
+      if (t != 3 && t != 9 && t != 91) return -2;
+      st = 0;
+    }
+    C.bcstate[s] = st;
+    if (t == 27 && !done[st]) {
+      done[st] = 1;
+      double* q = &C.refprim[6 * st];
+      const double talpha = std::tan(PP_Pi / 180. * q[1]), tbeta = std::tan(PP_Pi / 180. * q[2]);
+      q[VEL1] = 1. / std::sqrt((1. + talpha * talpha + tbeta * tbeta));
+      q[VEL2] = talpha / std::sqrt((1. + talpha * talpha + tbeta * tbeta));
+      q[VEL3] = tbeta / std::sqrt((1. + talpha * talpha + tbeta * tbeta));
+    }
+  }
+  return 0;
+}
 
 int orc_rhs(orc_handle* h, const double* U, double* Ut) {
   DGTimeDerivative(h->C, h->W, U, Ut);

@@ -34,6 +34,7 @@ def lib():
         L.orc_create.restype = _P
         L.orc_create.argtypes = [_P, ctypes.c_int, ctypes.c_int] + [_P] * 10
         L.orc_destroy.argtypes = [_P]
+        L.orc_set_boundaries.argtypes = [_P, ctypes.c_int, _P, _P, ctypes.c_int, _P]
         L.orc_rhs.argtypes = [_P, _P, _P]
         L.orc_get_work.argtypes = [_P, ctypes.c_int, _P]
         L.orc_lserk_steps.argtypes = [_P, ctypes.c_double, ctypes.c_double, ctypes.c_int, _P, _P]
@@ -82,12 +83,24 @@ def s2v2(N):
 class Oracle:
     """CPU restatement of DGTimeDerivative_weakForm / TimeStepByLSERKW2 on one mesh."""
 
-    def __init__(self, cfg, mesh):
+    def __init__(self, cfg, mesh, boundaries=None):
+        """boundaries: (bc_type, bc_state, refstates) of the mesh's BC sides, as for the DG operator."""
         self.cfg, self.mesh = cfg, mesh
         m = mesh
         self._keep = [m.Metrics_fTilde, m.Metrics_gTilde, m.Metrics_hTilde, m.sJ, m.NormVec, m.TangVec1, m.TangVec2,
                       m.SurfElem, m.ElemToSide, m.SideToElem]
         self._h = lib().orc_create(ctypes.byref(cfg), m.nElems, m.nSides, *[_p(a) for a in self._keep])
+        nb = getattr(m, "nBCSides", 0)
+        if nb:
+            if boundaries is None:
+                raise ValueError("mesh has BC sides: pass boundaries=(bc_type, bc_state, refstates)")
+            bt, bs, rs = boundaries
+            bt = np.ascontiguousarray(bt, dtype=np.int32)
+            bs = np.ascontiguousarray(bs, dtype=np.int32)
+            rs = np.ascontiguousarray(rs, dtype=np.float64).reshape(-1, 5)
+            rc = lib().orc_set_boundaries(self._h, nb, _p(bt), _p(bs), rs.shape[0], _p(rs))
+            if rc != 0:
+                raise ValueError(f"orc_set_boundaries failed ({rc})")
 
     def close(self):
         if self._h:

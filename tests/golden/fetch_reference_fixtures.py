@@ -17,6 +17,14 @@ tree is absent:
                                Taylor-Green vortex analysis of the split-form regression run
                                (regressioncheck/checks/tgv/split/), one row every 10 time steps
   CART_HEX_PERIODIC_008_mesh.h5  the HOPR mesh of that run (8^3 periodic hexahedra on [0,2pi]^3)
+  cavity4x4x4_mesh.h5          the lid-driven cavity regression (regressioncheck/checks/parabolic/
+                               cavity_3D/): 4^3 elements, isothermal walls and a Dirichlet lid
+  reggie_cavity_Re100_State_0000001.000000000.h5
+                               that regression's reference state at t = 1 (DG_Solution, N = 2)
+  CART_HEX2D_FlatPlateG_mesh.h5  flat-plate tutorial mesh (tutorials/flatPlate/meshes/): Dirichlet,
+                               pressure-outflow, adiabatic-wall and slip-wall sides
+  NACA0012_652_Ng2_mesh.h5     curved (NGeo = 2) airfoil mesh of regressioncheck/checks/naca/3D/:
+                               adiabatic wall, far-field and periodic sides
 
 Usage:  python tests/golden/fetch_reference_fixtures.py [/path/to/reference]
 """
@@ -40,6 +48,10 @@ FILES = [
 REGRESSION = [
     ("regressioncheck/checks/tgv/split", "TGV_Re1600_Split_TGVAnalysis_Reference.csv"),
     ("regressioncheck/checks/tgv/split", "CART_HEX_PERIODIC_008_mesh.h5"),
+    ("regressioncheck/checks/parabolic/cavity_3D", "cavity4x4x4_mesh.h5"),
+    ("regressioncheck/checks/parabolic/cavity_3D", "reggie_cavity_Re100_State_0000001.000000000.h5"),
+    ("tutorials/flatPlate/meshes", "CART_HEX2D_FlatPlateG_mesh.h5"),
+    ("regressioncheck/checks/naca/3D", "NACA0012_652_Ng2_mesh.h5"),
 ]
 
 
