@@ -46,6 +46,10 @@ class DGConfig(ctypes.Structure):
         ("Pr", ctypes.c_double),
         ("mu0", ctypes.c_double),
         ("precision", ctypes.c_int),
+        ("filter_type", ctypes.c_int),
+        ("n_filter", ctypes.c_int),
+        ("hest_filter_param", ctypes.c_double * 3),
+        ("laf_alpha", ctypes.c_double),
     ]
 
 
@@ -77,6 +81,7 @@ _SIGS = {
     "dg_kernel_launch_count": (ctypes.c_longlong, [_P]),
     "dg_get_gradients": (_I, [_P, _P, _P, _P, _P]),
     "dg_set_boundaries": (_I, [_P, _P, _P, _I, _P]),
+    "dg_laf_state": (_I, [_P, _P, _P, _P]),
     "dg_mesh_hopr_sizes": (_I, [ctypes.c_char_p, _IP, _IP, _IP, _IP]),
     "dg_mesh_hopr": (_I, [ctypes.c_char_p, _I, _I] + [_P] * 12),
     "dg_mesh_hopr_bcs": (_I, [ctypes.c_char_p, _IP, _P, _I, _P]),

@@ -272,6 +272,7 @@ int need_fp64(dg_ctx* ctx, const char* what) {
 int tlm_setup(dg_ctx* ctx) {
   if (int rc = need_fp64(ctx, "tangent-linear operator")) return rc;
   if (ctx->nBCSides) { set_error("tangent-linear operator: periodic meshes only"); return DG_ERR_UNSUPPORTED; }
+  if (ctx->cfg.filter_type) { set_error("tangent-linear operator: no solution filter"); return DG_ERR_UNSUPPORTED; }
   if (ctx->cfg.split_dg != DG_SPLIT_NONE && ctx->cfg.split_dg != DG_SPLIT_PI && ctx->cfg.split_dg != DG_SPLIT_KG) {
     set_error("tangent-linear operator: split forms PI and KG only"); return DG_ERR_UNSUPPORTED;
   }
@@ -296,6 +297,7 @@ int tlm_setup(dg_ctx* ctx) {
 int adj_setup(dg_ctx* ctx) {
   if (int rc = need_fp64(ctx, "adjoint")) return rc;
   if (ctx->nBCSides) { set_error("adjoint: periodic meshes only"); return DG_ERR_UNSUPPORTED; }
+  if (ctx->cfg.filter_type) { set_error("adjoint: no solution filter"); return DG_ERR_UNSUPPORTED; }
   const dg_config& c = ctx->cfg;
   if (c.split_dg != DG_SPLIT_NONE && c.split_dg != DG_SPLIT_PI && c.split_dg != DG_SPLIT_KG) {
     set_error("adjoint: split forms PI and KG only"); return DG_ERR_UNSUPPORTED;
@@ -414,6 +416,11 @@ int dg_ctx_create(const dg_config* cfg, dg_ctx** out) {
   if (!(cfg->kappa > 1.) || !(cfg->R > 0.)) { set_error("bad kappa or R"); return DG_ERR_ARG; }
   if (cfg->parabolic && !(cfg->Pr > 0.)) { set_error("bad Pr"); return DG_ERR_ARG; }
   if (cfg->precision != DG_PRECISION_FP64 && cfg->precision != DG_PRECISION_MIXED) { set_error("bad precision"); return DG_ERR_ARG; }
+  std::vector<double> fmat;
+  if (cfg->filter_type < DG_FILTER_NONE || cfg->filter_type > DG_FILTER_LAF) { set_error("unknown FilterType"); return DG_ERR_ARG; }
+  if (cfg->filter_type != DG_FILTER_NONE && gxh::filter_matrix(*cfg, fmat) != 0) {
+    set_error("filter: NFilter must be in 0..N (cut-off and LAF)"); return DG_ERR_ARG;
+  }
   dg_ctx* ctx = new dg_ctx();
   ctx->cfg = *cfg;
   ctx->N = cfg->N;
@@ -426,6 +433,16 @@ int dg_ctx_create(const dg_config* cfg, dg_ctx** out) {
   if (rc == DG_OK && cfg->precision == DG_PRECISION_MIXED) rc = upload_basis(ctx, ctx->f);
   if (rc == DG_OK) rc = (cfg->precision == DG_PRECISION_FP64) ? T->configure_d() : T->configure_f();
   if (rc == DG_OK && !(ctx->red.alloc(2) && ctx->bad.alloc(1))) { set_error("cudaMalloc"); rc = DG_ERR_ALLOC; }
+  if (rc == DG_OK && !fmat.empty()) {
+    if (!ctx->filt.alloc(fmat.size())) { set_error("cudaMalloc filter"); rc = DG_ERR_ALLOC; }
+    else if (cudaMemcpy(ctx->filt.p, fmat.data(), fmat.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+      set_error("upload FilterMat"); rc = DG_ERR_CUDA;
+    }
+    // normMod of the LAF filter (filter.f90:194)
+    const double Nf = (double)cfg->n_filter, Np = (double)cfg->N;
+    ctx->laf_norm = (std::pow(Nf + 1., -2. / 3.) - std::pow(2., -2. / 3.)) /
+                    (std::pow(Np + 1., -2. / 3.) - std::pow(Nf + 1., -2. / 3.));
+  }
   if (rc != DG_OK) { dg_ctx_destroy(ctx); return rc; }
   *out = ctx;
   return DG_OK;
@@ -444,6 +461,7 @@ int dg_ctx_destroy(dg_ctx* ctx) {
   ctx->t.release(); ctx->Ud.release(); ctx->Utd.release();
   ctx->UfB.release(); ctx->GfB.release(); ctx->JB.release(); ctx->UBv.release(); ctx->part.release();
   ctx->acc.release(); ctx->W.release(); ctx->K.release(); ctx->tape.store.release();
+  ctx->filt.release(); ctx->laf.release();
   delete ctx;
   return DG_OK;
 }
@@ -542,8 +560,39 @@ int dg_set_mesh(dg_ctx* ctx, int nElems, int nSides, int nBCSides, const double*
   ctx->t.release(); ctx->Ud.release(); ctx->Utd.release();
   ctx->UfB.release(); ctx->GfB.release(); ctx->JB.release(); ctx->UBv.release(); ctx->part.release();
   ctx->W.release(); ctx->K.release(); ctx->tape.store.release();
+  ctx->laf.release();
+  if (ctx->cfg.filter_type == DG_FILTER_LAF) {
+    // IntegrationWeight = w_i w_j w_k / sJ normalised by the element volume, and the initial state
+    // lim = 1e-8, eRatio = r = 0, previous energies 1e-16 (InitFilter, filter.f90:170-199)
+    const size_t nE = nElems;
+    std::vector<double> h(5 * nE + nE * n3);
+    for (size_t e = 0; e < nE; ++e) {
+      h[e] = 1e-8; h[nE + e] = 0.; h[2 * nE + e] = 0.; h[3 * nE + e] = 1e-16; h[4 * nE + e] = 1e-16;
+      double* iw = &h[5 * nE + e * n3];
+      double vol = 0.;
+      for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
+        const int node = i + n * (j + n * k);
+        iw[node] = ctx->B.w[i] * ctx->B.w[j] * ctx->B.w[k] / sJ[e * n3 + node];
+        vol = vol + iw[node];
+      }
+      for (int t = 0; t < n3; ++t) iw[t] = iw[t] / vol;
+    }
+    if (!ctx->laf.alloc(h.size())) { set_error("cudaMalloc LAF state"); return DG_ERR_ALLOC; }
+    CUDA_TRY(cudaMemcpy(ctx->laf.p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice), "upload LAF state");
+  }
   ctx->mesh_ok = true;
   ctx->grad_ok = false;
+  return DG_OK;
+}
+
+int dg_laf_state(dg_ctx* ctx, double* lim, double* eRatio, double* r) {
+  if (int rc = check_ctx(ctx, true)) return rc;
+  if (ctx->cfg.filter_type != DG_FILTER_LAF || !ctx->laf.p) { set_error("dg_laf_state: FilterType is not LAF"); return DG_ERR_ARG; }
+  const size_t nE = ctx->nElems;
+  CUDA_TRY(cudaDeviceSynchronize(), "LAF state");
+  if (lim) CUDA_TRY(cudaMemcpy(lim, ctx->laf.p, nE * sizeof(double), cudaMemcpyDeviceToHost), "LAF lim");
+  if (eRatio) CUDA_TRY(cudaMemcpy(eRatio, ctx->laf.p + nE, nE * sizeof(double), cudaMemcpyDeviceToHost), "LAF eRatio");
+  if (r) CUDA_TRY(cudaMemcpy(r, ctx->laf.p + 2 * nE, nE * sizeof(double), cudaMemcpyDeviceToHost), "LAF r");
   return DG_OK;
 }
 
@@ -596,7 +645,7 @@ int dg_set_boundaries(dg_ctx* ctx, const int* bc_type, const int* bc_state, int 
   return DG_OK;
 }
 
-int dg_rhs(dg_ctx* ctx, double t, const double* d_U, double* d_Ut, void* stream) {
+int dg_rhs(dg_ctx* ctx, double t, double* d_U, double* d_Ut, void* stream) {
   if (int rc = check_ctx(ctx, true)) return rc;
   if (!d_U || !d_Ut) { set_error("dg_rhs: null state"); return DG_ERR_ARG; }
   (void)t;  // periodic meshes: no time-dependent boundary states or sources

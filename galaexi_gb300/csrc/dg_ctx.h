@@ -112,6 +112,10 @@ struct dg_ctx {
   bool mesh_ok = false;
   bool grad_ok = false;    // Gvol holds the lifted gradients of the last RHS evaluation
   double pref = 0.;       // reference pressure of the mixed form (dg_set_pressure_offset)
+  // solution filter (FilterType > 0): FilterMat (n x n); LAF: per-element state [5][nElems] followed
+  // by the normalised integration weights [e][n3], and normMod
+  gxc::DBuf<double> filt, laf;
+  double laf_norm = 0.;
 };
 
 namespace gxc {

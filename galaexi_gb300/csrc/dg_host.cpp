@@ -173,6 +173,61 @@ void basis_1d(int N, int node_type, Basis1D& B) {
   for (int i = 0; i < n; ++i) { B.Lhm[i] = (1. / B.w[i]) * B.Lm[i]; B.Lhp[i] = (1. / B.w[i]) * B.Lp[i]; }
 }
 
+// FilterMat of InitFilter (filter.f90:100-222): Vdm_Leg diag(sigma) sVdm_Leg with the modal
+// Vandermonde of the normalised Legendre polynomials (buildLegendreVdm, basis.f90:100-160); its
+// inverse by Gauss quadrature of the interpolant (the reference's VDM_ANALYTICAL branch, exact for
+// N+1 Gauss points).  sigma: cut-off (1 up to NFilter) or Hesthaven's exponential filter (HestFilter,
+// filter.f90:231-263).  F(i,l) column-major.
+int filter_matrix(const dg_config& c, std::vector<double>& F) {
+  const int N = c.N, n = N + 1;
+  std::vector<double> sigma(n, 0.);
+  if (c.filter_type == DG_FILTER_CUTOFF || c.filter_type == DG_FILTER_LAF) {
+    if (c.n_filter < 0 || c.n_filter > N) return -1;
+    for (int d = 0; d <= c.n_filter; ++d) sigma[d] = 1.;
+  } else if (c.filter_type == DG_FILTER_MODAL) {
+    const double alpha = c.hest_filter_param[0], s = c.hest_filter_param[1];
+    const double etac = c.hest_filter_param[2] / (double)(N + 1);
+    const int cut = (int)c.hest_filter_param[2];
+    for (int d = 0; d <= std::min(cut - 1, N); ++d) sigma[d] = 1.;
+    if (alpha >= 0.)
+      for (int d = std::max(cut, 0); d <= N; ++d) {
+        const double eta = (double)(d + 1) / (double)(N + 1);
+        sigma[d] = std::exp(-alpha * std::pow((eta - etac) / (1. - etac), s));
+      }
+  } else {
+    return -1;
+  }
+  Basis1D B, G;
+  basis_1d(N, c.node_type, B);
+  basis_1d(N, DG_NODETYPE_GAUSS, G);
+  std::vector<double> V(n * n), sV(n * n, 0.), Vlag;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      double L, dL;
+      legendre(j, B.x[i], L, dL);
+      V[i + n * j] = L;  // Vdm_Leg(i,j) = L_j(x_i)
+    }
+  vandermonde(N, B.x.data(), B.wb.data(), N, G.x.data(), Vlag);  // Vlag(g,i) = l_i(xGauss_g)
+  for (int m = 0; m < n; ++m)
+    for (int i = 0; i < n; ++i) {
+      double acc = 0.;
+      for (int g = 0; g < n; ++g) {
+        double L, dL;
+        legendre(m, G.x[g], L, dL);
+        acc += L * G.w[g] * Vlag[g + n * i];
+      }
+      sV[m + n * i] = acc;  // sVdm_Leg(m,i)
+    }
+  F.assign(n * n, 0.);
+  for (int i = 0; i < n; ++i)
+    for (int l = 0; l < n; ++l) {
+      double acc = 0.;
+      for (int m = 0; m < n; ++m) acc += V[i + n * m] * sigma[m] * sV[m + n * l];
+      F[i + n * l] = acc;
+    }
+  return 0;
+}
+
 // interpolation matrix V(i,j) = l_j(y_i) from nodes x (degree N) to points y (m+1 points)
 void vandermonde(int N, const double* x, const double* wb, int M, const double* y, std::vector<double>& V) {
   V.assign((size_t)(M + 1) * (N + 1), 0.);
@@ -211,6 +266,31 @@ extern "C" void dg_config_default(dg_config* c) {
   c->Pr = 0.72;         // idealgas/eos.f90:88
   c->mu0 = 0.;          // idealgas/eos.f90:89
   c->precision = DG_PRECISION_FP64;
+  c->filter_type = DG_FILTER_NONE;  // filter.f90:78-79
+  c->n_filter = -1;                 // NFilter has no default (required for cut-off / LAF)
+  c->hest_filter_param[0] = 36.;    // filter.f90:143
+  c->hest_filter_param[1] = 12.;
+  c->hest_filter_param[2] = 1.;
+  c->laf_alpha = 1.;                // filter.f90:85
+}
+
+// "(/a, b, c/)" or "a, b, c" -> up to n doubles
+static int parse_real_array(const std::string& v, double* out, int n) {
+  std::string s;
+  for (char ch : v) s += (ch == '(' || ch == ')' || ch == '/' || ch == ',') ? ' ' : ch;
+  size_t pos = 0;
+  int k = 0;
+  while (k < n) {
+    size_t a = s.find_first_not_of(" \t", pos);
+    if (a == std::string::npos) break;
+    size_t b = s.find_first_of(" \t", a);
+    std::string tok = s.substr(a, b == std::string::npos ? std::string::npos : b - a);
+    for (auto& ch : tok) if (ch == 'd' || ch == 'D') ch = 'e';  // Fortran exponent
+    out[k++] = std::stod(tok);
+    if (b == std::string::npos) break;
+    pos = b;
+  }
+  return k;
 }
 
 static std::string lower(std::string s) {
@@ -279,7 +359,18 @@ extern "C" int dg_config_from_ini(const char* text, dg_config* cfg) {
       } else if (key == "doconservativelifting") {
         int b; if (!parse_bool(val, b)) { set_error("bad doConservativeLifting"); return DG_ERR_ARG; }
         cfg->do_conservative_lifting = b;
-      } else if (key == "precision") {
+      } else if (key == "filtertype") {
+        static const char* names[] = {"none", "cutoff", "modal", "laf"};
+        int found = -1;
+        for (int i = 0; i < 4; ++i) if (lv == names[i]) found = i;
+        if (found < 0 && !lv.empty() && std::isdigit((unsigned char)lv[0])) found = std::stoi(lv);
+        if (found < 0 || found > 3) { set_error("unknown FilterType " + val); return DG_ERR_ARG; }
+        cfg->filter_type = found;
+      } else if (key == "nfilter") cfg->n_filter = std::stoi(val);
+      else if (key == "hestfilterparam") {
+        if (parse_real_array(val, cfg->hest_filter_param, 3) != 3) { set_error("HestFilterParam needs 3 values"); return DG_ERR_ARG; }
+      } else if (key == "laf_alpha") cfg->laf_alpha = std::stod(val);
+      else if (key == "precision") {
         if (lv == "fp64" || lv == "double") cfg->precision = DG_PRECISION_FP64;
         else if (lv == "mixed") cfg->precision = DG_PRECISION_MIXED;
         else { set_error("unknown Precision " + val); return DG_ERR_ARG; }

@@ -3,6 +3,8 @@
 #include <string>
 #include <vector>
 
+#include "../../include/galaexi_gb300.h"
+
 namespace gxh {
 
 // 1D basis of degree N on one node set (column-major (0:N,0:N) matrices)
@@ -18,6 +20,8 @@ struct Basis1D {
 inline double D_at(const Basis1D& B, int i, int l) { return B.D[i + (B.N + 1) * l]; }
 
 void basis_1d(int N, int node_type, Basis1D& B);
+// FilterMat (0:N,0:N) of the configured filter type (column-major); -1 if the configuration is invalid
+int filter_matrix(const dg_config& c, std::vector<double>& F);
 void set_error(const std::string& s);
 
 // Lagrange interpolation matrix V(j,i) = l_i(y_j) from the N+1 nodes x (barycentric weights wb) to

@@ -2,6 +2,7 @@
 // with GX_NP defined, so the kernels of every degree compile in their own translation unit.
 #pragma once
 #include "dg_ctx.h"
+#include "dg_filter.cuh"
 
 #ifndef GX_NP
 #error "define GX_NP before including dg_np.cuh"
@@ -108,10 +109,23 @@ void rhs_front(dg_ctx* ctx, PrecData<R>& P, const S* U, const gx::Gas<R>& gas, c
   if (ev) cudaEventRecord(ev[3], st);
 }
 
+// step 1 of the operator: the solution filter, in place on the FP64 state (dg.f90:330)
+inline void filter(dg_ctx* ctx, double* U, cudaStream_t st) {
+  if (ctx->cfg.filter_type == DG_FILTER_LAF) {
+    gx::LafState S{ctx->laf.p, ctx->laf.p + 5 * (size_t)ctx->nElems, ctx->cfg.laf_alpha, ctx->laf_norm};
+    gx::k_filter_laf<NP><<<ctx->nElems, ((NP * NP * NP + 31) / 32) * 32, 0, st>>>(U, ctx->filt.p, ctx->nElems, S);
+  } else {
+    gx::k_filter<NP><<<(ctx->nElems + EPB - 1) / EPB, NT, 0, st>>>(U, ctx->filt.p, ctx->nElems);
+  }
+  ctx->launches++;
+}
+
 template <typename R>
 int rhs(dg_ctx* ctx, PrecData<R>& P, const double* U, gx::RKArgs rk, int rkmode, cudaStream_t st,
         cudaEvent_t* ev = nullptr) {
   if (ev) cudaEventRecord(ev[0], st);
+  // the reference filters its module array d_U in place; U is the caller's state array
+  if (ctx->cfg.filter_type != DG_FILTER_NONE) filter(ctx, const_cast<double*>(U), st);
   const gx::Gas<R> gas = gxc::make_gas<R>(ctx->cfg, ctx->cfg.precision == DG_PRECISION_MIXED ? ctx->pref : 0.);
   rhs_front<R>(ctx, P, U, gas, st, ev, true);
   int vrc = DG_OK;

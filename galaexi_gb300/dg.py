@@ -20,7 +20,7 @@ from . import _native as nat
 
 def config(N=3, NodeType="gauss-lobatto", Riemann="lf", SplitDG="none", parabolic=False, kappa=1.4, R=287.058,
            Pr=0.72, mu0=0.0, doWeakLifting=False, doConservativeLifting=False, etaBR2=2.0, precision="fp64",
-           Lifting="br1"):
+           Lifting="br1", FilterType="none", NFilter=None, HestFilterParam=None, LAF_alpha=None):
     """Build a dg_config from the reference's ini key names (see dg_config_from_ini)."""
     cfg = nat.DGConfig()
     nat.lib().dg_config_default(ctypes.byref(cfg))
@@ -29,7 +29,10 @@ def config(N=3, NodeType="gauss-lobatto", Riemann="lf", SplitDG="none", paraboli
         "Parabolic = %s" % ("T" if parabolic else "F"), "kappa = %r" % kappa, "R = %r" % R, "Pr = %r" % Pr,
         "mu0 = %r" % mu0, "doWeakLifting = %s" % ("T" if doWeakLifting else "F"),
         "doConservativeLifting = %s" % ("T" if doConservativeLifting else "F"), "etaBR2 = %r" % etaBR2,
-        "Precision = %s" % precision, "Lifting = %s" % Lifting])
+        "Precision = %s" % precision, "Lifting = %s" % Lifting, "FilterType = %s" % FilterType]
+        + (["NFilter = %d" % NFilter] if NFilter is not None else [])
+        + (["HestFilterParam = (/%r, %r, %r/)" % tuple(HestFilterParam)] if HestFilterParam is not None else [])
+        + (["LAF_alpha = %r" % LAF_alpha] if LAF_alpha is not None else []))
     nat.check(nat.lib().dg_config_from_ini(text.encode(), ctypes.byref(cfg)), "dg_config_from_ini")
     return cfg
 
@@ -379,6 +382,12 @@ class DG:
                                               ctypes.byref(J), _tp(G), ctypes.byref(mb), _tp(Uf),
                                               self._stream(stream)), "dg_adjoint_window")
         return J.value, G, mb.value, Uf
+
+    def laf_state(self):
+        """(lim, eRatio, r) per element of the LAF filter after the last operator call (dg_laf_state)."""
+        out = [np.zeros(self.mesh.nElems) for _ in range(3)]
+        nat.check(nat.lib().dg_laf_state(self._h, *[_ptr(a) for a in out]), "dg_laf_state")
+        return tuple(out)
 
     def gradients(self, stream=None):
         """Lifted gradients (GradUx, GradUy, GradUz) of the last RHS evaluation, each a float64 CUDA

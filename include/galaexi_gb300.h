@@ -89,7 +89,18 @@ typedef struct dg_config {
   double eta_br2;               /* etaBR2                                             */
   double kappa, R, Pr, mu0;     /* EOS_Vars (idealgas/eos.f90:191-203)                */
   int    precision;             /* DG_PRECISION_*                                     */
+  /* filter of the solution at the start of every operator call (filter.f90:100-311) */
+  int    filter_type;           /* DG_FILTER_* (FilterType)                           */
+  int    n_filter;              /* NFilter: highest kept mode (cut-off, LAF)          */
+  double hest_filter_param[3];  /* HestFilterParam (alpha, s, cut-off mode), modal    */
+  double laf_alpha;             /* LAF_alpha                                          */
 } dg_config;
+
+/* FilterType (filter.f90:40-43) */
+#define DG_FILTER_NONE   0
+#define DG_FILTER_CUTOFF 1
+#define DG_FILTER_MODAL  2
+#define DG_FILTER_LAF    3
 
 #define DG_MAX_N 9
 
@@ -103,7 +114,8 @@ void dg_config_default(dg_config* cfg);
 /* Parse ini text (key = value lines, '!' comments, case-insensitive keys and
  * string values) into *cfg, starting from the values already in *cfg.
  * Recognised keys: N, NodeType, Riemann, SplitDG, Lifting, Parabolic, kappa, R, Pr,
- * mu0, doWeakLifting, doConservativeLifting, etaBR2, Precision.  Replaces the
+ * mu0, doWeakLifting, doConservativeLifting, etaBR2, Precision, FilterType, NFilter,
+ * HestFilterParam, LAF_alpha.  Replaces the
  * GET* calls of src/readintools/readintools.f90:1021-1229 for these keys. */
 int dg_config_from_ini(const char* ini_text, dg_config* cfg);
 
@@ -137,8 +149,15 @@ int dg_set_mesh(dg_ctx* ctx, int nElems, int nSides, int nBCSides,
 int dg_set_boundaries(dg_ctx* ctx, const int* bc_type, const int* bc_state, int nRefState, const double* refstate);
 
 /* Ut = DGTimeDerivative_weakForm(U) at time t (src/dg/dg.f90:255-425).
- * d_U, d_Ut: device FP64 arrays (5,0:N,0:N,0:N,nElems); stream: cudaStream_t or NULL. */
-int dg_rhs(dg_ctx* ctx, double t, const double* d_U, double* d_Ut, void* stream);
+ * d_U, d_Ut: device FP64 arrays (5,0:N,0:N,0:N,nElems); stream: cudaStream_t or NULL.
+ * With a filter configured (FilterType > 0) d_U is first filtered in place, as the reference's
+ * step 1 does (dg.f90:330); otherwise it is only read. */
+int dg_rhs(dg_ctx* ctx, double t, double* d_U, double* d_Ut, void* stream);
+
+/* Per-element state of the LAF filter after the last operator call (Filter_LAF,
+ * filter.f90:318-474; written as element data LAF_lim, LAF_eRatio, LAF_r by the reference):
+ * host arrays of nElems values, any may be NULL.  DG_ERR_ARG unless FilterType is LAF. */
+int dg_laf_state(dg_ctx* ctx, double* lim, double* eRatio, double* r);
 
 /* One Carpenter-Kennedy RK4-5 low-storage step (TimeStepByLSERKW2,
  * timestep.f90:49-120, coefficients timedisc_vars.f90:213-227), updating

@@ -305,6 +305,9 @@ struct Ctx {
   int s2v2_inv(int c, int a, int b, int flip, int locSide) const {
     return S2V2_inv[c + 2 * (a + n * (b + n * (flip + 5 * (locSide - 1))))];
   }
+  // solution filter (InitFilter, filter.f90:100-222): FilterMat(i,l) column-major, LAF weights/normMod
+  std::vector<double> FilterMat, IntegrationWeight;
+  double normMod = 0.;
   // boundary sides 0..nBCSides-1 (InitBC, getboundaryflux.f90:87-256): type, 0-based RefState index,
   // RefStatePrim (rho, u, v, w, p, T) per state
   int nBCSides = 0;
@@ -1232,6 +1235,8 @@ static void SurfInt_GPUorder(const Ctx& C, int nVar, const double* Flux_master, 
 }
 
 struct Work {
+  // LAF filter state per element (filter_vars.f90): lim, eRatio, r, ekin_avg_old, ekin_fluc_avg_old
+  std::vector<double> lim, eRatio, r, ekin_avg_old, ekin_fluc_avg_old;
   std::vector<double> UPrim, U_master, U_slave, UPrim_master, UPrim_slave, Flux_master, Flux_slave;
   std::vector<double> gradUx, gradUy, gradUz, gx_m, gy_m, gz_m, gx_s, gy_s, gz_s, liftflux;
   std::vector<double> f, g, h;
@@ -1457,12 +1462,238 @@ static void ApplyDMatrix_GPUorder(const Ctx& C, double* Ut, const double* f, con
     }
 }
 
+// ---------------------------------------------------------------------------------------
+// Filter: src/filter/filter.f90
+// ---------------------------------------------------------------------------------------
+// INVERSE (mathtools; LAPACK DGETRF/DGETRI in the reference): Gauss-Jordan elimination with partial
+// pivoting, column-major n x n
+static void INVERSE(int n, const std::vector<double>& A, std::vector<double>& Ainv) {
+  std::vector<double> M(A);
+  Ainv.assign(n * n, 0.);
+  for (int i = 0; i < n; ++i) Ainv[i + n * i] = 1.;
+  for (int c = 0; c < n; ++c) {
+    int p = c;
+    for (int r = c + 1; r < n; ++r) if (std::fabs(M[r + n * c]) > std::fabs(M[p + n * c])) p = r;
+    if (p != c)
+      for (int k = 0; k < n; ++k) { std::swap(M[c + n * k], M[p + n * k]); std::swap(Ainv[c + n * k], Ainv[p + n * k]); }
+    const double d = M[c + n * c];
+    for (int k = 0; k < n; ++k) { M[c + n * k] /= d; Ainv[c + n * k] /= d; }
+    for (int r = 0; r < n; ++r) {
+      if (r == c) continue;
+      const double f = M[r + n * c];
+      if (f == 0.) continue;
+      for (int k = 0; k < n; ++k) { M[r + n * k] -= f * M[c + n * k]; Ainv[r + n * k] -= f * Ainv[c + n * k]; }
+    }
+  }
+}
+
+// buildLegendreVdm  basis.f90:100-160 (default branch: sVdm_Leg = INVERSE(Vdm_Leg))
+static void buildLegendreVdm(int N_In, const double* xi_In, std::vector<double>& Vdm_Leg, std::vector<double>& sVdm_Leg) {
+  const int n = N_In + 1;
+  Vdm_Leg.assign(n * n, 0.);
+  for (int i = 0; i <= N_In; ++i)
+    for (int j = 0; j <= N_In; ++j) {
+      double dummy;
+      LegendrePolynomialAndDerivative(j, xi_In[i], Vdm_Leg[i + n * j], dummy);
+    }
+  INVERSE(n, Vdm_Leg, sVdm_Leg);
+}
+
+// InitializeVandermonde  basis.f90:168-186: Vdm(iXi,:) = l(xi_Out(iXi)), (0:N_Out,0:N_In)
+static void InitializeVandermonde(int N_In, int N_Out, const double* wBary_In, const double* xi_In,
+                                  const double* xi_Out, double* Vdm) {
+  std::vector<double> row(N_In + 1);
+  for (int iXi = 0; iXi <= N_Out; ++iXi) {
+    LagrangeInterpolationPolys(xi_Out[iXi], N_In, xi_In, wBary_In, row.data());
+    for (int j = 0; j <= N_In; ++j) Vdm[iXi + (N_Out + 1) * j] = row[j];
+  }
+}
+
+// GetVandermonde  interpolation.f90:324-395 (column-major Vdm_In_Out(0:N_out,0:N_in), Vdm_Out_In(0:N_in,0:N_out))
+static void GetVandermonde(int N_in, int nt_in, int N_out, int nt_out, double* Vdm_In_Out, double* Vdm_Out_In,
+                           bool modal) {
+  const int ni = N_in + 1, no = N_out + 1;
+  if (nt_in == nt_out && N_in == N_out) {
+    for (int t = 0; t < ni * ni; ++t) { Vdm_In_Out[t] = 0.; if (Vdm_Out_In) Vdm_Out_In[t] = 0.; }
+    for (int i = 0; i < ni; ++i) { Vdm_In_Out[i + ni * i] = 1.; if (Vdm_Out_In) Vdm_Out_In[i + ni * i] = 1.; }
+    return;
+  }
+  std::vector<double> xin(ni), xout(no), wbin(ni), wbout(no);
+  GetNodesAndWeights(N_in, nt_in, xin.data(), nullptr, wbin.data());
+  GetNodesAndWeights(N_out, nt_out, xout.data(), nullptr, wbout.data());
+  std::vector<double> VLi, sVLi, VLo, sVLo;
+  if (modal) {
+    buildLegendreVdm(N_in, xin.data(), VLi, sVLi);
+    buildLegendreVdm(N_out, xout.data(), VLo, sVLo);
+  }
+  if (N_out < N_in && modal) {
+    // MATMUL(Vdm_Leg_Out(0:N_Out,0:N_Out), sVdm_Leg_In(0:N_Out,0:N_In))
+    for (int i = 0; i < no; ++i)
+      for (int j = 0; j < ni; ++j) {
+        double acc = 0.;
+        for (int k = 0; k < no; ++k) acc = acc + VLo[i + no * k] * sVLi[k + ni * j];
+        Vdm_In_Out[i + no * j] = acc;
+      }
+  } else {
+    InitializeVandermonde(N_in, N_out, wbin.data(), xin.data(), xout.data(), Vdm_In_Out);
+  }
+  if (Vdm_Out_In) {
+    if (N_in < N_out && modal) {
+      // MATMUL(Vdm_Leg_In(0:N_In,0:N_In), sVdm_Leg_Out(0:N_In,0:N_Out))
+      for (int i = 0; i < ni; ++i)
+        for (int j = 0; j < no; ++j) {
+          double acc = 0.;
+          for (int k = 0; k < ni; ++k) acc = acc + VLi[i + ni * k] * sVLo[k + no * j];
+          Vdm_Out_In[i + ni * j] = acc;
+        }
+    } else {
+      InitializeVandermonde(N_out, N_in, wbout.data(), xout.data(), xin.data(), Vdm_Out_In);
+    }
+  }
+}
+
+// ChangeBasis3D_XYZ  changeBasis.t90 (ChangeBasis3D :231-279 with one Vandermonde per direction):
+// xi, eta, zeta sweeps, each output accumulated over the input index in increasing order
+static void ChangeBasis3D_XYZ(int nVar, int NIn, int NOut, const double* Vx, const double* Vy, const double* Vz,
+                              const double* X_In, double* X_Out) {
+  const int ni = NIn + 1, no = NOut + 1;
+  std::vector<double> B1((size_t)nVar * no * ni * ni, 0.), B2((size_t)nVar * no * no * ni, 0.);
+  for (int kI = 0; kI < ni; ++kI) for (int jI = 0; jI < ni; ++jI) for (int iI = 0; iI < ni; ++iI)
+    for (int iO = 0; iO < no; ++iO)
+      for (int v = 0; v < nVar; ++v)
+        B1[v + nVar * (iO + no * (jI + (size_t)ni * kI))] =
+            B1[v + nVar * (iO + no * (jI + (size_t)ni * kI))] + Vx[iO + no * iI] * X_In[v + nVar * (iI + ni * (jI + (size_t)ni * kI))];
+  for (int kI = 0; kI < ni; ++kI) for (int jI = 0; jI < ni; ++jI) for (int jO = 0; jO < no; ++jO)
+    for (int iO = 0; iO < no; ++iO)
+      for (int v = 0; v < nVar; ++v)
+        B2[v + nVar * (iO + no * (jO + (size_t)no * kI))] =
+            B2[v + nVar * (iO + no * (jO + (size_t)no * kI))] + Vy[jO + no * jI] * B1[v + nVar * (iO + no * (jI + (size_t)ni * kI))];
+  for (size_t t = 0; t < (size_t)nVar * no * no * no; ++t) X_Out[t] = 0.;
+  for (int kI = 0; kI < ni; ++kI) for (int kO = 0; kO < no; ++kO) for (int jO = 0; jO < no; ++jO)
+    for (int iO = 0; iO < no; ++iO)
+      for (int v = 0; v < nVar; ++v)
+        X_Out[v + nVar * (iO + no * (jO + (size_t)no * kO))] =
+            X_Out[v + nVar * (iO + no * (jO + (size_t)no * kO))] + Vz[kO + no * kI] * B2[v + nVar * (iO + no * (jO + (size_t)no * kI))];
+}
+
+// InitFilter (filter.f90:100-222) with HestFilter (:231-263) and buildLegendreVdm (basis.f90:100-160)
+static int InitFilter(Ctx& C) {
+  const dg_config& c = C.cfg;
+  if (c.filter_type == DG_FILTER_NONE) return 0;
+  const int N = C.B.N, n = N + 1;
+  std::vector<double> Fd(n * n, 0.);
+  if (c.filter_type == DG_FILTER_CUTOFF || c.filter_type == DG_FILTER_LAF) {
+    if (c.n_filter < 0 || c.n_filter > N) return -1;
+    for (int iDeg = 0; iDeg <= c.n_filter; ++iDeg) Fd[iDeg + n * iDeg] = 1.;
+  } else if (c.filter_type == DG_FILTER_MODAL) {
+    const double alpha = c.hest_filter_param[0], sExp = c.hest_filter_param[1];
+    const double etac = c.hest_filter_param[2] / (double)(N + 1);
+    for (int iDeg = 0; iDeg <= std::min((int)c.hest_filter_param[2] - 1, N); ++iDeg) Fd[iDeg + n * iDeg] = 1.;
+    if (alpha >= 0.)
+      for (int iDeg = (int)c.hest_filter_param[2]; iDeg <= N; ++iDeg) {
+        const double eta = (double)(iDeg + 1) / (double)(N + 1);
+        Fd[iDeg + n * iDeg] = std::exp(-alpha * std::pow((eta - etac) / (1. - etac), sExp));
+      }
+  } else {
+    return -1;
+  }
+  std::vector<double> Vdm_Leg, sVdm_Leg;
+  buildLegendreVdm(N, C.B.xGP.data(), Vdm_Leg, sVdm_Leg);
+  // FilterMat = MATMUL(MATMUL(Vdm_Leg, FilterMat), sVdm_Leg)
+  std::vector<double> T(n * n, 0.);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      double acc = 0.;
+      for (int k = 0; k < n; ++k) acc = acc + Vdm_Leg[i + n * k] * Fd[k + n * j];
+      T[i + n * j] = acc;
+    }
+  C.FilterMat.assign(n * n, 0.);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      double acc = 0.;
+      for (int k = 0; k < n; ++k) acc = acc + T[i + n * k] * sVdm_Leg[k + n * j];
+      C.FilterMat[i + n * j] = acc;
+    }
+  if (c.filter_type == DG_FILTER_LAF) {
+    const int n3 = C.n3;
+    C.IntegrationWeight.assign((size_t)n3 * C.M.nElems, 0.);
+    for (int e = 0; e < C.M.nElems; ++e) {
+      double Vol = 0.;
+      for (int k = 0; k <= N; ++k) for (int j = 0; j <= N; ++j) for (int i = 0; i <= N; ++i) {
+        const size_t id = C.vol(i, j, k, e);
+        C.IntegrationWeight[id] = C.B.wGP[i] * C.B.wGP[j] * C.B.wGP[k] / C.M.sJ[id];
+        Vol = Vol + C.IntegrationWeight[id];
+      }
+      for (int t = 0; t < n3; ++t) C.IntegrationWeight[(size_t)e * n3 + t] = C.IntegrationWeight[(size_t)e * n3 + t] / Vol;
+    }
+    C.normMod = (std::pow((double)c.n_filter + 1, -2. / 3.) - std::pow(2., -2. / 3.)) /
+                (std::pow((double)(N + 1), -2. / 3.) - std::pow((double)(c.n_filter + 1), -2. / 3.));
+  }
+  return 0;
+}
+
+// one element through the three 1D sweeps xi, eta, zeta (Filter -> ChangeBasis3D_GPU,
+// changeBasis.t90:287-359; same accumulation order as the host ChangeBasis3D)
+static void filter_element(const Ctx& C, const double* Uin, double* Uout) {
+  const double* F = C.FilterMat.data();
+  ChangeBasis3D_XYZ(5, C.B.N, C.B.N, F, F, F, Uin, Uout);
+}
+
+// Filter (filter.f90:272-311) or Filter_LAF (filter.f90:318-474), in place
+static void ApplyFilter(const Ctx& C, Work& W, double* U) {
+  const int n3 = C.n3;
+  if (C.cfg.filter_type != DG_FILTER_LAF) {
+#pragma omp parallel for schedule(static)
+    for (int e = 0; e < C.M.nElems; ++e) {
+      std::vector<double> Uf(5 * n3);
+      filter_element(C, &U[(size_t)5 * n3 * e], Uf.data());
+      std::memcpy(&U[(size_t)5 * n3 * e], Uf.data(), sizeof(double) * 5 * n3);
+    }
+    return;
+  }
+  const double LAF_alpha = C.cfg.laf_alpha;
+#pragma omp parallel for schedule(static)
+  for (int e = 0; e < C.M.nElems; ++e) {
+    double* Ue = &U[(size_t)5 * n3 * e];
+    const double* IW = &C.IntegrationWeight[(size_t)n3 * e];
+    std::vector<double> Uf(5 * n3);
+    filter_element(C, Ue, Uf.data());
+    double U_Avg[5] = {0., 0., 0., 0., 0.};
+    for (int t = 0; t < n3; ++t)
+      for (int c = 1; c <= 3; ++c) U_Avg[c] = U_Avg[c] + Uf[c + 5 * t] / Ue[0 + 5 * t] * IW[t];
+    double ekin_avg = 0., ekin_fluc_avg = 0.;
+    for (int t = 0; t < n3; ++t) {
+      const double r2 = Ue[5 * t] * Ue[5 * t];
+      const double f1 = Ue[1 + 5 * t] - Uf[1 + 5 * t], f2 = Ue[2 + 5 * t] - Uf[2 + 5 * t], f3 = Ue[3 + 5 * t] - Uf[3 + 5 * t];
+      ekin_fluc_avg = ekin_fluc_avg + (f1 * f1 / r2 + f3 * f3 / r2 + f2 * f2 / r2) * IW[t];
+      ekin_avg = ekin_avg + ((Uf[1 + 5 * t] - U_Avg[1]) * (Uf[1 + 5 * t] - U_Avg[1]) / r2 +
+                             (Uf[2 + 5 * t] - U_Avg[2]) * (Uf[2 + 5 * t] - U_Avg[2]) / r2 +
+                             (Uf[3 + 5 * t] - U_Avg[3]) * (Uf[3 + 5 * t] - U_Avg[3]) / r2) * IW[t];
+    }
+    W.eRatio[e] = (ekin_fluc_avg / ekin_avg) * C.normMod;
+    W.lim[e] = std::max(W.lim[e], 1.0E-8);
+    const double dedt_lim = std::fabs(ekin_avg - W.ekin_avg_old[e]) / ((ekin_fluc_avg - W.ekin_fluc_avg_old[e]));
+    if ((dedt_lim > 1.0) && ((ekin_fluc_avg - W.ekin_fluc_avg_old[e]) > 0.)) {
+      W.lim[e] = W.eRatio[e];
+    } else if ((ekin_fluc_avg - W.ekin_fluc_avg_old[e]) < 0.) {
+      W.lim[e] = W.eRatio[e];
+    } else if (W.eRatio[e] > W.lim[e] * LAF_alpha) {
+      std::memcpy(Ue, Uf.data(), sizeof(double) * 5 * n3);
+      W.r[e] = W.r[e] + 1.;
+    }
+    W.ekin_avg_old[e] = ekin_avg;
+    W.ekin_fluc_avg_old[e] = ekin_fluc_avg;
+  }
+}
+
 // DGTimeDerivative_weakForm  src/dg/dg.f90:255-425 (periodic/inner sides, no MPI, no filter/source)
-static void DGTimeDerivative(const Ctx& C, Work& W, const double* U, double* Ut) {
+static void DGTimeDerivative(const Ctx& C, Work& W, double* U, double* Ut) {
   const dg_config& cfg = C.cfg;
   const int N = C.B.N, n = C.n;
   const size_t nDOF = (size_t)C.n3 * C.M.nElems, nF = (size_t)C.n2 * C.M.nSides;
   const double Kappa = cfg.kappa, R = cfg.R;
+  // 1. Filter the solution vector, in place
+  if (cfg.filter_type != DG_FILTER_NONE) ApplyFilter(C, W, U);
   // 2. ProlongToFaceCons
   ProlongToFace_GPUorder(C, 5, U, W.U_master.data(), W.U_slave.data());
   // 3. ConsToPrim volume
@@ -1829,7 +2060,30 @@ orc_handle* orc_create(const dg_config* cfg, int nElems, int nSides, const doubl
   build_s2v2(h->C);
   alloc_work(h->C, h->W);
   h->Ut.assign((size_t)5 * h->C.n3 * nElems, 0.);
+  if (InitFilter(h->C) != 0) { delete h; return nullptr; }
+  // LAF state initial values (filter.f90:195-199)
+  h->W.lim.assign(nElems, 1E-8); h->W.eRatio.assign(nElems, 0.); h->W.r.assign(nElems, 0.);
+  h->W.ekin_avg_old.assign(nElems, 1.E-16); h->W.ekin_fluc_avg_old.assign(nElems, 1.E-16);
   return h;
+}
+
+// GetVandermonde / ChangeBasis3D(_XYZ) for the golden checks against unitTests/{Vandermonde,ChangeBasis}.bin
+int orc_get_vandermonde(int N_in, int nt_in, int N_out, int nt_out, int modal, double* Vdm_In_Out, double* Vdm_Out_In) {
+  GetVandermonde(N_in, nt_in, N_out, nt_out, Vdm_In_Out, Vdm_Out_In, modal != 0);
+  return 0;
+}
+int orc_change_basis_3d(int nVar, int NIn, int NOut, const double* Vx, const double* Vy, const double* Vz,
+                        const double* X_In, double* X_Out) {
+  ChangeBasis3D_XYZ(nVar, NIn, NOut, Vx, Vy, Vz, X_In, X_Out);
+  return 0;
+}
+
+int orc_laf_state(orc_handle* h, double* lim, double* eRatio, double* r) {
+  const size_t nE = h->C.M.nElems;
+  if (lim) std::memcpy(lim, h->W.lim.data(), nE * sizeof(double));
+  if (eRatio) std::memcpy(eRatio, h->W.eRatio.data(), nE * sizeof(double));
+  if (r) std::memcpy(r, h->W.r.data(), nE * sizeof(double));
+  return 0;
 }
 
 void orc_destroy(orc_handle* h) { delete h; }
@@ -1871,7 +2125,7 @@ int orc_set_boundaries(orc_handle* h, int nBCSides, const int* bc_type, const in
   return 0;
 }
 
-int orc_rhs(orc_handle* h, const double* U, double* Ut) {
+int orc_rhs(orc_handle* h, double* U, double* Ut) {
   DGTimeDerivative(h->C, h->W, U, Ut);
   return 0;
 }

@@ -35,6 +35,9 @@ def lib():
         L.orc_create.argtypes = [_P, ctypes.c_int, ctypes.c_int] + [_P] * 10
         L.orc_destroy.argtypes = [_P]
         L.orc_set_boundaries.argtypes = [_P, ctypes.c_int, _P, _P, ctypes.c_int, _P]
+        L.orc_laf_state.argtypes = [_P, _P, _P, _P]
+        L.orc_get_vandermonde.argtypes = [ctypes.c_int] * 5 + [_P, _P]
+        L.orc_change_basis_3d.argtypes = [ctypes.c_int] * 3 + [_P] * 5
         L.orc_rhs.argtypes = [_P, _P, _P]
         L.orc_get_work.argtypes = [_P, ctypes.c_int, _P]
         L.orc_lserk_steps.argtypes = [_P, ctypes.c_double, ctypes.c_double, ctypes.c_int, _P, _P]
@@ -80,6 +83,26 @@ def s2v2(N):
     return a
 
 
+def get_vandermonde(N_in, nt_in, N_out, nt_out, modal):
+    """GetVandermonde: (Vdm_In_Out (N_out+1, N_in+1), Vdm_Out_In (N_in+1, N_out+1)), Fortran order."""
+    a = np.zeros((N_out + 1, N_in + 1), order="F")
+    b = np.zeros((N_in + 1, N_out + 1), order="F")
+    lib().orc_get_vandermonde(N_in, nt_in, N_out, nt_out, int(modal), _p(a), _p(b))
+    return a, b
+
+
+def change_basis_3d(X, Vx, Vy=None, Vz=None):
+    """ChangeBasis3D(_XYZ) of X(nVar,0:NIn,0:NIn,0:NIn) (Fortran order) with (0:NOut,0:NIn) matrices."""
+    Vy = Vx if Vy is None else Vy
+    Vz = Vx if Vz is None else Vz
+    Vx, Vy, Vz = (np.asfortranarray(v, dtype=np.float64) for v in (Vx, Vy, Vz))
+    X = np.asfortranarray(X, dtype=np.float64)
+    nVar, NIn, NOut = X.shape[0], X.shape[1] - 1, Vx.shape[0] - 1
+    out = np.zeros((nVar, NOut + 1, NOut + 1, NOut + 1), order="F")
+    lib().orc_change_basis_3d(nVar, NIn, NOut, _p(Vx), _p(Vy), _p(Vz), _p(X), _p(out))
+    return out
+
+
 class Oracle:
     """CPU restatement of DGTimeDerivative_weakForm / TimeStepByLSERKW2 on one mesh."""
 
@@ -90,6 +113,8 @@ class Oracle:
         self._keep = [m.Metrics_fTilde, m.Metrics_gTilde, m.Metrics_hTilde, m.sJ, m.NormVec, m.TangVec1, m.TangVec2,
                       m.SurfElem, m.ElemToSide, m.SideToElem]
         self._h = lib().orc_create(ctypes.byref(cfg), m.nElems, m.nSides, *[_p(a) for a in self._keep])
+        if not self._h:
+            raise ValueError("orc_create failed (filter configuration)")
         nb = getattr(m, "nBCSides", 0)
         if nb:
             if boundaries is None:
@@ -114,10 +139,19 @@ class Oracle:
             pass
 
     def rhs(self, U):
-        U = np.ascontiguousarray(U, dtype=np.float64)
-        Ut = np.zeros_like(U)
-        lib().orc_rhs(self._h, _p(U), _p(Ut))
+        """Ut of the state U; with a filter configured U itself is filtered in place first (as the
+        reference's DGTimeDerivative_weakForm does), so a numpy U receives the filtered state."""
+        Uc = np.array(U, dtype=np.float64, copy=True, order="C")
+        Ut = np.zeros_like(Uc)
+        lib().orc_rhs(self._h, _p(Uc), _p(Ut))
+        if self.cfg.filter_type and isinstance(U, np.ndarray):
+            U[...] = Uc
         return Ut
+
+    def laf_state(self):
+        out = [np.zeros(self.mesh.nElems) for _ in range(3)]
+        lib().orc_laf_state(self._h, *[_p(a) for a in out])
+        return tuple(out)
 
     def work(self, which, shape):
         out = np.zeros(shape)

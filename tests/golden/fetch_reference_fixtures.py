@@ -13,6 +13,8 @@ tree is absent:
   ProlongToFace_{G,GL}3D.bin   prolonged face data
   SurfIntFlux.bin              random face flux                       (unitTests/SurfInt.f90)
   SurfInt_{G,GL}3D.bin         surface-integral result
+  Vandermonde.bin              nodal and modal Vandermonde matrices, 4 node sets  (unitTests/Vandermonde.f90)
+  ChangeBasis.bin              ChangeBasis3D / ChangeBasis3D_XYZ of a fixed field (unitTests/ChangeBasis.f90)
   TGV_Re1600_Split_TGVAnalysis_Reference.csv
                                Taylor-Green vortex analysis of the split-form regression run
                                (regressioncheck/checks/tgv/split/), one row every 10 time steps
@@ -42,6 +44,8 @@ FILES = [
     "SurfIntFlux.bin",
     "SurfInt_G3D.bin",
     "SurfInt_GL3D.bin",
+    "Vandermonde.bin",
+    "ChangeBasis.bin",
 ]
 
 

@@ -1,8 +1,9 @@
 """The oracle against the reference's own golden vectors (unitTests/*.bin, copied to tests/golden).
 
 Tolerances follow the reference's unit tests: ALMOSTEQUALABSORREL(..., 50*PP_RealTolerance) for nodes
-(unitTests/NodesAndWeights.f90:46-50) and 100*PP_RealTolerance for D, ProlongToFace and SurfInt
-(unitTests/DerivativeMatrix.f90:76, SurfInt.f90:151-153).
+(unitTests/NodesAndWeights.f90:46-50) and for ChangeBasis (ChangeBasis.f90), 100*PP_RealTolerance for
+D, ProlongToFace, SurfInt and the Vandermonde matrices (unitTests/DerivativeMatrix.f90:76,
+SurfInt.f90:151-153, Vandermonde.f90).
 """
 import os
 
@@ -168,3 +169,43 @@ def test_br2_equals_br1_for_continuous_data():
     out = _lifting_pair(5, 2, 0.0, smooth)
     a, b = out["br1"][0], out["br2"][0]
     assert np.abs(a - b).max() <= 1e-11 * np.abs(a).max()
+
+
+def test_vandermonde_golden():
+    """GetVandermonde (interpolation.f90:324-395) for N_in = 2..5, N_out = 3..6, the four node sets in
+    and out, nodal and modal (the modal branches use buildLegendreVdm, basis.f90:100-160)."""
+    a = np.frombuffer(records(os.path.join(GOLD, "Vandermonde.bin"))[0], "<f8")
+    voi = a[:6 * 7 * 512].reshape(512, 7, 6).transpose(2, 1, 0)   # Vdm_Out_In(0:5,0:6,k)
+    vio = a[6 * 7 * 512:].reshape(512, 6, 7).transpose(2, 1, 0)   # Vdm_In_Out(0:6,0:5,k)
+    k = 0
+    for nin in range(2, 6):
+        for nout in range(3, 7):
+            for tin in range(1, 5):
+                for tout in range(1, 5):
+                    for modal in (False, True):
+                        io, oi = orc.get_vandermonde(nin, tin, nout, tout, modal)
+                        assert almost_equal_abs_or_rel(io, vio[:nout + 1, :nin + 1, k], 100 * EPS), (nin, nout, tin, tout, modal)
+                        assert almost_equal_abs_or_rel(oi, voi[:nin + 1, :nout + 1, k], 100 * EPS), (nin, nout, tin, tout, modal)
+                        k += 1
+    assert k == 512
+
+
+def test_change_basis_golden():
+    """ChangeBasis3D and ChangeBasis3D_XYZ (changeBasis.t90) on the unit test's fixed field: the
+    sweeps the solution filter applies."""
+    nVar, NIn, NOut, nElems = 3, 4, 5, 6
+    a = np.frombuffer(records(os.path.join(GOLD, "ChangeBasis.bin"))[0], "<f8")
+    n3 = nVar * (NOut + 1) ** 3
+    uout = a[:n3 * nElems * 4].reshape(4, nElems, n3)
+    Vdm = np.zeros((NOut + 1, NIn + 1), order="F")
+    Vdm2, Vdm3 = np.zeros_like(Vdm), np.zeros_like(Vdm)
+    z = 1
+    for q in range(NIn + 1):
+        for p in range(NOut + 1):
+            z += 1
+            Vdm[p, q], Vdm2[p, q], Vdm3[p, q] = 1.0 + 1.0 / z, 1.0 - 1.0 / z, 1.0 + 0.1 * z
+    cnt = nVar * (NIn + 1) ** 3
+    uin = (1.0 + 0.1 * (2 + np.arange(cnt, dtype=np.float64))).reshape((nVar, NIn + 1, NIn + 1, NIn + 1), order="F")
+    for slot, mats in ((2, (Vdm, Vdm, Vdm)), (3, (Vdm, Vdm2, Vdm3))):
+        out = orc.change_basis_3d(uin, *mats).ravel(order="F")
+        assert almost_equal_abs_or_rel(out, uout[slot, 0], 50 * EPS), slot
