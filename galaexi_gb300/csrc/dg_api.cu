@@ -721,6 +721,11 @@ int dg_get_gradients(dg_ctx* ctx, double* d_gradUx, double* d_gradUy, double* d_
   if (!ctx->cfg.parabolic) { set_error("dg_get_gradients: operator is not parabolic"); return DG_ERR_UNSUPPORTED; }
   if (!ctx->grad_ok) { set_error("dg_get_gradients: no RHS evaluated on this mesh yet"); return DG_ERR_ARG; }
   cudaStream_t st = (cudaStream_t)stream;
+  if (!ctx->grad_rho) {
+    // the operator lifts without the density gradient; complete it from the stored primitive state
+    if (int rc = table_for(ctx->n)->relift(ctx, st)) return rc;
+    ctx->grad_rho = true;
+  }
   const long long nNodes = (long long)ctx->nElems * ctx->n3;
   int grid = (int)((nNodes + 255) / 256);
   if (grid > 152 * 16) grid = 152 * 16;

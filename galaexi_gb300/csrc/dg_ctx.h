@@ -111,6 +111,7 @@ struct dg_ctx {
   AdjTape tape;
   bool mesh_ok = false;
   bool grad_ok = false;    // Gvol holds the lifted gradients of the last RHS evaluation
+  bool grad_rho = false;   // ... including the density gradient (the operator itself skips it)
   double pref = 0.;       // reference pressure of the mixed form (dg_set_pressure_offset)
   // solution filter (FilterType > 0): FilterMat (n x n); LAF: per-element state [5][nElems] followed
   // by the normalised integration weights [e][n3], and normMod
@@ -155,6 +156,8 @@ struct NPTable {
   int (*configure_a)();
   int (*adj)(dg_ctx*, const double* U, gx::CotSrc cs, int mode, double* Uout, double* Ubar, double* Kbar,
              double b_dt, double mRKA, double* acc, cudaStream_t st);
+  // the full lifting of the stored primitive state of the last operator call (with the density gradient)
+  int (*relift)(dg_ctx*, cudaStream_t st);
 };
 
 }  // namespace gxc

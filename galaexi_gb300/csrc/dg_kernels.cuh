@@ -181,18 +181,19 @@ k_prolong(const S* __restrict__ U, const int* __restrict__ E2S, const double* __
 // k_lift: Lifting_BR1 (lifting_br1.t90:47-167): volume part + surface part + sJ, then
 // ProlongToFaceLifting.  Lifted variables (rho,u,v,w,T) = PRIM_LIFT (eos.h:143).
 // =====================================================================================
-// Outer state of the lifting flux at a face node: the slave primitives (rho,u,v,w,T), or on a BC
-// side the ghost state that reproduces the boundary lifting flux (Lifting_GetBoundaryFlux_Kernel,
-// getboundaryflux.f90:945-1019)
+// Boundary sides in the lifting: the slave slot of a BC side (no slave element) receives the ghost
+// state 2F - P_master of the lifted variables (rho,u,v,w,T) for the reference's boundary lifting value
+// F (Lifting_GetBoundaryFlux_Kernel, getboundaryflux.f90:945-1019); the BR1 flux 0.5 (P_master +
+// ghost) (weak) and 0.5 (ghost - P_master) (strong), and the BR2 jump, then reproduce it, so the
+// lifting kernel itself carries no boundary code.  Thread per BC face node.
 template <typename R>
-__device__ __forceinline__ void lift_outer_state(const Launch& L, const Gas<R>& gas, int side, const R* pm,
-                                                 const R* ps, const R* fg, int n2, R out[5]) {
-  const int liftc[5] = {0, 1, 2, 3, 5};
-  if (side >= L.nBCSides) {
-#pragma unroll
-    for (int v = 0; v < 5; ++v) out[v] = ps[liftc[v] * n2];
-    return;
-  }
+__global__ void __launch_bounds__(256)
+k_bc_lift_ghost(R* __restrict__ Pf, const R* __restrict__ Fgeo, Gas<R> gas, Launch L, int n2) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)L.nBCSides * n2) return;
+  const int side = (int)(t / n2), pq = (int)(t - (long long)side * n2);
+  const R* pm = Pf + (size_t)side * 6 * n2 + pq;
+  const R* fg = Fgeo + (size_t)side * 10 * n2 + pq;
   R Pm[6];
 #pragma unroll
   for (int c = 0; c < 6; ++c) Pm[c] = pm[c * n2];
@@ -202,16 +203,21 @@ __device__ __forceinline__ void lift_outer_state(const Launch& L, const Gas<R>& 
   const R t2[3] = {fg[6 * n2], fg[7 * n2], fg[8 * n2]};
   const int bt = L.bctype[side];
   const R* ref = static_cast<const R*>(L.bcref) + 6 * L.bcstate[side];
-  R Pb[6];
+  R Pb[6], gh[5];
   bc_state(bt, Pm, ref, nv, t1, t2, gas.kappa, gas.R_gas, Pb);
-  bc_lift_ghost(bt, Pm, Pb, out);
+  bc_lift_ghost(bt, Pm, Pb, gh);
+  R* ps = Pf + ((size_t)L.nSides + side) * 6 * n2 + pq;
+  const int liftc[5] = {0, 1, 2, 3, 5};
+#pragma unroll
+  for (int v = 0; v < 5; ++v) ps[liftc[v] * n2] = gh[v];
 }
 
-template <int NP, typename R>
+// V0 = 1 skips the density gradient, which no flux of the operator reads (EvalDiffFlux3D uses the
+// velocity and temperature gradients only); Gvol/Gf then hold no density entries.
+template <int NP, typename R, int V0 = 0>
 __global__ void __launch_bounds__(EPBof<NP>::v * NP * NP * NP)
 k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restrict__ Pf, const R* __restrict__ Fgeo,
-       const int* __restrict__ E2S, DevBasis<R> basis, Launch L, Gas<R> gas_lift, R* __restrict__ Gvol,
-       R* __restrict__ Gf) {
+       const int* __restrict__ E2S, DevBasis<R> basis, Launch L, R* __restrict__ Gvol, R* __restrict__ Gf) {
   constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, EPB = EPBof<NP>::v, N = NP - 1;
   __shared__ SBasis<NP, R> sb;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -241,12 +247,12 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
       // the surface integral (surfint.t90:718-723) folded into the metric terms
       R gxi[5], geta[5], gzeta[5];
 #pragma unroll
-      for (int v = 0; v < 5; ++v) { gxi[v] = R(0); geta[v] = R(0); gzeta[v] = R(0); }
+      for (int v = V0; v < 5; ++v) { gxi[v] = R(0); geta[v] = R(0); gzeta[v] = R(0); }
 #pragma unroll
       for (int l = 0; l < n; ++l) {
         const R dxi = sb.D[i + n * l], deta = sb.D[j + n * l], dzeta = sb.D[k + n * l];
 #pragma unroll
-        for (int v = 0; v < 5; ++v) {
+        for (int v = V0; v < 5; ++v) {
           gxi[v] = gxi[v] + dxi * Ps[el][v][l + n * (j + n * k)];
           geta[v] = geta[v] + deta * Ps[el][v][i + n * (l + n * k)];
           gzeta[v] = gzeta[v] + dzeta * Ps[el][v][i + n * (j + n * l)];
@@ -257,7 +263,7 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
 #pragma unroll
       for (int d = 0; d < 3; ++d)
 #pragma unroll
-        for (int v = 0; v < 5; ++v) g[d][v] = mf[d] * gxi[v] + mg[d] * geta[v] + mh[d] * gzeta[v];
+        for (int v = V0; v < 5; ++v) g[d][v] = mf[d] * gxi[v] + mg[d] * geta[v] + mh[d] * gzeta[v];
     } else {
       // Lifting_VolInt_Conservative (lifting_volint.t90:345-455): D_T (strong) or D_hat_T (weak)
       const R* Dm = (L.lift_mode == 2) ? sb.DhatT : sb.D;  // DhatT(l,i) vs D_T(l,i) = D(i,l)
@@ -265,7 +271,7 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
 #pragma unroll
-        for (int v = 0; v < 5; ++v) g[d][v] = R(0);
+        for (int v = V0; v < 5; ++v) g[d][v] = R(0);
         for (int l = 0; l < n; ++l) {
           R ci, cj, ck;
           if (L.lift_mode == 2) { ci = Dm[l + n * i]; cj = Dm[l + n * j]; ck = Dm[l + n * k]; }
@@ -273,10 +279,10 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
           const int ni = l + n * (j + n * k), nj = i + n * (l + n * k), nk = i + n * (j + n * l);
           const R wf = ci * Me[(0 + d) * n3 + ni], wh = ck * Me[(6 + d) * n3 + nk], wg = cj * Me[(3 + d) * n3 + nj];
 #pragma unroll
-          for (int v = 0; v < 5; ++v) g[d][v] = g[d][v] + wf * Ps[el][v][ni] + wh * Ps[el][v][nk] + wg * Ps[el][v][nj];
+          for (int v = V0; v < 5; ++v) g[d][v] = g[d][v] + wf * Ps[el][v][ni] + wh * Ps[el][v][nk] + wg * Ps[el][v][nj];
         }
 #pragma unroll
-        for (int v = 0; v < 5; ++v) g[d][v] = sj * g[d][v];
+        for (int v = V0; v < 5; ++v) g[d][v] = sj * g[d][v];
       }
     }
     if (L.br2) {
@@ -285,14 +291,14 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
 #pragma unroll
       for (int d = 0; d < 3; ++d)
 #pragma unroll
-        for (int v = 0; v < 5; ++v) Gs[el][d * 5 + v][node] = g[d][v];
+        for (int v = V0; v < 5; ++v) Gs[el][d * 5 + v][node] = g[d][v];
     }
     if (facepass) {
       // Gauss-Lobatto BR1: the surface part is added below by face-node threads
 #pragma unroll
       for (int d = 0; d < 3; ++d)
 #pragma unroll
-        for (int v = 0; v < 5; ++v) Gs[el][d * 5 + v][node] = g[d][v];
+        for (int v = V0; v < 5; ++v) Gs[el][d * 5 + v][node] = g[d][v];
       continue;
     }
     // surface part (SurfInt_Device_Single_Flux, surfint.t90:591-725) of the BR1 flux
@@ -322,15 +328,13 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
       const R* pm = Pf + (size_t)side * 6 * n2 + pq;
       const R* ps = Pf + ((size_t)L.nSides + side) * 6 * n2 + pq;
       const R* fg = Fgeo + (size_t)side * 10 * n2 + pq;
-      R psv[5];
-      lift_outer_state(L, gas_lift, side, pm, ps, fg, n2, psv);
       const R sig = (L.lift_mode == 2) ? ((flip == 0) ? R(1) : R(-1)) : R(1);
       const R wgt = sig * Lhat * R(0.5) * fg[9 * n2] * sj;
       const R nvv[3] = {wgt * fg[0], wgt * fg[n2], wgt * fg[2 * n2]};
 #pragma unroll
-      for (int v = 0; v < 5; ++v) {
+      for (int v = V0; v < 5; ++v) {
         const int c = liftc[v];
-        const R fl = sigflux * pm[c * n2] + psv[v];
+        const R fl = sigflux * pm[c * n2] + ps[c * n2];
 #pragma unroll
         for (int d = 0; d < 3; ++d) g[d][v] = g[d][v] + fl * nvv[d];
       }
@@ -339,7 +343,7 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
 #pragma unroll
     for (int d = 0; d < 3; ++d)
 #pragma unroll
-      for (int v = 0; v < 5; ++v) {
+      for (int v = V0; v < 5; ++v) {
         const R val = g[d][v];
         if (!L.br2) Gs[el][d * 5 + v][node] = val;
         G[(d * 5 + v) * n3] = val;
@@ -370,16 +374,14 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
         const R* pm = Pf + (size_t)side * 6 * n2 + pq;
         const R* ps = Pf + ((size_t)L.nSides + side) * 6 * n2 + pq;
         const R* fg = Fgeo + (size_t)side * 10 * n2 + pq;
-        R psv[5];
-        lift_outer_state(L, gas_lift, side, pm, ps, fg, n2, psv);
         const R sj = Met[((size_t)e * 10 + 9) * n3 + node];
         const R sig = (L.lift_mode == 2) ? ((flip == 0) ? R(1) : R(-1)) : R(1);
         const R wgt = sig * Lhat * R(0.5) * fg[9 * n2] * sj;
         const R nvv[3] = {wgt * fg[0], wgt * fg[n2], wgt * fg[2 * n2]};
 #pragma unroll
-        for (int v = 0; v < 5; ++v) {
+        for (int v = V0; v < 5; ++v) {
           const int c = liftc[v];
-          const R fl = sigflux * pm[c * n2] + psv[v];
+          const R fl = sigflux * pm[c * n2] + ps[c * n2];
 #pragma unroll
           for (int d = 0; d < 3; ++d) Gs[el][d * 5 + v][node] = Gs[el][d * 5 + v][node] + fl * nvv[d];
         }
@@ -390,7 +392,8 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
       const int el = t / n3, node = t - el * n3;
       R* G = Gvol + (size_t)(e0 + el) * 15 * n3 + node;
 #pragma unroll
-      for (int c = 0; c < 15; ++c) G[c * n3] = Gs[el][c][node];
+      for (int c = 0; c < 15; ++c)
+        if (c % 5 >= V0) G[c * n3] = Gs[el][c][node];
     }
   }
   // ProlongToFaceLifting
@@ -412,7 +415,6 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
     const R* pm = nullptr;
     const R* ps = nullptr;
     const R* fg = nullptr;
-    R psv[5];
     if (L.br2) {
       const R* Lv = is_minus(ls) ? sb.Lm : sb.Lp;
       const R* Lh = is_minus(ls) ? sb.Lhm : sb.Lhp;
@@ -423,9 +425,9 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
       bw = R(L.eta_br2) * R(0.5) * fg[9 * n2] * bw;
       pm = Pf + (size_t)side * 6 * n2 + pq;
       ps = Pf + ((size_t)L.nSides + side) * 6 * n2 + pq;
-      lift_outer_state(L, gas_lift, side, pm, ps, fg, n2, psv);
     }
     for (int c = 0; c < 15; ++c) {
+      if (c % 5 < V0) continue;
       R s;
       if (!L.gauss) {
         s = Gs[el][c][face_node(n, ls, a, b, is_minus(ls) ? 0 : N)];
@@ -437,11 +439,83 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
       }
       if (L.br2) {
         const int d = c / 5, v = c - 5 * d;
-        s = s + bw * (psv[v] - pm[liftc[v] * n2]) * fg[d * n2];
+        s = s + bw * (ps[liftc[v] * n2] - pm[liftc[v] * n2]) * fg[d * n2];
       }
       gf[c * n2] = s;
     }
   }
+}
+
+// k_bc_face: GetBoundaryFlux_GPU (getboundaryflux.f90:542-838) with the SurfElem factor of
+// FillFlux (fillflux.f90:162-170), thread per face node of the BC sides (a launch of its own, so
+// that the boundary code does not weigh on the registers of k_face)
+template <typename R>
+__global__ void __launch_bounds__(256)
+k_bc_face(const R* __restrict__ Pf, const R* __restrict__ Gf, const R* __restrict__ Fgeo, Gas<R> gas, Launch L,
+          int n2, R* __restrict__ Flux) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)L.nBCSides * n2) return;
+  const int side = (int)(t / n2), pq = (int)(t - (long long)side * n2);
+  const int bt = L.bctype[side];
+  const R* ref = static_cast<const R*>(L.bcref) + 6 * L.bcstate[side];
+  const int riemann = L.riemann, split = L.split, parabolic = L.parabolic;
+  const R* pf = Pf + (size_t)side * 6 * n2 + pq;
+  const R* gm = Gf + (size_t)side * 15 * n2 + pq;
+  const R* fg = Fgeo + (size_t)side * 10 * n2 + pq;
+  R* out = Flux + (size_t)side * 5 * n2 + pq;
+  R PL[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) PL[c] = pf[c * n2];
+  const R nv[3] = {fg[0], fg[n2], fg[2 * n2]};
+  const R t1[3] = {fg[3 * n2], fg[4 * n2], fg[5 * n2]};
+  const R t2[3] = {fg[6 * n2], fg[7 * n2], fg[8 * n2]};
+  const R se = fg[9 * n2];
+  R F[5];
+  R Pm[6], Pb[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) Pm[c] = PL[c];
+  Pm[4] = p_abs(PL[4], gas);
+  bc_state(bt, Pm, ref, nv, t1, t2, gas.kappa, gas.R_gas, Pb);
+  R gx[5], gy[5], gz[5], fd[5];
+  if (parabolic) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) { gx[v] = gm[v * n2]; gy[v] = gm[(5 + v) * n2]; gz[v] = gm[(10 + v) * n2]; }
+  }
+  if (bc_riemann_type(bt)) {
+    // Riemann solver between the inner state and the boundary state (both via PrimToCons)
+    R Uc[5], Ub[5], Ps[6];
+    prim_to_cons_face(Pm, gas, Uc);
+    prim_to_cons_face(Pb, gas, Ub);
+#pragma unroll
+    for (int c = 0; c < 6; ++c) Ps[c] = Pb[c];
+    Ps[4] = OffsetOf<R>::v ? Pb[4] - gas.pref : Pb[4];
+    riemann_face(riemann, split, Uc, Ub, PL, Ps, nv, t1, t2, gas, F);
+    if (parabolic) {
+      normal_diff_flux(PL, gx, gy, gz, nv, gas.mu, gas.lambda, fd);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) F[v] = F[v] + R(0.5) * fd[v];
+      normal_diff_flux(Pb, gx, gy, gz, nv, gas.mu, gas.lambda, fd);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) F[v] = F[v] + R(0.5) * fd[v];
+    }
+  } else {
+    // walls: pressure flux, plus the viscous flux of the wall state
+    const R pw = OffsetOf<R>::v ? Pb[4] - gas.pref : Pb[4];
+    F[0] = R(0);
+    F[1] = pw * nv[0];
+    F[2] = pw * nv[1];
+    F[3] = pw * nv[2];
+    F[4] = R(0);
+    if (parabolic) {
+      if (bt == 9 || bt == 91) bc_wall_gradients(bt, nv, t1, t2, gx, gy, gz);
+      normal_diff_flux(Pb, gx, gy, gz, nv, gas.mu, gas.lambda, fd);
+      if (bt == 3) fd[4] = R(0);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) F[v] = F[v] + fd[v];
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < 5; ++v) out[v * n2] = F[v] * se;
 }
 
 // =====================================================================================
@@ -451,7 +525,8 @@ template <typename R>
 __global__ void __launch_bounds__(256)
 k_face(const R* __restrict__ Uf, const R* __restrict__ Pf, const R* __restrict__ Gf, const R* __restrict__ Fgeo,
        Gas<R> gas, Launch L, int n2, R* __restrict__ Flux) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  // connected sides only (nBCSides .. nSides-1); the BC sides are k_bc_face's
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x + (long long)L.nBCSides * n2;
   if (t >= (long long)L.nSides * n2) return;
   const int side = (int)(t / n2), pq = (int)(t - (long long)side * n2);
   const size_t S = L.nSides;
@@ -472,59 +547,6 @@ k_face(const R* __restrict__ Uf, const R* __restrict__ Pf, const R* __restrict__
   const R t2[3] = {fg[6 * n2], fg[7 * n2], fg[8 * n2]};
   const R se = fg[9 * n2];
   R F[5];
-  if (side < L.nBCSides) {
-    // GetBoundaryFlux_GPU (getboundaryflux.f90:542-838)
-    const int bt = L.bctype[side];
-    const R* ref = static_cast<const R*>(L.bcref) + 6 * L.bcstate[side];
-    R Pm[6], Pb[6];
-#pragma unroll
-    for (int c = 0; c < 6; ++c) Pm[c] = PL[c];
-    Pm[4] = p_abs(PL[4], gas);
-    bc_state(bt, Pm, ref, nv, t1, t2, gas.kappa, gas.R_gas, Pb);
-    R gx[5], gy[5], gz[5], fd[5];
-    if (L.parabolic) {
-      const R* gm = Gf + (size_t)side * 15 * n2 + pq;
-#pragma unroll
-      for (int v = 0; v < 5; ++v) { gx[v] = gm[v * n2]; gy[v] = gm[(5 + v) * n2]; gz[v] = gm[(10 + v) * n2]; }
-    }
-    if (bc_riemann_type(bt)) {
-      // Riemann solver between the inner state and the boundary state (both via PrimToCons)
-      R Uc[5], Ub[5], Ps[6];
-      prim_to_cons_face(Pm, gas, Uc);
-      prim_to_cons_face(Pb, gas, Ub);
-#pragma unroll
-      for (int c = 0; c < 6; ++c) Ps[c] = Pb[c];
-      Ps[4] = OffsetOf<R>::v ? Pb[4] - gas.pref : Pb[4];
-      riemann_face(L.riemann, L.split, Uc, Ub, PL, Ps, nv, t1, t2, gas, F);
-      if (L.parabolic) {
-        normal_diff_flux(PL, gx, gy, gz, nv, gas.mu, gas.lambda, fd);
-#pragma unroll
-        for (int v = 0; v < 5; ++v) F[v] = F[v] + R(0.5) * fd[v];
-        normal_diff_flux(Pb, gx, gy, gz, nv, gas.mu, gas.lambda, fd);
-#pragma unroll
-        for (int v = 0; v < 5; ++v) F[v] = F[v] + R(0.5) * fd[v];
-      }
-    } else {
-      // walls: pressure flux, plus the viscous flux of the wall state
-      const R pw = OffsetOf<R>::v ? Pb[4] - gas.pref : Pb[4];
-      F[0] = R(0);
-      F[1] = pw * nv[0];
-      F[2] = pw * nv[1];
-      F[3] = pw * nv[2];
-      F[4] = R(0);
-      if (L.parabolic) {
-        if (bt == 9 || bt == 91) bc_wall_gradients(bt, nv, t1, t2, gx, gy, gz);
-        normal_diff_flux(Pb, gx, gy, gz, nv, gas.mu, gas.lambda, fd);
-        if (bt == 3) fd[4] = R(0);
-#pragma unroll
-        for (int v = 0; v < 5; ++v) F[v] = F[v] + fd[v];
-      }
-    }
-    R* out = Flux + (size_t)side * 5 * n2 + pq;
-#pragma unroll
-    for (int v = 0; v < 5; ++v) out[v * n2] = F[v] * se;
-    return;
-  }
   riemann_face(L.riemann, L.split, UL, UR, PL, PR, nv, t1, t2, gas, F);
   if (L.parabolic) {
     // ViscousFlux_Kernel_CUDA (riemann.f90:638-700): F = F + 0.5*f(L); F = F + 0.5*f(R)

@@ -56,6 +56,8 @@ template <typename R>
 int configure() {
   GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_lift<NP, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lift_smem<R>()),
               "k_lift shared-memory attribute");
+  GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_lift<NP, R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lift_smem<R>()),
+              "k_lift shared-memory attribute");
   int rc = cfg_vol<R, -1, 0>() | cfg_vol<R, -1, 1>();
   if constexpr (NP >= 3) {
     rc |= cfg_vol<R, 0, 0>() | cfg_vol<R, 0, 1>() | cfg_vol<R, 1, 0>() | cfg_vol<R, 1, 1>() | cfg_vol<R, 2, 0>() |
@@ -83,8 +85,9 @@ int vol(dg_ctx* ctx, PrecData<R>& P, const S* U, gx::RKArgsT<S> rk, int rkmode, 
   return DG_OK;
 }
 
-// forward kernels up to (and excluding) the volume kernel: prims + face traces, lifting, face fluxes
-template <typename R, typename S = double>
+// forward kernels up to (and excluding) the volume kernel: prims + face traces, lifting, face fluxes;
+// V0 = 1 lifts without the density gradient (no flux reads it; dg_get_gradients completes it)
+template <typename R, typename S = double, int V0 = 0>
 void rhs_front(dg_ctx* ctx, PrecData<R>& P, const S* U, const gx::Gas<R>& gas, cudaStream_t st, cudaEvent_t* ev,
                bool face) {
   const int grid = (ctx->nElems + EPB - 1) / EPB;
@@ -93,18 +96,29 @@ void rhs_front(dg_ctx* ctx, PrecData<R>& P, const S* U, const gx::Gas<R>& gas, c
   const gx::DevBasis<double> bd = gxc::dev_basis(ctx->d, NP);  // FP64 face interpolation in every form
   gx::k_prolong<NP, R, S><<<grid, NT, 0, st>>>(U, ctx->E2S.p, bd.Lm, bd.Lp, gas, L, P.Pvol.p, P.Uf.p, P.Pf.p);
   ctx->launches++;
+  const long long nbc = (long long)ctx->nBCSides * NP * NP;
+  if (ctx->cfg.parabolic && nbc > 0) {
+    gx::k_bc_lift_ghost<R><<<(int)((nbc + 255) / 256), 256, 0, st>>>(P.Pf.p, P.Fgeo.p, gas, L, NP * NP);
+    ctx->launches++;
+  }
   if (ev) cudaEventRecord(ev[1], st);
   if (ctx->cfg.parabolic) {
-    gx::k_lift<NP, R><<<grid, NT, lift_smem<R>(), st>>>(P.Pvol.p, P.Met.p, P.Pf.p, P.Fgeo.p, ctx->E2S.p, b, L, gas,
-                                                        P.Gvol.p, P.Gf.p);
+    gx::k_lift<NP, R, V0><<<grid, NT, lift_smem<R>(), st>>>(P.Pvol.p, P.Met.p, P.Pf.p, P.Fgeo.p, ctx->E2S.p, b, L,
+                                                            P.Gvol.p, P.Gf.p);
     ctx->launches++;
   }
   if (ev) cudaEventRecord(ev[2], st);
   if (face) {
-    const long long nt = (long long)ctx->nSides * NP * NP;
-    const int fgrid = (int)((nt + 255) / 256);
-    gx::k_face<R><<<fgrid, 256, 0, st>>>(P.Uf.p, P.Pf.p, P.Gf.p, P.Fgeo.p, gas, L, NP * NP, P.Flux.p);
-    ctx->launches++;
+    const long long nt = (long long)(ctx->nSides - ctx->nBCSides) * NP * NP;
+    if (nt > 0) {
+      gx::k_face<R><<<(int)((nt + 255) / 256), 256, 0, st>>>(P.Uf.p, P.Pf.p, P.Gf.p, P.Fgeo.p, gas, L, NP * NP,
+                                                               P.Flux.p);
+      ctx->launches++;
+    }
+    if (nbc > 0) {
+      gx::k_bc_face<R><<<(int)((nbc + 255) / 256), 256, 0, st>>>(P.Pf.p, P.Gf.p, P.Fgeo.p, gas, L, NP * NP, P.Flux.p);
+      ctx->launches++;
+    }
   }
   if (ev) cudaEventRecord(ev[3], st);
 }
@@ -127,7 +141,8 @@ int rhs(dg_ctx* ctx, PrecData<R>& P, const double* U, gx::RKArgs rk, int rkmode,
   // the reference filters its module array d_U in place; U is the caller's state array
   if (ctx->cfg.filter_type != DG_FILTER_NONE) filter(ctx, const_cast<double*>(U), st);
   const gx::Gas<R> gas = gxc::make_gas<R>(ctx->cfg, ctx->cfg.precision == DG_PRECISION_MIXED ? ctx->pref : 0.);
-  rhs_front<R>(ctx, P, U, gas, st, ev, true);
+  rhs_front<R, double, 1>(ctx, P, U, gas, st, ev, true);
+  ctx->grad_rho = false;
   int vrc = DG_OK;
   switch (ctx->cfg.split_dg) {
     case DG_SPLIT_NONE: vrc = vol<R, -1>(ctx, P, U, rk, rkmode, gas, st); break;
@@ -273,6 +288,20 @@ int adj(dg_ctx* ctx, const double* U, gx::CotSrc cs, int mode, double* Uout, dou
   return DG_OK;
 }
 
+// the full lifting (density gradient included) of the primitive state stored by the last operator call
+template <typename R>
+int relift_p(dg_ctx* ctx, PrecData<R>& P, cudaStream_t st) {
+  const int grid = (ctx->nElems + EPB - 1) / EPB;
+  gx::k_lift<NP, R, 0><<<grid, NT, lift_smem<R>(), st>>>(P.Pvol.p, P.Met.p, P.Pf.p, P.Fgeo.p, ctx->E2S.p,
+                                                         gxc::dev_basis(P, NP), gxc::make_launch(ctx), P.Gvol.p, P.Gf.p);
+  ctx->launches++;
+  GX_CUDA_TRY(cudaGetLastError(), "k_lift launch");
+  return DG_OK;
+}
+int relift(dg_ctx* ctx, cudaStream_t st) {
+  return ctx->cfg.precision == DG_PRECISION_FP64 ? relift_p<double>(ctx, ctx->d, st) : relift_p<float>(ctx, ctx->f, st);
+}
+
 int rhs_d(dg_ctx* ctx, const double* U, gx::RKArgs rk, int rkmode, cudaStream_t st) { return rhs<double>(ctx, ctx->d, U, rk, rkmode, st); }
 int rhs_f(dg_ctx* ctx, const double* U, gx::RKArgs rk, int rkmode, cudaStream_t st) { return rhs<float>(ctx, ctx->f, U, rk, rkmode, st); }
 
@@ -295,4 +324,4 @@ int cfl(dg_ctx* ctx, const double* U, double cflS, double dflS, double kpr, cuda
 #define GX_CAT2(a, b) a##b
 #define GX_CAT(a, b) GX_CAT2(a, b)
 extern const gxc::NPTable GX_CAT(gx_np_table_, GX_NP) = {configure<double>, configure<float>, rhs_d, rhs_f, cfl,
-                                                         stage_events, configure_t, rhs_t, configure_a, adj};
+                                                         stage_events, configure_t, rhs_t, configure_a, adj, relift};
