@@ -574,6 +574,11 @@ k_face(const R* __restrict__ Uf, const R* __restrict__ Pf, const R* __restrict__
 // (surfint.t90:352-586) + VAX_GPU(-1) + ApplyJacobian, and in RK mode the fused
 // VAXPB_OUT_VAXPB_IN stage update (vector.f90:163-183).
 // =====================================================================================
+// staging slots per node of k_volume (see there); shared by the kernel and its launch code
+__host__ __device__ constexpr int vol_stage_slots(int split, int parab) {
+  return split < 0 ? 15 : (parab ? 12 : (split == DG_SPLIT_PI ? 6 : 9));
+}
+
 template <typename S>
 struct RKArgsT {
   S* U;              // in/out (RK mode)
@@ -590,7 +595,11 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
          const R* __restrict__ Met, const R* __restrict__ Flux, const int* __restrict__ E2S, DevBasis<R> basis,
          Gas<R> gas, Launch L, RKArgsT<S> rk, int rkmode) {
   constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, EPB = EPBof<NP>::v, N = NP - 1;
-  constexpr int NA = (SPLIT >= 0) ? 19 : 15;  // staging: 10 node data + 9 metrics, or 15 fluxes
+  // staging slots per node: the flux-form fluxes of phase A (15; split form: the 12 non-zero viscous
+  // ones), then the node data of phase B (PI: rho, aux, u, v, w, p; other split forms also m1..m3);
+  // the metrics of phase B are read from global memory (L1), so that at N=7 two blocks fit an SM
+  constexpr int NA = vol_stage_slots(SPLIT, PARAB);
+  constexpr int S_RHO = 0, S_AUX = 1, S_U = 2, S_V = 3, S_W = 4, S_PM = 5, S_M1 = 6, S_M2 = 7, S_M3 = 8;
   __shared__ SBasis<NP, R> sb;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   R* A = reinterpret_cast<R*>(smem_raw);             // [EPB][NA][n3]
@@ -659,22 +668,25 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
           fl[d][4] = -Ms[d][0] * tq[0] - Ms[d][1] * tq[1] - Ms[d][2] * tq[2];
         }
       }
+      // slot of flux (d, v): d*5+v, or d*4+v-1 for the split form's viscous fluxes (no density row)
+      constexpr int v0 = (SPLIT < 0) ? 0 : 1, nvs = 5 - v0;
 #pragma unroll
       for (int d = 0; d < 3; ++d)
 #pragma unroll
-        for (int v = 0; v < 5; ++v) Ae[(d * 5 + v) * n3 + node] = fl[d][v];
+        for (int v = v0; v < 5; ++v) Ae[(d * nvs + v - v0) * n3 + node] = fl[d][v];
     }
     __syncthreads();
     if (active) {
       // ApplyDMatrix_Kernel (applydmatrix.t90:19-75), order f, h, g
-      constexpr int v0 = (SPLIT < 0) ? 0 : 1;
+      constexpr int v0 = (SPLIT < 0) ? 0 : 1, nvs = 5 - v0;
 #pragma unroll
       for (int l = 0; l < n; ++l) {
         const R ci = sb.DhatT[l + n * i], ck = sb.DhatT[l + n * k], cj = sb.DhatT[l + n * j];
         const int ni = l + n * (j + n * k), nk = i + n * (j + n * l), nj = i + n * (l + n * k);
 #pragma unroll
         for (int v = v0; v < 5; ++v)
-          vacc[v] = vacc[v] + ci * Ae[(0 + v) * n3 + ni] + ck * Ae[(10 + v) * n3 + nk] + cj * Ae[(5 + v) * n3 + nj];
+          vacc[v] = vacc[v] + ci * Ae[(0 * nvs + v - v0) * n3 + ni] + ck * Ae[(2 * nvs + v - v0) * n3 + nk] +
+                    cj * Ae[(1 * nvs + v - v0) * n3 + nj];
       }
     }
   }
@@ -687,21 +699,19 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
     if (active) {
       const S* Un = U + ((size_t)e * n3 + node) * 5;
       const R* P = Pvol + (size_t)e * 7 * n3 + node;
-      const R* M = Met + (size_t)e * 10 * n3 + node;
       const R E = (R)Un[4];
       const R rho = P[0], uu = P[n3], vv = P[2 * n3], ww = P[3 * n3], pm = P[4 * n3];
-      Ae[0 * n3 + node] = rho;
-      Ae[1 * n3 + node] = (R)Un[1];
-      Ae[2 * n3 + node] = (R)Un[2];
-      Ae[3 * n3 + node] = (R)Un[3];
-      Ae[4 * n3 + node] = pair_aux<SPLIT, R>(rho, uu, vv, ww, E, p_abs(pm, gas), P[6 * n3]);
-      Ae[5 * n3 + node] = uu;
-      Ae[6 * n3 + node] = vv;
-      Ae[7 * n3 + node] = ww;
-      Ae[8 * n3 + node] = (SPLIT == DG_SPLIT_PI) ? R(4) * pm : pm;  // PI: 4p (exact scaling)
-      Ae[9 * n3 + node] = R(0);
-#pragma unroll
-      for (int c = 0; c < 9; ++c) Ae[(10 + c) * n3 + node] = M[c * n3];
+      Ae[S_RHO * n3 + node] = rho;
+      Ae[S_AUX * n3 + node] = pair_aux<SPLIT, R>(rho, uu, vv, ww, E, p_abs(pm, gas), P[6 * n3]);
+      Ae[S_U * n3 + node] = uu;
+      Ae[S_V * n3 + node] = vv;
+      Ae[S_W * n3 + node] = ww;
+      Ae[S_PM * n3 + node] = (SPLIT == DG_SPLIT_PI) ? R(4) * pm : pm;  // PI: 4p (exact scaling)
+      if constexpr (SPLIT != DG_SPLIT_PI) {
+        Ae[S_M1 * n3 + node] = (R)Un[1];
+        Ae[S_M2 * n3 + node] = (R)Un[2];
+        Ae[S_M3 * n3 + node] = (R)Un[3];
+      }
       R* Ad = AccD + (size_t)el * 15 * n3;
 #pragma unroll
       for (int c = 0; c < 15; ++c) Ad[c * n3 + node] = R(0);
@@ -718,15 +728,19 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
       if (dir == 0) { base = n * li; stride = 1; }
       else if (dir == 1) { base = (li % n) + n2 * (li / n); stride = n; }
       else { base = li; stride = n2; }
-      const int mc = 10 + 3 * dir;
+      const R* Ml = Met + ((size_t)(e0 + lel) * 10 + 3 * dir) * n3;  // this direction's metric terms
 #pragma unroll 1
       for (int a = 0; a < NP - 1; ++a) {
         const int na = base + a * stride;
         PairNode<R> A_;
-        A_.rho = Al[0 * n3 + na]; A_.m1 = Al[1 * n3 + na]; A_.m2 = Al[2 * n3 + na]; A_.m3 = Al[3 * n3 + na];
-        A_.aux = Al[4 * n3 + na]; A_.u = Al[5 * n3 + na]; A_.v = Al[6 * n3 + na]; A_.w = Al[7 * n3 + na];
-        A_.pm = Al[8 * n3 + na];
-        const R ma0 = Al[mc * n3 + na], ma1 = Al[(mc + 1) * n3 + na], ma2 = Al[(mc + 2) * n3 + na];
+        A_.rho = Al[S_RHO * n3 + na]; A_.aux = Al[S_AUX * n3 + na];
+        A_.u = Al[S_U * n3 + na]; A_.v = Al[S_V * n3 + na]; A_.w = Al[S_W * n3 + na]; A_.pm = Al[S_PM * n3 + na];
+        if constexpr (SPLIT != DG_SPLIT_PI) {
+          A_.m1 = Al[S_M1 * n3 + na]; A_.m2 = Al[S_M2 * n3 + na]; A_.m3 = Al[S_M3 * n3 + na];
+        } else {
+          A_.m1 = A_.m2 = A_.m3 = R(0);
+        }
+        const R ma0 = Ml[na], ma1 = Ml[n3 + na], ma2 = Ml[2 * n3 + na];
         R sa[5];
 #pragma unroll
         for (int v = 0; v < 5; ++v) sa[v] = Ad[v * n3 + na];
@@ -734,10 +748,14 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
         for (int b = a + 1; b < NP; ++b) {
           const int nb = base + b * stride;
           PairNode<R> B_;
-          B_.rho = Al[0 * n3 + nb]; B_.m1 = Al[1 * n3 + nb]; B_.m2 = Al[2 * n3 + nb]; B_.m3 = Al[3 * n3 + nb];
-          B_.aux = Al[4 * n3 + nb]; B_.u = Al[5 * n3 + nb]; B_.v = Al[6 * n3 + nb]; B_.w = Al[7 * n3 + nb];
-          B_.pm = Al[8 * n3 + nb];
-          const R Ms0 = ma0 + Al[mc * n3 + nb], Ms1 = ma1 + Al[(mc + 1) * n3 + nb], Ms2 = ma2 + Al[(mc + 2) * n3 + nb];
+          B_.rho = Al[S_RHO * n3 + nb]; B_.aux = Al[S_AUX * n3 + nb];
+          B_.u = Al[S_U * n3 + nb]; B_.v = Al[S_V * n3 + nb]; B_.w = Al[S_W * n3 + nb]; B_.pm = Al[S_PM * n3 + nb];
+          if constexpr (SPLIT != DG_SPLIT_PI) {
+            B_.m1 = Al[S_M1 * n3 + nb]; B_.m2 = Al[S_M2 * n3 + nb]; B_.m3 = Al[S_M3 * n3 + nb];
+          } else {
+            B_.m1 = B_.m2 = B_.m3 = R(0);
+          }
+          const R Ms0 = ma0 + Ml[nb], Ms1 = ma1 + Ml[n3 + nb], Ms2 = ma2 + Ml[2 * n3 + nb];
           R F[5];
           if constexpr (SPLIT == DG_SPLIT_PI) {
             // 8 x the PI flux of split_pair_flux, with the density row at 4 x (its accumulators are

@@ -25,8 +25,8 @@ constexpr int NP = GX_NP;
 constexpr int EPB = gx::EPBof<NP>::v;
 constexpr int NT = EPB * NP * NP * NP;  // threads per element block
 
-template <typename R, int SPL> constexpr size_t volume_smem() {
-  return sizeof(R) * (size_t)EPB * (SPL >= 0 ? 19 + 15 : 15) * NP * NP * NP;
+template <typename R, int SPL, int PAR> constexpr size_t volume_smem() {
+  return sizeof(R) * (size_t)EPB * (gx::vol_stage_slots(SPL, PAR) + (SPL >= 0 ? 15 : 0)) * NP * NP * NP;
 }
 template <typename R> constexpr size_t lift_smem() { return sizeof(R) * (size_t)EPB * 20 * NP * NP * NP; }
 
@@ -38,17 +38,21 @@ int smem_limit() {
   return lim;
 }
 
-template <typename R, int SPL>
+template <typename R, int SPL, int PAR>
 bool vol_fits() {
-  return volume_smem<R, SPL>() + sizeof(gx::SBasis<NP, R>) <= (size_t)smem_limit();
+  return volume_smem<R, SPL, PAR>() + sizeof(gx::SBasis<NP, R>) <= (size_t)smem_limit();
 }
 
 template <typename R, int SPL, int PAR, typename S = double>
 int cfg_vol() {
-  if (!vol_fits<R, SPL>()) return DG_OK;  // variant not runnable on this device; rejected at launch
+  if (!vol_fits<R, SPL, PAR>()) return DG_OK;  // variant not runnable on this device; rejected at launch
   GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_volume<NP, R, SPL, PAR, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)volume_smem<R, SPL>()),
+                                   (int)volume_smem<R, SPL, PAR>()),
               "k_volume shared-memory attribute");
+  // the largest shared-memory carve-out, so that two blocks share an SM where their staging fits
+  GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_volume<NP, R, SPL, PAR, S>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                   100),
+              "k_volume carve-out attribute");
   return DG_OK;
 }
 
@@ -69,7 +73,7 @@ int configure() {
 template <typename R, int SPL, typename S = double>
 int vol(dg_ctx* ctx, PrecData<R>& P, const S* U, gx::RKArgsT<S> rk, int rkmode, const gx::Gas<R>& gas,
         cudaStream_t st) {
-  if (!vol_fits<R, SPL>()) {
+  if (ctx->cfg.parabolic ? !vol_fits<R, SPL, 1>() : !vol_fits<R, SPL, 0>()) {
     gxh::set_error("this N / precision / form needs more shared memory per block than the device offers");
     return DG_ERR_UNSUPPORTED;
   }
@@ -77,11 +81,11 @@ int vol(dg_ctx* ctx, PrecData<R>& P, const S* U, gx::RKArgsT<S> rk, int rkmode, 
   const gx::DevBasis<R> b = gxc::dev_basis(P, NP);
   const gx::Launch L = gxc::make_launch(ctx);
   if (ctx->cfg.parabolic)
-    gx::k_volume<NP, R, SPL, 1, S><<<grid, NT, volume_smem<R, SPL>(), st>>>(U, P.Pvol.p, P.Gvol.p, P.Met.p, P.Flux.p,
-                                                                        ctx->E2S.p, b, gas, L, rk, rkmode);
+    gx::k_volume<NP, R, SPL, 1, S><<<grid, NT, volume_smem<R, SPL, 1>(), st>>>(U, P.Pvol.p, P.Gvol.p, P.Met.p,
+                                                                           P.Flux.p, ctx->E2S.p, b, gas, L, rk, rkmode);
   else
-    gx::k_volume<NP, R, SPL, 0, S><<<grid, NT, volume_smem<R, SPL>(), st>>>(U, P.Pvol.p, P.Gvol.p, P.Met.p, P.Flux.p,
-                                                                        ctx->E2S.p, b, gas, L, rk, rkmode);
+    gx::k_volume<NP, R, SPL, 0, S><<<grid, NT, volume_smem<R, SPL, 0>(), st>>>(U, P.Pvol.p, P.Gvol.p, P.Met.p,
+                                                                           P.Flux.p, ctx->E2S.p, b, gas, L, rk, rkmode);
   return DG_OK;
 }
 
