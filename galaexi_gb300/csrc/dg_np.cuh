@@ -115,7 +115,7 @@ void rhs_front(dg_ctx* ctx, PrecData<R>& P, const S* U, const gx::Gas<R>& gas, c
   if (face) {
     const long long nt = (long long)(ctx->nSides - ctx->nBCSides) * NP * NP;
     if (nt > 0) {
-      gx::k_face<R><<<(int)((nt + 255) / 256), 256, 0, st>>>(P.Uf.p, P.Pf.p, P.Gf.p, P.Fgeo.p, gas, L, NP * NP,
+      gx::k_face<R><<<(int)((nt + 127) / 128), 128, 0, st>>>(P.Uf.p, P.Pf.p, P.Gf.p, P.Fgeo.p, gas, L, NP * NP,
                                                                P.Flux.p);
       ctx->launches++;
     }
