@@ -37,7 +37,7 @@ ALG_BYTES_N7 = 510.0  # compulsory HBM bytes per DOF-stage of a fully fused impl
 # ncu on the 16^3 case of the same kernels (profiles/dgsem_fp64_kernels_tgv_n7_16cube.md): DRAM bytes
 # and executed FP64 thread-instructions (DFMA+DADD+DMUL) per DOF for one k_volume launch; traffic
 # grows with the number of elements, so it is scaled to a launch by nDOF
-KVOL_DRAM_BYTES_PER_DOF = (669.912832e6 + 144.459520e6) / 2097152
+KVOL_DRAM_BYTES_PER_DOF = (670.293248e6 + 143.461888e6) / 2097152
 KVOL_FP64_INSTR_PER_DOF = 519.0
 FP64_ISSUE_PER_CYCLE = 304  # sm__sass_thread_inst_executed_op_dfma_pred_on.sum.peak_sustained (152 SMs x 2)
 TGV_R = 71.42857
