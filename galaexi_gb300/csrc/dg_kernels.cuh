@@ -216,7 +216,7 @@ k_bc_lift_ghost(R* __restrict__ Pf, const R* __restrict__ Fgeo, Gas<R> gas, Laun
 // V0 = 1 skips the density gradient, which no flux of the operator reads (EvalDiffFlux3D uses the
 // velocity and temperature gradients only); Gvol/Gf then hold no density entries.
 template <int NP, typename R, int V0 = 0>
-__global__ void __launch_bounds__(EPBof<NP>::v * NP * NP * NP)
+__global__ void __launch_bounds__(EPBof<NP>::v * NP * NP * NP, 2)
 k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restrict__ Pf, const R* __restrict__ Fgeo,
        const int* __restrict__ E2S, DevBasis<R> basis, Launch L, R* __restrict__ Gvol, R* __restrict__ Gf) {
   constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, EPB = EPBof<NP>::v, N = NP - 1;

@@ -62,6 +62,11 @@ int configure() {
               "k_lift shared-memory attribute");
   GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_lift<NP, R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lift_smem<R>()),
               "k_lift shared-memory attribute");
+  // the largest shared-memory carve-out: at least two lifting blocks per SM
+  GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_lift<NP, R>, cudaFuncAttributePreferredSharedMemoryCarveout, 100),
+              "k_lift carve-out attribute");
+  GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_lift<NP, R, 1>, cudaFuncAttributePreferredSharedMemoryCarveout, 100),
+              "k_lift carve-out attribute");
   int rc = cfg_vol<R, -1, 0>() | cfg_vol<R, -1, 1>();
   if constexpr (NP >= 3) {
     rc |= cfg_vol<R, 0, 0>() | cfg_vol<R, 0, 1>() | cfg_vol<R, 1, 0>() | cfg_vol<R, 1, 1>() | cfg_vol<R, 2, 0>() |

@@ -40,16 +40,21 @@ __device__ __forceinline__ void cons_to_prim_d(const S u[5], const Gas<R>& g, R 
     prim[4] = g.kappaM1 * ((R)u[4] - R(0.5) * ((R)u[1] * prim[1] + (R)u[2] * prim[2] + (R)u[3] * prim[3]));
     prim[5] = prim[4] * srho * g.sR;
   } else {
-    const double sr = 1. / u[0];
-    const double v1 = u[1] * sr, v2 = u[2] * sr, v3 = u[3] * sr;
-    const double p = g.kappaM1D * (u[4] - 0.5 * (u[1] * v1 + u[2] * v2 + u[3] * v3));
-    srho = (R)sr;
-    prim[0] = (R)u[0];
-    prim[1] = (R)v1;
-    prim[2] = (R)v2;
-    prim[3] = (R)v3;
+    // mixed form: velocities and kinetic energy in FP32 (relative error ~1e-7 of quantities that
+    // are themselves rounded to FP32), the energy difference E - ke and p' = p - p_ref in FP64,
+    // where the cancellation at low Mach would lose the pressure fluctuations
+    const R rho = (R)u[0], m1 = (R)u[1], m2 = (R)u[2], m3 = (R)u[3];
+    const R sr = R(1) / rho;
+    const R v1 = m1 * sr, v2 = m2 * sr, v3 = m3 * sr;
+    const R ke = R(0.5) * (m1 * v1 + m2 * v2 + m3 * v3);
+    const double p = g.kappaM1D * (u[4] - (double)ke);
+    srho = sr;
+    prim[0] = rho;
+    prim[1] = v1;
+    prim[2] = v2;
+    prim[3] = v3;
     prim[4] = (R)(p - g.prefD);
-    prim[5] = (R)(p * sr * g.sRD);
+    prim[5] = (R)p * sr * g.sR;
   }
 }
 // absolute pressure from the stored one
