@@ -576,6 +576,21 @@ k_face(const R* __restrict__ Uf, const R* __restrict__ Pf, const R* __restrict__
 // (surfint.t90:352-586) + VAX_GPU(-1) + ApplyJacobian, and in RK mode the fused
 // VAXPB_OUT_VAXPB_IN stage update (vector.f90:163-183).
 // =====================================================================================
+// Shared-memory position of node i + n(j + nk) in the staging of k_volume.  N=7: the i and j bits
+// are XOR-swizzled with bits of j and k so that the x-, y- and z-line threads of phase B and the
+// node threads hit 32 distinct FP32 banks (two wavefronts per FP64 access); the plain layout gave
+// 8-way (FP32) and 16-way (FP64) conflicts on the x-lines.  An involution that permutes each block
+// of 32 consecutive nodes.
+template <int NP>
+__device__ __forceinline__ int vsw(int node) {
+  if constexpr (NP == 8) {
+    const int kk = (node >> 6) & 3;
+    return node ^ ((((node >> 5) & 1) << 2) | kk | (kk << 3));
+  } else {
+    return node;
+  }
+}
+
 // staging slots per node of k_volume (see there); shared by the kernel and its launch code
 __host__ __device__ constexpr int vol_stage_slots(int split, int parab) {
   return split < 0 ? 15 : (parab ? 12 : (split == DG_SPLIT_PI ? 6 : 9));
@@ -619,6 +634,7 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
   const int el = tid / n3, node = tid - (tid / n3) * n3;
   const int e = e0 + el;
   const int i = node % n, j = (node / n) % n, k = node / n2;
+  const int snode = vsw<NP>(node);  // shared-memory position of this node
   R* Ae = A + (size_t)el * NA * n3;
   R vacc[5] = {0, 0, 0, 0, 0};  // this node's volume integral, kept in registers through phase B
 
@@ -675,7 +691,7 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
 #pragma unroll
       for (int d = 0; d < 3; ++d)
 #pragma unroll
-        for (int v = v0; v < 5; ++v) Ae[(d * nvs + v - v0) * n3 + node] = fl[d][v];
+        for (int v = v0; v < 5; ++v) Ae[(d * nvs + v - v0) * n3 + snode] = fl[d][v];
     }
     __syncthreads();
     if (active) {
@@ -684,7 +700,8 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
 #pragma unroll
       for (int l = 0; l < n; ++l) {
         const R ci = sb.DhatT[l + n * i], ck = sb.DhatT[l + n * k], cj = sb.DhatT[l + n * j];
-        const int ni = l + n * (j + n * k), nk = i + n * (j + n * l), nj = i + n * (l + n * k);
+        const int ni = vsw<NP>(l + n * (j + n * k)), nk = vsw<NP>(i + n * (j + n * l)),
+                  nj = vsw<NP>(i + n * (l + n * k));
 #pragma unroll
         for (int v = v0; v < 5; ++v)
           vacc[v] = vacc[v] + ci * Ae[(0 * nvs + v - v0) * n3 + ni] + ck * Ae[(2 * nvs + v - v0) * n3 + nk] +
@@ -703,20 +720,20 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
       const R* P = Pvol + (size_t)e * 7 * n3 + node;
       const R E = (R)Un[4];
       const R rho = P[0], uu = P[n3], vv = P[2 * n3], ww = P[3 * n3], pm = P[4 * n3];
-      Ae[S_RHO * n3 + node] = rho;
-      Ae[S_AUX * n3 + node] = pair_aux<SPLIT, R>(rho, uu, vv, ww, E, p_abs(pm, gas), P[6 * n3]);
-      Ae[S_U * n3 + node] = uu;
-      Ae[S_V * n3 + node] = vv;
-      Ae[S_W * n3 + node] = ww;
-      Ae[S_PM * n3 + node] = (SPLIT == DG_SPLIT_PI) ? R(4) * pm : pm;  // PI: 4p (exact scaling)
+      Ae[S_RHO * n3 + snode] = rho;
+      Ae[S_AUX * n3 + snode] = pair_aux<SPLIT, R>(rho, uu, vv, ww, E, p_abs(pm, gas), P[6 * n3]);
+      Ae[S_U * n3 + snode] = uu;
+      Ae[S_V * n3 + snode] = vv;
+      Ae[S_W * n3 + snode] = ww;
+      Ae[S_PM * n3 + snode] = (SPLIT == DG_SPLIT_PI) ? R(4) * pm : pm;  // PI: 4p (exact scaling)
       if constexpr (SPLIT != DG_SPLIT_PI) {
-        Ae[S_M1 * n3 + node] = (R)Un[1];
-        Ae[S_M2 * n3 + node] = (R)Un[2];
-        Ae[S_M3 * n3 + node] = (R)Un[3];
+        Ae[S_M1 * n3 + snode] = (R)Un[1];
+        Ae[S_M2 * n3 + snode] = (R)Un[2];
+        Ae[S_M3 * n3 + snode] = (R)Un[3];
       }
       R* Ad = AccD + (size_t)el * 15 * n3;
 #pragma unroll
-      for (int c = 0; c < 15; ++c) Ad[c * n3 + node] = R(0);
+      for (int c = 0; c < 15; ++c) Ad[c * n3 + snode] = R(0);
     }
     __syncthreads();
     const int lel = tid / (3 * n2);
@@ -733,27 +750,27 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
       const R* Ml = Met + ((size_t)(e0 + lel) * 10 + 3 * dir) * n3;  // this direction's metric terms
 #pragma unroll 1
       for (int a = 0; a < NP - 1; ++a) {
-        const int na = base + a * stride;
+        const int na = base + a * stride, sna = vsw<NP>(na);
         PairNode<R> A_;
-        A_.rho = Al[S_RHO * n3 + na]; A_.aux = Al[S_AUX * n3 + na];
-        A_.u = Al[S_U * n3 + na]; A_.v = Al[S_V * n3 + na]; A_.w = Al[S_W * n3 + na]; A_.pm = Al[S_PM * n3 + na];
+        A_.rho = Al[S_RHO * n3 + sna]; A_.aux = Al[S_AUX * n3 + sna];
+        A_.u = Al[S_U * n3 + sna]; A_.v = Al[S_V * n3 + sna]; A_.w = Al[S_W * n3 + sna]; A_.pm = Al[S_PM * n3 + sna];
         if constexpr (SPLIT != DG_SPLIT_PI) {
-          A_.m1 = Al[S_M1 * n3 + na]; A_.m2 = Al[S_M2 * n3 + na]; A_.m3 = Al[S_M3 * n3 + na];
+          A_.m1 = Al[S_M1 * n3 + sna]; A_.m2 = Al[S_M2 * n3 + sna]; A_.m3 = Al[S_M3 * n3 + sna];
         } else {
           A_.m1 = A_.m2 = A_.m3 = R(0);
         }
         const R ma0 = Ml[na], ma1 = Ml[n3 + na], ma2 = Ml[2 * n3 + na];
         R sa[5];
 #pragma unroll
-        for (int v = 0; v < 5; ++v) sa[v] = Ad[v * n3 + na];
+        for (int v = 0; v < 5; ++v) sa[v] = Ad[v * n3 + sna];
 #pragma unroll 4
         for (int b = a + 1; b < NP; ++b) {
-          const int nb = base + b * stride;
+          const int nb = base + b * stride, snb = vsw<NP>(nb);
           PairNode<R> B_;
-          B_.rho = Al[S_RHO * n3 + nb]; B_.aux = Al[S_AUX * n3 + nb];
-          B_.u = Al[S_U * n3 + nb]; B_.v = Al[S_V * n3 + nb]; B_.w = Al[S_W * n3 + nb]; B_.pm = Al[S_PM * n3 + nb];
+          B_.rho = Al[S_RHO * n3 + snb]; B_.aux = Al[S_AUX * n3 + snb];
+          B_.u = Al[S_U * n3 + snb]; B_.v = Al[S_V * n3 + snb]; B_.w = Al[S_W * n3 + snb]; B_.pm = Al[S_PM * n3 + snb];
           if constexpr (SPLIT != DG_SPLIT_PI) {
-            B_.m1 = Al[S_M1 * n3 + nb]; B_.m2 = Al[S_M2 * n3 + nb]; B_.m3 = Al[S_M3 * n3 + nb];
+            B_.m1 = Al[S_M1 * n3 + snb]; B_.m2 = Al[S_M2 * n3 + snb]; B_.m3 = Al[S_M3 * n3 + snb];
           } else {
             B_.m1 = B_.m2 = B_.m3 = R(0);
           }
@@ -778,11 +795,11 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
 #pragma unroll
           for (int v = 0; v < 5; ++v) {
             sa[v] = sa[v] + dba * F[v];
-            Ad[v * n3 + nb] += dab * F[v];
+            Ad[v * n3 + snb] += dab * F[v];
           }
         }
 #pragma unroll
-        for (int v = 0; v < 5; ++v) Ad[v * n3 + na] = sa[v];
+        for (int v = 0; v < 5; ++v) Ad[v * n3 + sna] = sa[v];
       }
     }
     __syncthreads();
@@ -790,7 +807,7 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
       const R* Ad = AccD + (size_t)el * 15 * n3;
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
-        R sv = Ad[v * n3 + node] + Ad[(5 + v) * n3 + node] + Ad[(10 + v) * n3 + node];
+        R sv = Ad[v * n3 + snode] + Ad[(5 + v) * n3 + snode] + Ad[(10 + v) * n3 + snode];
         if (SPLIT == DG_SPLIT_PI && v == 0) sv = sv * R(2);
         vacc[v] = vacc[v] + sv;
       }
@@ -827,7 +844,7 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
         int p, q;
         s2v2_inv(N, a, b, flip, ls, p, q);
         const R* fx = Flux + (size_t)side * 5 * n2 + p + n * q;
-        R* Su = A + (size_t)el2 * NA * n3 + fnode;
+        R* Su = A + (size_t)el2 * NA * n3 + vsw<NP>(fnode);
         if (flip == 0) {
 #pragma unroll
           for (int v = 0; v < 5; ++v) Su[v * n3] = Su[v * n3] + fx[v * n2] * Lhat;
@@ -840,7 +857,7 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
     }
     if (!active) return;
 #pragma unroll
-    for (int v = 0; v < 5; ++v) ut[v] = Ae[v * n3 + node];
+    for (int v = 0; v < 5; ++v) ut[v] = Ae[v * n3 + snode];
   }
   if (!active) return;
 #pragma unroll
