@@ -60,10 +60,13 @@ def parse():
                     help="skip the mixed-precision comparisons and the adjoint measurement")
     ap.add_argument("--adjoint-fd", type=int, default=0,
                     help="central-difference check of the adjoint gradient along this many random directions")
-    ap.add_argument("--adjoint-steps", type=int, default=200)
+    ap.add_argument("--adjoint-steps", type=int, default=None,
+                    help="steps of the adjoint window (default 200 for the N=5 case, 50 for --only scale64)")
     ap.add_argument("--only", default=None, choices=["adjoint", "mixed_tgv", "mixed_curved", "scale64"],
                     help="run one of the extra measurements alone and print its JSON (profiling runs)")
-    return ap.parse_args()
+    args = ap.parse_args()
+    args.steps_given = any(a == "--steps" or a.startswith("--steps=") for a in sys.argv[1:])
+    return args
 
 
 class ClockSampler:
@@ -257,7 +260,7 @@ def run_ours(args, world, rank, local):
     if not args.no_extras and args.precision == "fp64":
         extras["mixed_vs_fp64"] = mixed_vs_fp64_tgv(args.workload, args.steps, stream)
         extras["mixed_vs_fp64_curved_br2"] = mixed_vs_fp64_curved_br2(stream)
-        extras["adjoint"] = adjoint_tgv(stream, steps=args.adjoint_steps, fd_dirs=args.adjoint_fd)
+        extras["adjoint"] = adjoint_tgv(stream, steps=args.adjoint_steps or 200, fd_dirs=args.adjoint_fd)
     if rank == 0:
         line = {"metric": "DOF-stage updates/s", "value": value, "unit": "DOF-stage/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -562,9 +565,10 @@ def main():
         torch.cuda.set_device(local)
         stream = torch.cuda.current_stream()
         if args.only == "adjoint":
-            res = adjoint_tgv(stream, steps=args.adjoint_steps, fd_dirs=args.adjoint_fd)
+            res = adjoint_tgv(stream, steps=args.adjoint_steps or 200, fd_dirs=args.adjoint_fd)
         elif args.only == "scale64":
-            res = scale_c5(stream, steps=args.steps, adj_steps=args.adjoint_steps)
+            # the 64^3 case: 100 LSERK steps per form and a 50-step adjoint window unless given
+            res = scale_c5(stream, steps=args.steps if args.steps_given else 100, adj_steps=args.adjoint_steps or 50)
         elif args.only == "mixed_tgv":
             res = mixed_vs_fp64_tgv(args.workload, args.steps, stream)
         else:

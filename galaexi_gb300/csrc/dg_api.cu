@@ -461,7 +461,7 @@ int dg_ctx_destroy(dg_ctx* ctx) {
   ctx->t.release(); ctx->Ud.release(); ctx->Utd.release();
   ctx->UfB.release(); ctx->GfB.release(); ctx->JB.release(); ctx->UBv.release(); ctx->part.release();
   ctx->acc.release(); ctx->W.release(); ctx->K.release(); ctx->tape.store.release();
-  ctx->filt.release(); ctx->laf.release();
+  ctx->filt.release(); ctx->laf.release(); ctx->cflm.release();
   delete ctx;
   return DG_OK;
 }
@@ -560,6 +560,25 @@ int dg_set_mesh(dg_ctx* ctx, int nElems, int nSides, int nBCSides, const double*
   ctx->t.release(); ctx->Ud.release(); ctx->Utd.release();
   ctx->UfB.release(); ctx->GfB.release(); ctx->JB.release(); ctx->UBv.release(); ctx->part.release();
   ctx->W.release(); ctx->K.release(); ctx->tape.store.release();
+  // MetricsAdv and MetricsVisc of InitCalctimestep (navierstokes/calctimestep.f90:51-92), FP64
+  {
+    const dg_config& c = ctx->cfg;
+    const double kpr = (4. / 3. > c.kappa / c.Pr) ? 4. / 3. : c.kappa / c.Pr;  // KAPPASPR_MAX_TIMESTEP_H
+    std::vector<double> h((size_t)nElems * 6 * n3);
+    const double* Ms[3] = {Mf, Mg, Mh};
+    for (size_t e = 0; e < (size_t)nElems; ++e)
+      for (int t = 0; t < n3; ++t) {
+        const size_t id = e * n3 + t;
+        const double sj = sJ[id];
+        for (int d = 0; d < 3; ++d) {
+          const double* m = Ms[d] + 3 * id;
+          h[(e * 6 + d) * n3 + t] = sj * std::sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+          h[(e * 6 + 3 + d) * n3 + t] = kpr * ((m[0] * sj) * (m[0] * sj) + (m[1] * sj) * (m[1] * sj) + (m[2] * sj) * (m[2] * sj));
+        }
+      }
+    if (!ctx->cflm.alloc(h.size())) { set_error("cudaMalloc CFL metrics"); return DG_ERR_ALLOC; }
+    CUDA_TRY(cudaMemcpy(ctx->cflm.p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice), "upload CFL metrics");
+  }
   ctx->laf.release();
   if (ctx->cfg.filter_type == DG_FILTER_LAF) {
     // IntegrationWeight = w_i w_j w_k / sJ normalised by the element volume, and the initial state

@@ -96,6 +96,7 @@ struct dg_ctx {
   gxc::PrecData<float> f;
   gxc::DBuf<double> MetD;  // FP64 packed metrics [e][10][n3] for the CFL reduction (mixed form only)
   const double* metd = nullptr;  // FP64 packed metrics: d.Met in the FP64 form, MetD in the mixed form
+  gxc::DBuf<double> cflm;  // [e][6][n3]: MetricsAdv(1:3), MetricsVisc(1:3) (InitCalctimestep)
   gxc::DBuf<int> E2S;      // [e][6][2]: 0-based side, flip
   gxc::DBuf<double> red;   // dt reduction result (2)
   gxc::DBuf<unsigned long long> bad;

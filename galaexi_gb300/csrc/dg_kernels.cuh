@@ -919,8 +919,8 @@ __device__ __forceinline__ void atomic_min_pos(double* addr, double val) {
 // one block per element, blockDim = n^3 rounded up to a warp multiple
 template <int NP>
 __global__ void __launch_bounds__(1024)
-k_cfl(const double* __restrict__ U, const double* __restrict__ MetD, int nElems, double kappa, double mu0,
-      int parabolic, double KappasPr_max, double CFLScale, double DFLScale, double* __restrict__ dt2,
+k_cfl(const double* __restrict__ U, const double* __restrict__ MetD, const double* __restrict__ Cm, int nElems,
+      double kappa, double mu0, int parabolic, double CFLScale, double DFLScale, double* __restrict__ dt2,
       unsigned long long* __restrict__ bad) {
   constexpr int n3 = NP * NP * NP;
   constexpr int NW = (n3 + 31) / 32;
@@ -936,17 +936,14 @@ k_cfl(const double* __restrict__ U, const double* __restrict__ MetD, int nElems,
     if (!(u[0] > 0.) || !(p > 0.) || !isfinite(u[4]) || !isfinite(u[1] + u[2] + u[3])) atomicAdd(bad, 1ULL);
     const double c = sqrt(kappa * p * srho);
     const double* M = MetD + (size_t)e * 10 * n3 + node;
+    const double* C = Cm + (size_t)e * 6 * n3 + node;  // MetricsAdv(1:3), MetricsVisc(1:3)
     const double sj = M[9 * n3];
     const double vs[3] = {vel[0] * sj, vel[1] * sj, vel[2] * sj};
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       const double m0 = M[(3 * d) * n3], m1 = M[(3 * d + 1) * n3], m2 = M[(3 * d + 2) * n3];
-      const double adv = sj * sqrt(m0 * m0 + m1 * m1 + m2 * m2);  // MetricsAdv (calctimestep.f90:68)
-      lam[d] = fabs(m0 * vs[0] + m1 * vs[1] + m2 * vs[2]) + c * adv;
-      if (parabolic) {  // MetricsVisc (calctimestep.f90:81)
-        const double vis = KappasPr_max * ((m0 * sj) * (m0 * sj) + (m1 * sj) * (m1 * sj) + (m2 * sj) * (m2 * sj));
-        lam[3 + d] = mu0 * srho * vis;
-      }
+      lam[d] = fabs(m0 * vs[0] + m1 * vs[1] + m2 * vs[2]) + c * C[d * n3];
+      if (parabolic) lam[3 + d] = mu0 * srho * C[(3 + d) * n3];
     }
   }
   // max over the element's nodes: warp shuffle, then across the element's warps

@@ -321,8 +321,10 @@ int stage_events(dg_ctx* ctx, double* U, gx::RKArgs rk, cudaStream_t st, cudaEve
 
 int cfl(dg_ctx* ctx, const double* U, double cflS, double dflS, double kpr, cudaStream_t st) {
   const int threads = ((NP * NP * NP + 31) / 32) * 32;
-  gx::k_cfl<NP><<<ctx->nElems, threads, 0, st>>>(U, ctx->metd, ctx->nElems, ctx->cfg.kappa, ctx->cfg.mu0,
-                                                 ctx->cfg.parabolic, kpr, cflS, dflS, ctx->red.p, ctx->bad.p);
+  (void)kpr;  // folded into the precomputed MetricsVisc
+  gx::k_cfl<NP><<<ctx->nElems, threads, 0, st>>>(U, ctx->metd, ctx->cflm.p, ctx->nElems, ctx->cfg.kappa,
+                                                 ctx->cfg.mu0, ctx->cfg.parabolic, cflS, dflS, ctx->red.p,
+                                                 ctx->bad.p);
   ctx->launches++;
   GX_CUDA_TRY(cudaGetLastError(), "k_cfl launch");
   return DG_OK;
