@@ -407,7 +407,7 @@ def scale_c5(stream, steps=100, adj_steps=50, budget_gb=180):
         op.close()
         del K
     res["mixed_speedup"] = res["dof_stage_per_s_mixed"] / res["dof_stage_per_s_fp64"]
-    del ends
+    del ends, U
     torch.cuda.empty_cache()
     cfg = gx.config(N=N, NodeType="gauss-lobatto", Riemann=w["Riemann"], SplitDG=w["SplitDG"], parabolic=True,
                     mu0=w["mu0"], R=TGV_R)
@@ -418,20 +418,21 @@ def scale_c5(stream, steps=100, adj_steps=50, budget_gb=180):
         op.TimeStepByLSERKW2(0.0, dt, U, K, nSteps=adj_steps)
         return U
 
-    ms_f, _ = timed(fwd, stream)
+    ms_f = timed(fwd, stream)[0]
     torch.cuda.empty_cache()
-    # checkpoint budget: at most budget_gb, and what is left of the device after the operator, the
-    # adjoint's work states and scratch (about 12 states at N=7) and a margin
+    # checkpoint budget: at most budget_gb (decimal GB), and what is left of the device after the
+    # operator, the adjoint's work states and scratch, the gradient tensor and a 2 GiB margin; the
+    # end state is written over U0
     free, _ = torch.cuda.mem_get_info()
     state = U0.numel() * 8
-    budget = int(min(budget_gb * 2 ** 30, free - 12 * state - 8 * 2 ** 30))
+    budget = int(min(budget_gb * 1e9, free - op.adjoint_scratch_bytes() - state - 2 * 2 ** 30))
     Uf, plan = None, None
-    t_rec, (Uf, plan) = timed(lambda: op.adjoint_forward(dt, adj_steps, U0, budget), stream)
+    t_rec, (Uf, plan) = timed(lambda: op.adjoint_forward(dt, adj_steps, U0, budget, out=U0), stream)
     J, G = op.kinetic_energy(Uf, grad=True)
     del Uf
     t_rev, mub = timed(lambda: op.adjoint_reverse(G), stream)
-    res.update({"adjoint_steps": adj_steps, "adjoint_budget_gb": budget / 2 ** 30, "adjoint_plan": plan,
-                "state_gb": U0.numel() * 8 / 2 ** 30, "forward_window_ms": ms_f, "adjoint_record_ms": t_rec,
+    res.update({"adjoint_steps": adj_steps, "adjoint_budget_gb": budget / 1e9, "adjoint_plan": plan,
+                "state_gb": U0.numel() * 8 / 1e9, "forward_window_ms": ms_f, "adjoint_record_ms": t_rec,
                 "adjoint_reverse_ms": t_rev, "adjoint_over_forward": (t_rec + t_rev) / ms_f, "J": J, "dJ_dmu": mub,
                 "grad_norm": float(G.norm())})
     op.close()

@@ -82,6 +82,7 @@ _SIGS = {
     "dg_get_gradients": (_I, [_P, _P, _P, _P, _P]),
     "dg_set_boundaries": (_I, [_P, _P, _P, _I, _P]),
     "dg_laf_state": (_I, [_P, _P, _P, _P]),
+    "dg_adjoint_scratch_bytes": (_I, [_P, ctypes.POINTER(ctypes.c_size_t)]),
     "dg_mesh_hopr_sizes": (_I, [ctypes.c_char_p, _IP, _IP, _IP, _IP]),
     "dg_mesh_hopr": (_I, [ctypes.c_char_p, _I, _I] + [_P] * 12),
     "dg_mesh_hopr_bcs": (_I, [ctypes.c_char_p, _IP, _P, _I, _P]),

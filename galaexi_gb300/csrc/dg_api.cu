@@ -844,6 +844,18 @@ int dg_rhs_vjp(dg_ctx* ctx, double t, const double* d_U, const double* d_Utbar, 
   return DG_OK;
 }
 
+int dg_adjoint_scratch_bytes(dg_ctx* ctx, size_t* bytes) {
+  if (int rc = check_ctx(ctx, true)) return rc;
+  if (!bytes) { set_error("dg_adjoint_scratch_bytes: null argument"); return DG_ERR_ARG; }
+  const size_t nE = ctx->nElems, nS = ctx->nSides, n2 = ctx->n2, n3 = ctx->n3, S = nE * 5 * n3;
+  size_t b = S;  // the reverse sweep's second K (plans 2 and 3), allocated per sweep
+  if (!ctx->UBv.p) b += 2 * nS * 5 * n2 + 2 * nS * 5 * n2 + S + 2 * nS * 15 * n2 + 8 + 6 * (size_t)grid_for(nE * n3) +
+                        (nS * n2 + 127) / 128 + nE;
+  if (!ctx->W.p) b += 2 * S;
+  *bytes = b * sizeof(double);
+  return DG_OK;
+}
+
 int dg_adjoint_forward(dg_ctx* ctx, double t0, double dt, int nSteps, const double* d_U0, double* d_U_final,
                        size_t budget_bytes, int* plan_out, void* stream) {
   if (int rc = check_ctx(ctx, true)) return rc;

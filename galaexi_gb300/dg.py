@@ -355,10 +355,17 @@ class DG:
                                        self._stream(stream)), "dg_rhs_vjp")
         return Ub, mb.value
 
-    def adjoint_forward(self, dt, nSteps, U0, budget_bytes, stream=None):
-        """Run and record nSteps steps from U0; returns (U_final, plan)."""
+    def adjoint_scratch_bytes(self):
+        """Device memory the adjoint still allocates besides its checkpoints (dg_adjoint_scratch_bytes)."""
+        b = ctypes.c_size_t()
+        nat.check(nat.lib().dg_adjoint_scratch_bytes(self._h, ctypes.byref(b)), "dg_adjoint_scratch_bytes")
+        return b.value
+
+    def adjoint_forward(self, dt, nSteps, U0, budget_bytes, stream=None, out=None):
+        """Run and record nSteps steps from U0; returns (U_final, plan).  out: tensor for U_final
+        (may be U0 itself)."""
         self._check_state(U0)
-        Uf = self._torch.empty_like(U0)
+        Uf = self._torch.empty_like(U0) if out is None else out
         plan = ctypes.c_int()
         nat.check(nat.lib().dg_adjoint_forward(self._h, 0.0, float(dt), int(nSteps), _tp(U0), _tp(Uf),
                                                int(budget_bytes), ctypes.byref(plan), self._stream(stream)),

@@ -254,6 +254,10 @@ int dg_rhs_vjp(dg_ctx* ctx, double t, const double* d_U, const double* d_Utbar, 
  * writes J, dJ/dU0 and dJ/dmu. */
 int dg_adjoint_forward(dg_ctx* ctx, double t0, double dt, int nSteps, const double* d_U0, double* d_U_final,
                        size_t budget_bytes, int* plan_out, void* stream);
+/* Device memory (bytes) that the adjoint entry points still allocate besides the checkpoints: its
+ * work states and scratch, for sizing budget_bytes against the free memory.  d_U_final may alias
+ * d_U0 (the start state is read once, at the start). */
+int dg_adjoint_scratch_bytes(dg_ctx* ctx, size_t* bytes);
 int dg_adjoint_reverse(dg_ctx* ctx, double* d_Ubar, double* mu_bar, void* stream);
 int dg_adjoint_window(dg_ctx* ctx, double t0, double dt, int nSteps, const double* d_U0, size_t budget_bytes,
                       double* J, double* d_dJdU0, double* dJdmu, double* d_U_final, void* stream);
