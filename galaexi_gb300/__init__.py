@@ -7,7 +7,7 @@ of the reference's operator interface (dg.py).
 """
 from . import _native
 from ._native import DGError, DGConfig, RIEMANN, SPLITDG
-from .dg import DG, Mesh, basis, config, config_from_ini, fill_ini, read_h5, tgv_state
+from .dg import DG, Mesh, basis, config, config_from_ini, fill_ini, read_h5, read_state, tgv_state, write_state
 
 __all__ = ["DG", "Mesh", "DGError", "DGConfig", "RIEMANN", "SPLITDG", "basis", "config", "config_from_ini",
            "fill_ini", "tgv_state"]

@@ -87,6 +87,7 @@ _SIGS = {
     "dg_mesh_hopr": (_I, [ctypes.c_char_p, _I, _I] + [_P] * 12),
     "dg_mesh_hopr_bcs": (_I, [ctypes.c_char_p, _IP, _P, _I, _P]),
     "dg_h5_read": (_I, [ctypes.c_char_p, ctypes.c_char_p, _I, _IP, _P, _P, ctypes.c_longlong, _P, _I]),
+    "dg_write_state": (_I, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, _I, ctypes.c_char_p, _D, _I, _P]),
     "dg_integrals": (_I, [_P, _P, _P, _P]),
     "dg_kinetic_energy": (_I, [_P, _P, _P, _P, _P]),
     "dg_rhs_jvp": (_I, [_P, _D, _P, _P, _D, _P, _P, _P]),

@@ -3,6 +3,7 @@
 // heap, v1 B-tree, dataspace / datatype / data-layout / attribute messages).
 #include "dg_hdf5.h"
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <stdexcept>
@@ -286,6 +287,216 @@ std::vector<std::string> Array::as_strings() const {
     v.push_back(s);
   }
   return v;
+}
+
+// ----------------------------------------------------------------------------------------------
+// Writer
+// ----------------------------------------------------------------------------------------------
+namespace {
+// datatype message bodies (class + version 1, bit field, size, properties)
+std::vector<uint8_t> type_double() {
+  return {0x11, 0x20, 0x3f, 0x00, 8, 0, 0, 0, 0, 0, 64, 0, 52, 11, 0, 52, 0xff, 0x03, 0, 0};
+}
+std::vector<uint8_t> type_int32() { return {0x10, 0x08, 0, 0, 4, 0, 0, 0, 0, 0, 32, 0}; }
+std::vector<uint8_t> type_string(uint32_t len) {  // fixed length, space padded, ASCII
+  return {0x13, 0x02, 0, 0, (uint8_t)(len & 0xff), (uint8_t)((len >> 8) & 0xff), (uint8_t)((len >> 16) & 0xff),
+          (uint8_t)(len >> 24)};
+}
+// dataspace message v1 with maximum dimensions equal to the dimensions
+std::vector<uint8_t> space(const std::vector<uint64_t>& dims) {
+  std::vector<uint8_t> b = {1, (uint8_t)dims.size(), 1, 0, 0, 0, 0, 0};
+  for (int rep = 0; rep < 2; ++rep)
+    for (uint64_t d : dims)
+      for (int k = 0; k < 8; ++k) b.push_back((uint8_t)(d >> (8 * k)));
+  return b;
+}
+struct Buf {
+  std::vector<uint8_t> b;
+  void u(uint64_t v, int n) { for (int k = 0; k < n; ++k) b.push_back((uint8_t)(v >> (8 * k))); }
+  void bytes(const std::vector<uint8_t>& x) { b.insert(b.end(), x.begin(), x.end()); }
+  void pad8() { while (b.size() % 8) b.push_back(0); }
+  void at(size_t off, uint64_t v, int n) { for (int k = 0; k < n; ++k) b[off + k] = (uint8_t)(v >> (8 * k)); }
+};
+const uint64_t kUndefAddr = ~0ULL;
+size_t pad8(size_t n) { return (n + 7) & ~(size_t)7; }
+// one object-header message: type, size, flags, reserved, body padded to 8
+void message(Buf& o, uint16_t type, uint8_t flags, const std::vector<uint8_t>& body) {
+  const size_t sz = pad8(body.size());
+  o.u(type, 2); o.u(sz, 2); o.u(flags, 1); o.u(0, 3);
+  o.bytes(body);
+  while (o.b.size() % 8) o.b.push_back(0);
+}
+// version-1 object header around the given messages (count, bytes)
+std::vector<uint8_t> object_header(int nmsg, const std::vector<uint8_t>& msgs) {
+  Buf h;
+  h.u(1, 1); h.u(0, 1); h.u(nmsg, 2); h.u(1, 4); h.u(msgs.size(), 4); h.u(0, 4);
+  h.bytes(msgs);
+  return h.b;
+}
+}  // namespace
+
+void Writer::attr_string(const std::string& name, const std::string& value) {
+  std::string v = value;
+  while (!v.empty() && v.back() == ' ') v.pop_back();
+  const uint32_t len = v.empty() ? 1 : (uint32_t)v.size();
+  Attr a{name, type_string(len), {1}, {}};
+  a.data.assign(len, ' ');
+  std::memcpy(a.data.data(), v.data(), v.size());
+  attrs_.push_back(a);
+}
+
+void Writer::attr_strings(const std::string& name, const std::vector<std::string>& values, int len) {
+  Attr a{name, type_string((uint32_t)len), {values.size()}, {}};
+  a.data.assign(values.size() * (size_t)len, ' ');
+  for (size_t i = 0; i < values.size(); ++i)
+    std::memcpy(a.data.data() + i * len, values[i].data(), std::min((size_t)len, values[i].size()));
+  attrs_.push_back(a);
+}
+
+void Writer::attr_int(const std::string& name, const std::vector<int32_t>& values) {
+  Attr a{name, type_int32(), {values.size()}, {}};
+  a.data.resize(values.size() * 4);
+  std::memcpy(a.data.data(), values.data(), a.data.size());
+  attrs_.push_back(a);
+}
+
+void Writer::attr_double(const std::string& name, const std::vector<double>& values) {
+  Attr a{name, type_double(), {values.size()}, {}};
+  a.data.resize(values.size() * 8);
+  std::memcpy(a.data.data(), values.data(), a.data.size());
+  attrs_.push_back(a);
+}
+
+void Writer::dataset_double(const std::string& name, const std::vector<uint64_t>& dims, const double* data) {
+  uint64_t cnt = 1;
+  for (uint64_t d : dims) cnt *= d;
+  Dset d{name, dims, {}};
+  d.data.resize(cnt * 8);
+  if (cnt) std::memcpy(d.data.data(), data, d.data.size());
+  dsets_.push_back(d);
+}
+
+bool Writer::write(const std::string& path, std::string& err) const {
+  if (dsets_.size() > 8) { err = "HDF5 writer: at most 8 datasets"; return false; }
+  const int leafK = 4, internK = 16;
+  // local heap data segment: "" at 0, the dataset names in symbol-table (sorted) order, a free block
+  std::vector<size_t> order(dsets_.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+  std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return dsets_[a].name < dsets_[b].name; });
+  Buf heapseg;
+  heapseg.u(0, 8);
+  std::vector<size_t> name_off(dsets_.size());
+  for (size_t i : order) {
+    name_off[i] = heapseg.b.size();
+    heapseg.bytes(std::vector<uint8_t>(dsets_[i].name.begin(), dsets_[i].name.end()));
+    heapseg.u(0, 1);
+    heapseg.pad8();
+  }
+  const size_t free_off = heapseg.b.size();
+  heapseg.u(1, 8);   // next free block: none (H5HL_FREE_NULL)
+  heapseg.u(16, 8);  // size of this free block
+  // root object header: symbol table message + attribute messages
+  const size_t sb_size = 96;
+  Buf rootmsgs;
+  message(rootmsgs, 0x11, 0, std::vector<uint8_t>(16, 0));  // patched below
+  for (const Attr& a : attrs_) {
+    Buf body;
+    const std::vector<uint8_t> sp = space(a.dims);
+    body.u(1, 1); body.u(0, 1); body.u(a.name.size() + 1, 2); body.u(a.type.size(), 2); body.u(sp.size(), 2);
+    body.bytes(std::vector<uint8_t>(a.name.begin(), a.name.end())); body.u(0, 1); body.pad8();
+    body.bytes(a.type); body.pad8();
+    body.bytes(sp); body.pad8();
+    body.bytes(a.data);
+    if (body.b.size() > 65535 - 8) { err = "HDF5 writer: attribute " + a.name + " too large"; return false; }
+    message(rootmsgs, 0x0c, 0, body.b);
+  }
+  const size_t root_addr = sb_size;
+  const size_t root_size = 16 + rootmsgs.b.size();
+  const size_t heap_addr = pad8(root_addr + root_size);
+  const size_t heapseg_addr = heap_addr + 32;
+  const size_t btree_addr = pad8(heapseg_addr + heapseg.b.size());
+  const size_t btree_size = 24 + (2 * internK + 1) * 8 + 2 * internK * 8;
+  const size_t snod_addr = btree_addr + btree_size;
+  const size_t snod_size = 8 + 2 * leafK * 40;
+  // dataset object headers, then the data
+  size_t at = pad8(snod_addr + snod_size);
+  std::vector<size_t> oh_addr(dsets_.size()), oh_size(dsets_.size());
+  for (size_t i = 0; i < dsets_.size(); ++i) {
+    // dataspace, datatype, fill value v2 (late allocation, fill written if set, default value),
+    // layout v3 contiguous: 8-byte headers + padded bodies
+    oh_size[i] = 16 + (8 + pad8(space(dsets_[i].dims).size())) + (8 + 24) + (8 + 8) + (8 + 24);
+    oh_addr[i] = at;
+    at = pad8(at + oh_size[i]);
+  }
+  std::vector<size_t> data_addr(dsets_.size());
+  for (size_t i = 0; i < dsets_.size(); ++i) {
+    data_addr[i] = at;
+    at = pad8(at + dsets_[i].data.size());
+  }
+  const size_t eof = at;
+  Buf f;
+  f.b.reserve(eof);
+  // superblock v0
+  const uint8_t sig[8] = {0x89, 'H', 'D', 'F', '\r', '\n', 0x1a, '\n'};
+  f.bytes(std::vector<uint8_t>(sig, sig + 8));
+  f.u(0, 1); f.u(0, 1); f.u(0, 1); f.u(0, 1); f.u(0, 1); f.u(8, 1); f.u(8, 1); f.u(0, 1);
+  f.u(leafK, 2); f.u(internK, 2); f.u(0, 4);
+  f.u(0, 8); f.u(kUndefAddr, 8); f.u(eof, 8); f.u(kUndefAddr, 8);
+  // root symbol table entry: name offset, object header, cache type 1 (B-tree and heap cached)
+  f.u(0, 8); f.u(root_addr, 8); f.u(1, 4); f.u(0, 4); f.u(btree_addr, 8); f.u(heap_addr, 8);
+  // root object header (symbol table message body patched)
+  Buf rm = rootmsgs;
+  rm.at(8, btree_addr, 8); rm.at(16, heap_addr, 8);
+  f.bytes(object_header(1 + (int)attrs_.size(), rm.b));
+  while (f.b.size() < heap_addr) f.b.push_back(0);
+  // local heap
+  f.bytes({'H', 'E', 'A', 'P', 0, 0, 0, 0});
+  f.u(heapseg.b.size(), 8); f.u(free_off, 8); f.u(heapseg_addr, 8);
+  f.bytes(heapseg.b);
+  while (f.b.size() < btree_addr) f.b.push_back(0);
+  // B-tree leaf (group node, level 0) with one child, the symbol-table node
+  f.bytes({'T', 'R', 'E', 'E', 0, 0});
+  f.u(dsets_.empty() ? 0 : 1, 2); f.u(kUndefAddr, 8); f.u(kUndefAddr, 8);
+  {
+    Buf kc;
+    if (!dsets_.empty()) {
+      kc.u(0, 8); kc.u(snod_addr, 8); kc.u(name_off[order.back()], 8);
+    }
+    kc.b.resize(btree_size - 24, 0);
+    f.bytes(kc.b);
+  }
+  // symbol-table node, entries sorted by name
+  f.bytes({'S', 'N', 'O', 'D', 1, 0});
+  f.u(dsets_.size(), 2);
+  {
+    Buf ent;
+    for (size_t i : order) { ent.u(name_off[i], 8); ent.u(oh_addr[i], 8); ent.u(0, 4); ent.u(0, 4); ent.u(0, 16); }
+    ent.b.resize(2 * leafK * 40, 0);
+    f.bytes(ent.b);
+  }
+  // dataset object headers
+  for (size_t i = 0; i < dsets_.size(); ++i) {
+    while (f.b.size() < oh_addr[i]) f.b.push_back(0);
+    Buf m;
+    message(m, 0x01, 0, space(dsets_[i].dims));
+    message(m, 0x03, 1, type_double());
+    message(m, 0x05, 1, {2, 2, 2, 1, 0, 0, 0, 0});
+    Buf lay;
+    lay.u(3, 1); lay.u(1, 1); lay.u(data_addr[i], 8); lay.u(dsets_[i].data.size(), 8);
+    message(m, 0x08, 1, lay.b);
+    f.bytes(object_header(4, m.b));
+  }
+  for (size_t i = 0; i < dsets_.size(); ++i) {
+    while (f.b.size() < data_addr[i]) f.b.push_back(0);
+    f.bytes(dsets_[i].data);
+  }
+  while (f.b.size() < eof) f.b.push_back(0);
+  FILE* fp = std::fopen(path.c_str(), "wb");
+  if (!fp) { err = "cannot create " + path; return false; }
+  const size_t w = std::fwrite(f.b.data(), 1, f.b.size(), fp);
+  const bool ok = std::fclose(fp) == 0 && w == f.b.size();
+  if (!ok) { err = "short write of " + path; return false; }
+  return true;
 }
 
 }  // namespace gxh5

@@ -54,4 +54,26 @@ class File {
   uint64_t u(uint64_t off, int n) const;
 };
 
+// Writer for the same subset: superblock version 0 at offset 0, a root group with a symbol table
+// (one v1 B-tree leaf, one symbol-table node, one local heap), version-1 object headers, attribute
+// messages v1 on the root group, contiguous datasets (layout message v3).  The structures mirror the
+// state files FLEXI writes through the HDF5 library (fixed-length space-padded strings, rank-1
+// attributes, maximum dimensions equal to the dimensions).  At most 8 datasets.
+class Writer {
+ public:
+  void attr_string(const std::string& name, const std::string& value);  // length = trimmed length
+  void attr_strings(const std::string& name, const std::vector<std::string>& values, int len);
+  void attr_int(const std::string& name, const std::vector<int32_t>& values);
+  void attr_double(const std::string& name, const std::vector<double>& values);
+  // dims slowest first (HDF5/C order); data copied
+  void dataset_double(const std::string& name, const std::vector<uint64_t>& dims, const double* data);
+  bool write(const std::string& path, std::string& err) const;
+
+ private:
+  struct Attr { std::string name; std::vector<uint8_t> type; std::vector<uint64_t> dims; std::vector<uint8_t> data; };
+  struct Dset { std::string name; std::vector<uint64_t> dims; std::vector<uint8_t> data; };
+  std::vector<Attr> attrs_;
+  std::vector<Dset> dsets_;
+};
+
 }  // namespace gxh5

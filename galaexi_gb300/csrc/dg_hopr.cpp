@@ -379,6 +379,35 @@ extern "C" int dg_h5_read(const char* path, const char* name, int attribute, int
   return DG_OK;
 }
 
+extern "C" int dg_write_state(const char* path, const char* project, const char* mesh_file, int N,
+                              const char* node_type, double time, int nElems, const double* U) {
+  if (!path || !project || !mesh_file || !node_type || !U || N < 1 || nElems < 1) {
+    set_error("dg_write_state: bad argument"); return DG_ERR_ARG;
+  }
+  const uint64_t n = (uint64_t)N + 1;
+  gxh5::Writer w;
+  // the attributes of GenerateFileSkeleton / WriteHeader (io_hdf5/hdf5_output.f90:744-870, 941-961)
+  w.attr_string("Program", "GALAEXI-GB300");
+  w.attr_string("File_Type", "State");
+  w.attr_string("Project_Name", project);
+  w.attr_double("File_Version", {0.1});
+  w.attr_strings("VarNames", {"Density", "MomentumX", "MomentumY", "MomentumZ", "EnergyStagnationDensity"}, 255);
+  w.attr_int("N", {N});
+  w.attr_int("Dimension", {3});
+  w.attr_double("Time", {time});
+  w.attr_string("MeshFile", mesh_file);
+  std::string base(path);
+  const size_t slash = base.find_last_of('/');
+  if (slash != std::string::npos) base = base.substr(slash + 1);
+  w.attr_string("NextFile", base);
+  w.attr_string("NodeType", node_type);
+  // DG_Solution(nVar, 0:N, 0:N, 0:N, nElems) in Fortran order = (nElems, k, j, i, nVar) in HDF5 order
+  w.dataset_double("DG_Solution", {(uint64_t)nElems, n, n, n, 5}, U);
+  std::string err;
+  if (!w.write(path, err)) { set_error(err); return DG_ERR_ARG; }
+  return DG_OK;
+}
+
 extern "C" int dg_mesh_hopr_bcs(const char* path, int* nBCs, char* names, int name_len, int* bc_type) {
   if (!path || !nBCs) { set_error("dg_mesh_hopr_bcs: null argument"); return DG_ERR_ARG; }
   gxh5::File f;

@@ -86,6 +86,25 @@ def read_h5(path, name, attribute=False):
     return out
 
 
+def write_state(path, U, N, node_type, time, mesh_file, project="galaexi_gb300"):
+    """A FLEXI state file (dg_write_state): U of shape (nElems, n, n, n, 5) (host numpy or torch),
+    node_type 1 (Gauss) / 2 (Gauss-Lobatto) or the reference's name."""
+    if hasattr(U, "detach"):
+        U = U.detach().cpu().numpy()
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    if isinstance(node_type, int):
+        node_type = "GAUSS" if node_type == 1 else "GAUSS-LOBATTO"
+    nat.check(nat.lib().dg_write_state(str(path).encode(), str(project).encode(), str(mesh_file).encode(), int(N),
+                                       str(node_type).encode(), float(time), U.shape[0], _ptr(U)), "dg_write_state")
+
+
+def read_state(path):
+    """(U, time, N, node_type, mesh_file) of a FLEXI state file."""
+    U = read_h5(path, "DG_Solution")
+    return (U, float(read_h5(path, "Time", True)[0]), int(read_h5(path, "N", True)[0]),
+            read_h5(path, "NodeType", True), read_h5(path, "MeshFile", True))
+
+
 class Mesh:
     """Periodic hexahedral box with the reference's connectivity and metric arrays.
 

@@ -300,6 +300,13 @@ int dg_mesh_hopr_bcs(const char* path, int* nBCs, char* names, int name_len, int
  * element into str (str_len bytes, NUL-terminated). */
 int dg_h5_read(const char* path, const char* name, int attribute, int* ndims, long long* dims, double* out,
                long long cap, char* str, int str_len);
+/* A FLEXI state file (WriteState, io_hdf5/hdf5_output.f90:84-211): the dataset DG_Solution
+ * (5,0:N,0:N,0:N,nElems) from the host array U, and the root attributes File_Type = 'State',
+ * Project_Name, File_Version, Program, VarNames, N, Dimension, Time, MeshFile, NextFile, NodeType
+ * ('GAUSS' or 'GAUSS-LOBATTO').  The file is written without libhdf5 (HDF5 superblock version 0,
+ * the structures of the reference's own state files). */
+int dg_write_state(const char* path, const char* project, const char* mesh_file, int N, const char* node_type,
+                   double time, int nElems, const double* U);
 int dg_mesh_hopr(const char* path, int N, int node_type, double* elem_xgp, double* metrics_f, double* metrics_g,
                  double* metrics_h, double* sJ, double* nvec, double* t1, double* t2, double* surfelem,
                  int* elem_to_side, int* side_to_elem, int* BCIndex);
