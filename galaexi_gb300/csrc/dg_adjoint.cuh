@@ -99,6 +99,20 @@ __device__ __forceinline__ void visc_close_vjp(const double tau[6], const double
 template <int SPLIT>
 __device__ __forceinline__ void pair_sum_vjp(double rs, double us, double vs, double ws, double ps, double auxs,
                                              double Ms0, double Ms1, double Ms2, const double Fb[5], double sb[6]) {
+  if constexpr (SPLIT == DG_SPLIT_PI) {
+    // Fb arrives scaled by 1/8 (DVolSurf / 8) with its density row doubled (2a staged): every
+    // constant below is folded that way, by powers of two, so the result has the same bits
+    const double Vs = Ms0 * us + Ms1 * vs + Ms2 * ws;
+    const double q8 = rs * Vs;
+    const double qb8 = Fb[0] + Fb[1] * us + Fb[2] * vs + Fb[3] * ws + Fb[4] * auxs;
+    sb[1] = Fb[1] * q8; sb[2] = Fb[2] * q8; sb[3] = Fb[3] * q8;
+    sb[4] = 4. * (Fb[1] * Ms0 + Fb[2] * Ms1 + Fb[3] * Ms2);
+    sb[5] = Fb[4] * q8;
+    const double Vsb = rs * qb8;
+    sb[0] = Vs * qb8;
+    sb[1] += Ms0 * Vsb; sb[2] += Ms1 * Vsb; sb[3] += Ms2 * Vsb;
+    return;
+  }
   const double Vs = Ms0 * us + Ms1 * vs + Ms2 * ws;
   const double q = 0.125 * rs * Vs;
   double qb = 2. * Fb[0] + Fb[1] * us + Fb[2] * vs + Fb[3] * ws + Fb[4] * auxs;
@@ -279,6 +293,11 @@ ka_volume(CotSrc cs, const double* __restrict__ U, const double* __restrict__ Pv
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* const sm = reinterpret_cast<double*>(smem_raw);
   load_basis(sb, basis);
+  if constexpr (SPLIT == DG_SPLIT_PI) {
+    // the 1/8 of the PI pair cotangents folded into DVolSurf (exact scaling, see pair_sum_vjp)
+    __syncthreads();
+    for (int t = threadIdx.x; t < NP * NP; t += blockDim.x) sb.DVS[t] = sb.DVS[t] * 0.125;
+  }
   const int e0 = blockIdx.x * EPB;
   const int nloc = min(EPB, L.nElems - e0);
   const int tid = threadIdx.x;
@@ -286,6 +305,7 @@ ka_volume(CotSrc cs, const double* __restrict__ U, const double* __restrict__ Pv
   const int el = tid / n3, node = tid - (tid / n3) * n3;
   const int e = e0 + el;
   const int i = node % n, j = (node / n) % n, k = node / n2;
+  const int snode = vsw<NP>(node);  // shared-memory position of this node (conflict-free at N=7)
   double* Aa = sm + (size_t)el * 38 * n3;  // [5][n3]   a = -sJ Ut_bar
   double* Bs = Aa + 5 * n3;                // [15][n3]  node data (split), later gradient cotangents
   double* Cs = Aa + 20 * n3;               // [18][n3]  pair-sum cotangents (3 dirs x 6), later lifting weights
@@ -300,20 +320,23 @@ ka_volume(CotSrc cs, const double* __restrict__ U, const double* __restrict__ Pv
     cot_at(cs, gU, ub);
     const double sj = M[9 * n3];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) Aa[v * n3 + node] = -sj * ub[v];
+    for (int v = 0; v < 5; ++v) Aa[v * n3 + snode] = -sj * ub[v];
+    // PI: the density row is staged doubled (exact), as pair_sum_vjp expects; the split forms' viscous
+    // part (phase C) reads the momentum and energy rows only
+    if constexpr (SPLIT == DG_SPLIT_PI) Aa[snode] = 2. * Aa[snode];
     if constexpr (SPLIT >= 0) {
       const double E = U[gU + 4];
       const double rho = P[0], uu = P[n3], vv = P[2 * n3], ww = P[3 * n3], pm = P[4 * n3];
-      Bs[0 * n3 + node] = rho;
-      Bs[1 * n3 + node] = uu;
-      Bs[2 * n3 + node] = vv;
-      Bs[3 * n3 + node] = ww;
-      Bs[4 * n3 + node] = pm;
-      Bs[5 * n3 + node] = pair_aux<SPLIT, double>(rho, uu, vv, ww, E, pm, P[6 * n3]);
+      Bs[0 * n3 + snode] = rho;
+      Bs[1 * n3 + snode] = uu;
+      Bs[2 * n3 + snode] = vv;
+      Bs[3 * n3 + snode] = ww;
+      Bs[4 * n3 + snode] = pm;
+      Bs[5 * n3 + snode] = pair_aux<SPLIT, double>(rho, uu, vv, ww, E, pm, P[6 * n3]);
 #pragma unroll
-      for (int c = 0; c < 9; ++c) Bs[(6 + c) * n3 + node] = M[c * n3];
+      for (int c = 0; c < 9; ++c) Bs[(6 + c) * n3 + snode] = M[c * n3];
 #pragma unroll
-      for (int c = 0; c < 18; ++c) Cs[c * n3 + node] = 0.;
+      for (int c = 0; c < 18; ++c) Cs[c * n3 + snode] = 0.;
     }
   }
   __syncthreads();
@@ -335,7 +358,7 @@ ka_volume(CotSrc cs, const double* __restrict__ U, const double* __restrict__ Pv
       const int mc = 6 + 3 * dir;
 #pragma unroll 1
       for (int a = 0; a < NP - 1; ++a) {
-        const int na = base + a * stride;
+        const int na = vsw<NP>(base + a * stride);
         const double ra = Bl[na], ua = Bl[n3 + na], va = Bl[2 * n3 + na], wa = Bl[3 * n3 + na],
                      pa = Bl[4 * n3 + na], xa = Bl[5 * n3 + na];
         const double ma0 = Bl[mc * n3 + na], ma1 = Bl[(mc + 1) * n3 + na], ma2 = Bl[(mc + 2) * n3 + na];
@@ -347,7 +370,7 @@ ka_volume(CotSrc cs, const double* __restrict__ U, const double* __restrict__ Pv
         for (int c = 0; c < 6; ++c) acc[c] = Cl[c * n3 + na];
 #pragma unroll 4
         for (int b = a + 1; b < NP; ++b) {
-          const int nb = base + b * stride;
+          const int nb = vsw<NP>(base + b * stride);
           const double dba = sb.DVS[b + n * a], dab = sb.DVS[a + n * b];
           double Fb[5];
 #pragma unroll
@@ -378,7 +401,7 @@ ka_volume(CotSrc cs, const double* __restrict__ U, const double* __restrict__ Pv
     if constexpr (SPLIT >= 0) {
       double s6[6];
 #pragma unroll
-      for (int c = 0; c < 6; ++c) s6[c] = Cs[c * n3 + node] + Cs[(6 + c) * n3 + node] + Cs[(12 + c) * n3 + node];
+      for (int c = 0; c < 6; ++c) s6[c] = Cs[c * n3 + snode] + Cs[(6 + c) * n3 + snode] + Cs[(12 + c) * n3 + snode];
       rb = s6[0]; ub_ = s6[1]; vb = s6[2]; wb = s6[3]; pb = s6[4]; xb = s6[5];
     }
     if (SPLIT < 0 || PARAB) {
@@ -392,7 +415,7 @@ ka_volume(CotSrc cs, const double* __restrict__ U, const double* __restrict__ Pv
 #pragma unroll
       for (int l = 0; l < n; ++l) {
         const double ci = sb.DhatT[i + n * l], cj = sb.DhatT[j + n * l], ck = sb.DhatT[k + n * l];
-        const int ni = l + n * (j + n * k), nj = i + n * (l + n * k), nk = i + n * (j + n * l);
+        const int ni = vsw<NP>(l + n * (j + n * k)), nj = vsw<NP>(i + n * (l + n * k)), nk = vsw<NP>(i + n * (j + n * l));
 #pragma unroll
         for (int v = v0; v < 5; ++v) {
           flb[0][v] += ci * Aa[v * n3 + ni];
@@ -477,19 +500,19 @@ ka_volume(CotSrc cs, const double* __restrict__ U, const double* __restrict__ Pv
     }
     const double sj = M[9 * n3];
 #pragma unroll
-    for (int c = 0; c < 15; ++c) Bs[c * n3 + node] = gb[c];
+    for (int c = 0; c < 15; ++c) Bs[c * n3 + snode] = gb[c];
     if (L.lift_mode == 0) {
       // h_dir[v] = sJ sum_d Mdir_d Gbar_d[v]
 #pragma unroll
       for (int dir = 0; dir < 3; ++dir) {
         const double m0 = sj * M[(3 * dir) * n3], m1 = sj * M[(3 * dir + 1) * n3], m2 = sj * M[(3 * dir + 2) * n3];
 #pragma unroll
-        for (int v = 0; v < 5; ++v) Cs[(dir * 5 + v) * n3 + node] = m0 * gb[v] + m1 * gb[5 + v] + m2 * gb[10 + v];
+        for (int v = 0; v < 5; ++v) Cs[(dir * 5 + v) * n3 + snode] = m0 * gb[v] + m1 * gb[5 + v] + m2 * gb[10 + v];
       }
     } else {
       // conservative: h'_d[v] = sJ Gbar_d[v]
 #pragma unroll
-      for (int c = 0; c < 15; ++c) Cs[c * n3 + node] = sj * gb[c];
+      for (int c = 0; c < 15; ++c) Cs[c * n3 + snode] = sj * gb[c];
     }
   }
   __syncthreads();
@@ -502,7 +525,8 @@ ka_volume(CotSrc cs, const double* __restrict__ U, const double* __restrict__ Pv
 #pragma unroll
         for (int l = 0; l < n; ++l) {
           const double ci = sb.D[l + n * i], cj = sb.D[l + n * j], ck = sb.D[l + n * k];
-          const int ni = l + n * (j + n * k), nj = i + n * (l + n * k), nk = i + n * (j + n * l);
+          const int ni = vsw<NP>(l + n * (j + n * k)), nj = vsw<NP>(i + n * (l + n * k)),
+                    nk = vsw<NP>(i + n * (j + n * l));
 #pragma unroll
           for (int v = 0; v < 5; ++v)
             lb[v] += ci * Cs[v * n3 + ni] + cj * Cs[(5 + v) * n3 + nj] + ck * Cs[(10 + v) * n3 + nk];
@@ -516,7 +540,7 @@ ka_volume(CotSrc cs, const double* __restrict__ U, const double* __restrict__ Pv
 #pragma unroll
           for (int l = 0; l < n; ++l) {
             const double c = sb.D[l + n * ii];
-            const int nx = dir == 0 ? l + n * (j + n * k) : (dir == 1 ? i + n * (l + n * k) : i + n * (j + n * l));
+            const int nx = vsw<NP>(dir == 0 ? l + n * (j + n * k) : (dir == 1 ? i + n * (l + n * k) : i + n * (j + n * l)));
 #pragma unroll
             for (int v = 0; v < 5; ++v)
               lb[v] += c * (m0 * Cs[v * n3 + nx] + m1 * Cs[(5 + v) * n3 + nx] + m2 * Cs[(10 + v) * n3 + nx]);
@@ -573,11 +597,11 @@ ka_volume(CotSrc cs, const double* __restrict__ U, const double* __restrict__ Pv
       const int l0 = L.gauss ? 0 : (minus ? 0 : N), l1 = L.gauss ? N : l0;
       for (int l = l0; l <= l1; ++l) {
         const double Lh = L.gauss ? (minus ? sb.Lhm[l] : sb.Lhp[l]) : (minus ? sb.Lhm[0] : sb.Lhp[N]);
-        const int x = face_node(n, ls, a, b, l);
+        const int x = face_node(n, ls, a, b, l), sx = vsw<NP>(x);
         const double w = Lh * hse * sJe[x];
 #pragma unroll
         for (int v = 0; v < 5; ++v)
-          jb[v] += w * (nv[0] * Bl[v * n3 + x] + nv[1] * Bl[(5 + v) * n3 + x] + nv[2] * Bl[(10 + v) * n3 + x]);
+          jb[v] += w * (nv[0] * Bl[v * n3 + sx] + nv[1] * Bl[(5 + v) * n3 + sx] + nv[2] * Bl[(10 + v) * n3 + sx]);
       }
       double* out = JB + ((size_t)(flip == 0 ? 0 : 1) * L.nSides + side) * 5 * n2 + pq;
 #pragma unroll

@@ -258,7 +258,9 @@ int adj(dg_ctx* ctx, const double* U, gx::CotSrc cs, int mode, double* Uout, dou
   }
   const dg_config& c = ctx->cfg;
   const gx::Gas<double> gas = gxc::make_gas<double>(c, 0.);
-  rhs_front<double>(ctx, ctx->d, U, gas, st, nullptr, false);
+  // the state's primitives, traces and lifted gradients (no flux reads the density gradient)
+  rhs_front<double, double, 1>(ctx, ctx->d, U, gas, st, nullptr, false);
+  ctx->grad_rho = false;
   gx::AdjLaunch AL;
   AL.nElems = ctx->nElems; AL.nSides = ctx->nSides;
   AL.gauss = c.node_type == DG_NODETYPE_GAUSS ? 1 : 0;
