@@ -893,18 +893,28 @@ int dg_adjoint_forward(dg_ctx* ctx, double t0, double dt, int nSteps, const doub
   }
   if (!plan) { set_error("dg_adjoint_forward: checkpoint budget too small for this window"); return DG_ERR_ALLOC; }
   if (!T.store.alloc(slots * S)) { set_error("cudaMalloc checkpoints"); return DG_ERR_ALLOC; }
+  // the first segment is the short one, so that the last segment, whose checkpoints this sweep
+  // records directly (the reverse sweep starts there and recomputes nothing for it), has k steps
   T.plan = plan; T.k = k; T.nSeg = nSeg; T.nSteps = nSteps; T.t0 = t0; T.dt = dt; T.state = S;
+  T.r = nSteps - (nSeg - 1) * k;
   double* W = ctx->W.p;
   double* K = ctx->K.p;
+  double* buf = T.store.p + (size_t)nSeg * S;  // plans 2 and 3: the buffer of one segment
+  const int nL = T.seg_start(nSeg - 1);
   CUDA_TRY(cudaMemcpyAsync(W, d_U0, bytes, cudaMemcpyDeviceToDevice, st), "copy U0");
   CUDA_TRY(cudaMemsetAsync(K, 0, bytes, st), "clear K");
   for (int nstep = 0; nstep < nSteps; ++nstep) {
-    if (plan != 1 && nstep % k == 0)
-      CUDA_TRY(cudaMemcpyAsync(T.store.p + (size_t)(nstep / k) * S, W, bytes, cudaMemcpyDeviceToDevice, st), "checkpoint");
+    const int sg = T.seg_of(nstep);
+    if (plan != 1 && nstep == T.seg_start(sg))
+      CUDA_TRY(cudaMemcpyAsync(T.store.p + (size_t)sg * S, W, bytes, cudaMemcpyDeviceToDevice, st), "checkpoint");
+    if (plan == 3 && nstep >= nL)
+      CUDA_TRY(cudaMemcpyAsync(buf + (size_t)(nstep - nL) * S, W, bytes, cudaMemcpyDeviceToDevice, st), "step start");
     for (int stage = 1; stage <= 5; ++stage) {
-      if (plan == 1)
-        CUDA_TRY(cudaMemcpyAsync(T.store.p + ((size_t)nstep * 5 + stage - 1) * S, W, bytes, cudaMemcpyDeviceToDevice, st),
-                 "stage checkpoint");
+      double* slot = nullptr;
+      if (plan == 1) slot = T.store.p + ((size_t)nstep * 5 + stage - 1) * S;
+      else if (plan == 2 && nstep >= nL) slot = buf + ((size_t)(nstep - nL) * 5 + stage - 1) * S;
+      else if (plan == 3 && nstep == nSteps - 1) slot = buf + ((size_t)k + stage - 1) * S;
+      if (slot) CUDA_TRY(cudaMemcpyAsync(slot, W, bytes, cudaMemcpyDeviceToDevice, st), "stage checkpoint");
       if (int rc = fwd_stage(ctx, stage, dt, W, K, st)) return rc;
     }
   }
@@ -938,10 +948,13 @@ int dg_adjoint_reverse(dg_ctx* ctx, double* d_Ubar, double* mu_bar, void* stream
     double* seg = T.store.p;
     double* buf = T.store.p + (size_t)T.nSeg * S;  // plan 2: 5k stage inputs; plan 3: k step starts + 5 stage inputs
     for (int sg = T.nSeg - 1; sg >= 0 && rc == DG_OK; --sg) {
-      const int n0 = sg * T.k, n1 = (n0 + T.k < T.nSteps) ? n0 + T.k : T.nSteps;
-      CUDA_TRY(cudaMemcpyAsync(W, seg + (size_t)sg * S, bytes, cudaMemcpyDeviceToDevice, st), "restore");
-      CUDA_TRY(cudaMemsetAsync(K2.p, 0, bytes, st), "clear");
-      for (int nstep = n0; nstep < n1 && rc == DG_OK; ++nstep) {
+      const int n0 = T.seg_start(sg), n1 = T.seg_end(sg);
+      const bool last = sg == T.nSeg - 1;  // recorded by the forward sweep
+      if (!last) {
+        CUDA_TRY(cudaMemcpyAsync(W, seg + (size_t)sg * S, bytes, cudaMemcpyDeviceToDevice, st), "restore");
+        CUDA_TRY(cudaMemsetAsync(K2.p, 0, bytes, st), "clear");
+      }
+      for (int nstep = n0; nstep < n1 && rc == DG_OK && !last; ++nstep) {
         if (T.plan == 3)
           CUDA_TRY(cudaMemcpyAsync(buf + (size_t)(nstep - n0) * S, W, bytes, cudaMemcpyDeviceToDevice, st), "step start");
         for (int stage = 1; stage <= 5 && rc == DG_OK; ++stage) {
@@ -955,13 +968,17 @@ int dg_adjoint_reverse(dg_ctx* ctx, double* d_Ubar, double* mu_bar, void* stream
         const double* X = nullptr;
         if (T.plan == 3) {
           double* sbuf = buf + (size_t)T.k * S;
-          CUDA_TRY(cudaMemcpyAsync(W, buf + (size_t)(nstep - n0) * S, bytes, cudaMemcpyDeviceToDevice, st), "restore step");
-          CUDA_TRY(cudaMemsetAsync(K2.p, 0, bytes, st), "clear");
-          for (int stage = 1; stage <= 4 && rc == DG_OK; ++stage) {
-            CUDA_TRY(cudaMemcpyAsync(sbuf + (size_t)(stage - 1) * S, W, bytes, cudaMemcpyDeviceToDevice, st), "stage input");
-            rc = fwd_stage(ctx, stage, dt, W, K2.p, st);
+          if (nstep != T.nSteps - 1) {  // the last step's stage inputs were recorded by the forward sweep
+            CUDA_TRY(cudaMemcpyAsync(W, buf + (size_t)(nstep - n0) * S, bytes, cudaMemcpyDeviceToDevice, st),
+                     "restore step");
+            CUDA_TRY(cudaMemsetAsync(K2.p, 0, bytes, st), "clear");
+            for (int stage = 1; stage <= 4 && rc == DG_OK; ++stage) {
+              CUDA_TRY(cudaMemcpyAsync(sbuf + (size_t)(stage - 1) * S, W, bytes, cudaMemcpyDeviceToDevice, st),
+                       "stage input");
+              rc = fwd_stage(ctx, stage, dt, W, K2.p, st);
+            }
+            CUDA_TRY(cudaMemcpyAsync(sbuf + (size_t)4 * S, W, bytes, cudaMemcpyDeviceToDevice, st), "stage input");
           }
-          CUDA_TRY(cudaMemcpyAsync(sbuf + (size_t)4 * S, W, bytes, cudaMemcpyDeviceToDevice, st), "stage input");
           for (int stage = 5; stage >= 1 && rc == DG_OK; --stage)
             rc = rev_stage(ctx, stage, dt, sbuf + (size_t)(stage - 1) * S, d_Ubar, Kbar, st);
           continue;

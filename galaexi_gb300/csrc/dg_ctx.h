@@ -75,10 +75,14 @@ struct AdjTape {
   int plan = 0;                 // 1: all stage inputs, 2: segment starts + stage inputs of one segment,
                                 // 3: segment starts + step starts of one segment + stage inputs of one step
   int nSteps = 0, k = 0, nSeg = 0;
+  int r = 0;                    // steps of the first segment (1..k); the other segments have k steps
   double t0 = 0., dt = 0.;
   gxc::DBuf<double> store;      // checkpoint slots, each one state
   size_t state = 0;             // doubles per state
   bool ok = false;
+  int seg_of(int nstep) const { return nstep < r ? 0 : 1 + (nstep - r) / k; }
+  int seg_start(int sg) const { return sg == 0 ? 0 : r + (sg - 1) * k; }
+  int seg_end(int sg) const { return sg == nSeg - 1 ? nSteps : seg_start(sg + 1); }
 };
 
 struct dg_ctx {

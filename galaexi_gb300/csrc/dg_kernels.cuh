@@ -107,6 +107,9 @@ struct Launch {
 };
 
 template <int NP> struct EPBof { static constexpr int v = (NP * NP * NP >= 128) ? 1 : (256 / (NP * NP * NP)); };
+// k_lift: shared-memory slots per element of the region that holds the lifted primitives (5 n^3) and
+// later the surface flux vectors of one normal direction (2 faces x 15 x n^2)
+__host__ __device__ constexpr int lift_ps_slots(int NP) { return 5 * NP * NP * NP > 30 * NP * NP ? 5 * NP * NP * NP : 30 * NP * NP; }
 
 // =====================================================================================
 // k_prolong: ConsToPrim_Volume + ProlongToFace_CUDA + GetPrimitiveStateSurface (at least two
@@ -223,7 +226,7 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
   __shared__ SBasis<NP, R> sb;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   R (*Ps)[5][n3] = reinterpret_cast<R (*)[5][n3]>(smem_raw);                                   // [EPB][5][n3]
-  R (*Gs)[15][n3] = reinterpret_cast<R (*)[15][n3]>(smem_raw + sizeof(R) * (size_t)EPB * 5 * n3); // [EPB][15][n3]
+  R (*Gs)[15][n3] = reinterpret_cast<R (*)[15][n3]>(smem_raw + sizeof(R) * (size_t)EPB * lift_ps_slots(NP)); // [EPB][15][n3]
   load_basis(sb, basis);
   const int e0 = blockIdx.x * EPB;
   const int nloc = min(EPB, L.nElems - e0);
@@ -236,13 +239,16 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
     Ps[el][c][node] = Pvol[(size_t)(e0 + el) * 7 * n3 + liftc[c] * n3 + node];
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < nloc * n3; t += blockDim.x) {
-    const int el = t / n3, node = t - el * n3;
-    const int e = e0 + el;
-    const int i = node % n, j = (node / n) % n, k = node / n2;
+  // thread per (element, node): the block has EPB * n^3 threads
+  const int el = threadIdx.x / n3, node = threadIdx.x - el * n3;
+  const bool act = el < nloc;
+  const int e = e0 + el;
+  const int i = node % n, j = (node / n) % n, k = node / n2;
+  R g[3][5];
+  R sj = R(0);
+  if (act) {
     const R* M = Met + (size_t)e * 10 * n3 + node;
-    const R sj = M[9 * n3];
-    R g[3][5];
+    sj = M[9 * n3];
     if (L.lift_mode == 0) {
       // Lifting_VolInt_Nonconservative_GPU_Kernel (lifting_volint.t90:262-328), with the Jacobian of
       // the surface integral (surfint.t90:718-723) folded into the metric terms
@@ -286,72 +292,18 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
         for (int v = V0; v < 5; ++v) g[d][v] = sj * g[d][v];
       }
     }
-    if (L.br2) {
+    if (L.br2 || facepass) {
       // BR2: the face traces prolong the volume part only (ApplyJacobianLifting before
-      // ProlongToFaceLifting, lifting_br2.t90:120-147)
+      // ProlongToFaceLifting, lifting_br2.t90:120-147); Gauss-Lobatto BR1: the surface part is added
+      // to the shared copy by face-node threads below
 #pragma unroll
       for (int d = 0; d < 3; ++d)
 #pragma unroll
         for (int v = V0; v < 5; ++v) Gs[el][d * 5 + v][node] = g[d][v];
     }
-    if (facepass) {
-      // Gauss-Lobatto BR1: the surface part is added below by face-node threads
-#pragma unroll
-      for (int d = 0; d < 3; ++d)
-#pragma unroll
-        for (int v = V0; v < 5; ++v) Gs[el][d * 5 + v][node] = g[d][v];
-      continue;
-    }
-    // surface part (SurfInt_Device_Single_Flux, surfint.t90:591-725) of the BR1 flux
-    // 0.5*SurfElem*(sig*U_master + U_slave) (Lifting_FillFlux, lifting_fillflux.t90:39-103) times the
-    // normal (Lifting_FillFlux_NormVec, :212-256) times L_hat and the Jacobian; the scalar factors of
-    // one face are folded into one weight.
-#pragma unroll
-    for (int ls = 1; ls <= 6; ++ls) {
-      int a, b, l;
-      switch (ls) {
-        case L_XI_MINUS: case L_XI_PLUS: a = j; b = k; l = i; break;
-        case L_ETA_MINUS: case L_ETA_PLUS: a = i; b = k; l = j; break;
-        default: a = i; b = j; l = k; break;
-      }
-      const bool minus = is_minus(ls);
-      R Lhat;
-      if (L.gauss) Lhat = minus ? sb.Lhm[l] : sb.Lhp[l];
-      else {
-        if (l != (minus ? 0 : N)) continue;
-        Lhat = minus ? sb.Lhm[0] : sb.Lhp[N];
-      }
-      const int side = E2S[(e * 6 + ls - 1) * 2 + 0];
-      const int flip = E2S[(e * 6 + ls - 1) * 2 + 1];
-      int p, q;
-      s2v2_inv(N, a, b, flip, ls, p, q);
-      const int pq = p + n * q;
-      const R* pm = Pf + (size_t)side * 6 * n2 + pq;
-      const R* ps = Pf + ((size_t)L.nSides + side) * 6 * n2 + pq;
-      const R* fg = Fgeo + (size_t)side * 10 * n2 + pq;
-      const R sig = (L.lift_mode == 2) ? ((flip == 0) ? R(1) : R(-1)) : R(1);
-      const R wgt = sig * Lhat * R(0.5) * fg[9 * n2] * sj;
-      const R nvv[3] = {wgt * fg[0], wgt * fg[n2], wgt * fg[2 * n2]};
-#pragma unroll
-      for (int v = V0; v < 5; ++v) {
-        const int c = liftc[v];
-        const R fl = sigflux * pm[c * n2] + ps[c * n2];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) g[d][v] = g[d][v] + fl * nvv[d];
-      }
-    }
-    R* G = Gvol + (size_t)e * 15 * n3 + node;
-#pragma unroll
-    for (int d = 0; d < 3; ++d)
-#pragma unroll
-      for (int v = V0; v < 5; ++v) {
-        const R val = g[d][v];
-        if (!L.br2) Gs[el][d * 5 + v][node] = val;
-        G[(d * 5 + v) * n3] = val;
-      }
   }
-  __syncthreads();
   if (facepass) {
+    __syncthreads();
     // surface part on Gauss-Lobatto nodes, one thread per face node, one normal direction per pass
     // (the two faces of a direction share no node); only face nodes do surface work, so no warp
     // executes the side bodies of nodes that are not on that face
@@ -389,14 +341,85 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
       }
       __syncthreads();
     }
-    for (int t = threadIdx.x; t < nloc * n3; t += blockDim.x) {
-      const int el = t / n3, node = t - el * n3;
-      R* G = Gvol + (size_t)(e0 + el) * 15 * n3 + node;
+    if (act) {
+      R* G = Gvol + (size_t)e * 15 * n3 + node;
 #pragma unroll
       for (int c = 0; c < 15; ++c)
         if (c % 5 >= V0) G[c * n3] = Gs[el][c][node];
     }
+  } else {
+    // surface part (SurfInt_Device_Single_Flux, surfint.t90:591-725) of the BR1 flux
+    // 0.5*SurfElem*(sig*U_master + U_slave) (Lifting_FillFlux, lifting_fillflux.t90:39-103) times the
+    // normal (Lifting_FillFlux_NormVec, :212-256), times L_hat and the Jacobian.  One normal direction
+    // per pass: the threads of the two faces' nodes put the flux vectors F = 0.5*SurfElem*flux*n of
+    // their node into shared memory (over the lifted primitives, which are no longer read), then every
+    // node adds sJ*(Lhat_minus(l)*F_minus + Lhat_plus(l)*F_plus) of its line (Gauss nodes) or of its
+    // face (Gauss-Lobatto nodes, BR2).  Each face node's data is read from global memory once.
+    R (*Fs)[2][15][n2] = reinterpret_cast<R (*)[2][15][n2]>(smem_raw);  // [EPB][minus/plus][15][n2]
+#pragma unroll 1
+    for (int dir = 0; dir < 3; ++dir) {
+      __syncthreads();
+      for (int t = threadIdx.x; t < nloc * 2 * n2; t += blockDim.x) {
+        const int fe = t / (2 * n2), r = t - fe * 2 * n2;
+        const int mp = r < n2 ? 0 : 1;
+        const int ab = r - mp * n2;
+        const int a = ab % n, b = ab / n;
+        const int ls = dir == 0 ? (mp == 0 ? L_XI_MINUS : L_XI_PLUS)
+                                : (dir == 1 ? (mp == 0 ? L_ETA_MINUS : L_ETA_PLUS) : (mp == 0 ? L_ZETA_MINUS : L_ZETA_PLUS));
+        const int ef = e0 + fe;
+        const int side = E2S[(ef * 6 + ls - 1) * 2 + 0];
+        const int flip = E2S[(ef * 6 + ls - 1) * 2 + 1];
+        int p, q;
+        s2v2_inv(N, a, b, flip, ls, p, q);
+        const int pq = p + n * q;
+        const R* pm = Pf + (size_t)side * 6 * n2 + pq;
+        const R* ps = Pf + ((size_t)L.nSides + side) * 6 * n2 + pq;
+        const R* fg = Fgeo + (size_t)side * 10 * n2 + pq;
+        const R sig = (L.lift_mode == 2) ? ((flip == 0) ? R(1) : R(-1)) : R(1);
+        const R wgt = sig * R(0.5) * fg[9 * n2];
+        const R nvv[3] = {wgt * fg[0], wgt * fg[n2], wgt * fg[2 * n2]};
+#pragma unroll
+        for (int v = V0; v < 5; ++v) {
+          const int c = liftc[v];
+          const R fl = sigflux * pm[c * n2] + ps[c * n2];
+#pragma unroll
+          for (int d = 0; d < 3; ++d) Fs[fe][mp][d * 5 + v][ab] = fl * nvv[d];
+        }
+      }
+      __syncthreads();
+      if (act) {
+        const int a = dir == 0 ? j : i, b = dir == 2 ? j : k, l = dir == 0 ? i : (dir == 1 ? j : k);
+        const int ab = a + n * b;
+        if (L.gauss) {
+          const R cm = sj * sb.Lhm[l], cp = sj * sb.Lhp[l];
+#pragma unroll
+          for (int d = 0; d < 3; ++d)
+#pragma unroll
+            for (int v = V0; v < 5; ++v)
+              g[d][v] = g[d][v] + cm * Fs[el][0][d * 5 + v][ab] + cp * Fs[el][1][d * 5 + v][ab];
+        } else if (l == 0 || l == N) {
+          const int mp = l == 0 ? 0 : 1;
+          const R cf = sj * (l == 0 ? sb.Lhm[0] : sb.Lhp[N]);
+#pragma unroll
+          for (int d = 0; d < 3; ++d)
+#pragma unroll
+            for (int v = V0; v < 5; ++v) g[d][v] = g[d][v] + cf * Fs[el][mp][d * 5 + v][ab];
+        }
+      }
+    }
+    if (act) {
+      R* G = Gvol + (size_t)e * 15 * n3 + node;
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int v = V0; v < 5; ++v) {
+          const R val = g[d][v];
+          if (!L.br2) Gs[el][d * 5 + v][node] = val;
+          G[(d * 5 + v) * n3] = val;
+        }
+    }
   }
+  __syncthreads();
   // ProlongToFaceLifting
   for (int t = threadIdx.x; t < nloc * 6 * n2; t += blockDim.x) {
     int el = t / (6 * n2), r = t - el * 6 * n2;
@@ -859,36 +882,50 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
 #pragma unroll
     for (int v = 0; v < 5; ++v) ut[v] = Ae[v * n3 + snode];
   }
-  if (!active) return;
+  if constexpr (SPLIT < 0) {
+    static_assert(30 * n2 <= NA * n3, "face fluxes of six faces fit the staging area");
+    if (L.gauss) {
+      // Gauss nodes: every node of a line gets L_hat(l) times the flux of the line's two faces.  The
+      // fluxes of the element block's six faces (slave sides negated) are put into the staging area
+      // once, 30 n^2 <= 15 n^3 slots per element, and the nodes read them from there.
+      __syncthreads();  // every read of the staging area is complete
+      for (int t = threadIdx.x; t < nloc * 6 * n2; t += blockDim.x) {
+        const int el2 = t / (6 * n2), r = t - el2 * 6 * n2;
+        const int ls = r / n2 + 1, ab = r - (ls - 1) * n2;
+        const int a = ab % n, b = ab / n;
+        const int e2 = e0 + el2;
+        const int side = E2S[(e2 * 6 + ls - 1) * 2 + 0];
+        const int flip = E2S[(e2 * 6 + ls - 1) * 2 + 1];
+        int p, q;
+        s2v2_inv(N, a, b, flip, ls, p, q);
+        const R* fx = Flux + (size_t)side * 5 * n2 + p + n * q;
+        R* Fv = A + (size_t)el2 * NA * n3 + (ls - 1) * 5 * n2 + ab;
+        if (flip == 0) {
 #pragma unroll
-  for (int ls = 1; ls <= 6; ++ls) {
-    if (!L.gauss) break;
-    int a, b, l;
-    switch (ls) {
-      case L_XI_MINUS: case L_XI_PLUS: a = j; b = k; l = i; break;
-      case L_ETA_MINUS: case L_ETA_PLUS: a = i; b = k; l = j; break;
-      default: a = i; b = j; l = k; break;
-    }
-    const bool minus = is_minus(ls);
-    R Lhat;
-    if (L.gauss) Lhat = minus ? sb.Lhm[l] : sb.Lhp[l];
-    else {
-      if (l != (minus ? 0 : N)) continue;
-      Lhat = minus ? sb.Lhm[0] : sb.Lhp[N];
-    }
-    const int side = E2S[(e * 6 + ls - 1) * 2 + 0];
-    const int flip = E2S[(e * 6 + ls - 1) * 2 + 1];
-    int p, q;
-    s2v2_inv(N, a, b, flip, ls, p, q);
-    const R* fx = Flux + (size_t)side * 5 * n2 + p + n * q;
-    if (flip == 0) {
+          for (int v = 0; v < 5; ++v) Fv[v * n2] = fx[v * n2];
+        } else {
 #pragma unroll
-      for (int v = 0; v < 5; ++v) ut[v] = ut[v] + fx[v * n2] * Lhat;
-    } else {
+          for (int v = 0; v < 5; ++v) Fv[v * n2] = -fx[v * n2];
+        }
+      }
+      __syncthreads();
+      if (!active) return;
 #pragma unroll
-      for (int v = 0; v < 5; ++v) ut[v] = ut[v] - fx[v * n2] * Lhat;
+      for (int ls = 1; ls <= 6; ++ls) {
+        int a, b, l;
+        switch (ls) {
+          case L_XI_MINUS: case L_XI_PLUS: a = j; b = k; l = i; break;
+          case L_ETA_MINUS: case L_ETA_PLUS: a = i; b = k; l = j; break;
+          default: a = i; b = j; l = k; break;
+        }
+        const R Lhat = is_minus(ls) ? sb.Lhm[l] : sb.Lhp[l];
+        const R* Fv = Ae + (ls - 1) * 5 * n2 + a + n * b;
+#pragma unroll
+        for (int v = 0; v < 5; ++v) ut[v] = ut[v] + Fv[v * n2] * Lhat;
+      }
     }
   }
+  if (!active) return;
   const R sj = Met[(size_t)e * 10 * n3 + 9 * n3 + node];
   const size_t g = ((size_t)e * n3 + node) * 5;
 #pragma unroll

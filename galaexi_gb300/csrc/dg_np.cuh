@@ -28,7 +28,9 @@ constexpr int NT = EPB * NP * NP * NP;  // threads per element block
 template <typename R, int SPL, int PAR> constexpr size_t volume_smem() {
   return sizeof(R) * (size_t)EPB * (gx::vol_stage_slots(SPL, PAR) + (SPL >= 0 ? 15 : 0)) * NP * NP * NP;
 }
-template <typename R> constexpr size_t lift_smem() { return sizeof(R) * (size_t)EPB * 20 * NP * NP * NP; }
+template <typename R> constexpr size_t lift_smem() {
+  return sizeof(R) * (size_t)EPB * (gx::lift_ps_slots(NP) + 15 * NP * NP * NP);
+}
 
 // opt-in shared memory per block of the current device (227 KB on GB300)
 int smem_limit() {

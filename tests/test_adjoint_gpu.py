@@ -152,13 +152,15 @@ def test_window_dot_product():
     op.close()
 
 
-def test_window_checkpoint_plans_agree():
+@pytest.mark.parametrize("nSteps", [12, 13])
+def test_window_checkpoint_plans_agree(nSteps):
+    """Plans 2 and 3 give the bits of plan 1; 13 steps leave a short first segment (plan 2: k = 2,
+    plan 3: k = 3, one step in the first segment)."""
     cfg, m, op, U0, dt, rng = window_case()
-    nSteps = 12
     state = U0.numel() * 8
     ybar = rand_like(rng, U0)
     out = {}
-    for budget in (state * 5 * nSteps, state * 20, state * 12):
+    for budget in (state * 5 * nSteps, state * 20, state * 13):
         _, plan = op.adjoint_forward(dt, nSteps, U0, budget_bytes=budget)
         Ub = ybar.clone()
         mub = op.adjoint_reverse(Ub)
