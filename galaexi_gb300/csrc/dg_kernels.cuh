@@ -121,9 +121,18 @@ k_prolong(const S* __restrict__ U, const int* __restrict__ E2S, const double* __
           const double* __restrict__ Lp, Gas<R> gas, Launch L, R* __restrict__ Pvol, R* __restrict__ Uf,
           R* __restrict__ Pf) {
   constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, EPB = EPBof<NP>::v, N = NP - 1;
+  // mixed form: FP32 copies of density and momenta (converted once per node; Gauss nodes interpolate
+  // them to the faces in FP32), the energy in FP64.  Static shared memory is limited to 48 KB, so N = 9
+  // keeps the plain FP64 interpolation.
+  constexpr bool C32 = OffsetOf<R>::v && (size_t)EPB * n3 * (5 * sizeof(S) + 4 * sizeof(R)) <= 40 * 1024;
   __shared__ SBasis<NP, double> sb;
   __shared__ S Us[EPB][5][n3];
-  for (int t = threadIdx.x; t < NP; t += blockDim.x) { sb.Lm[t] = Lm[t]; sb.Lp[t] = Lp[t]; }
+  __shared__ R Cs[C32 ? EPB : 1][4][C32 ? n3 : 1];
+  __shared__ R Lf[2][NP];
+  for (int t = threadIdx.x; t < NP; t += blockDim.x) {
+    sb.Lm[t] = Lm[t]; sb.Lp[t] = Lp[t];
+    Lf[0][t] = (R)Lm[t]; Lf[1][t] = (R)Lp[t];
+  }
   const int e0 = blockIdx.x * EPB;
   const int nloc = min(EPB, L.nElems - e0);
   // coalesced load of the element block (AoS (5,n^3) per element in global memory)
@@ -136,14 +145,22 @@ k_prolong(const S* __restrict__ U, const int* __restrict__ E2S, const double* __
   // volume prims
   for (int t = threadIdx.x; t < nloc * n3; t += blockDim.x) {
     int el = t / n3, node = t - el * n3;
-    const S u[5] = {Us[el][0][node], Us[el][1][node], Us[el][2][node], Us[el][3][node], Us[el][4][node]};
     R prim[6], srho;
-    cons_to_prim_d(u, gas, prim, srho);
+    if constexpr (C32) {
+      const R c[4] = {(R)Us[el][0][node], (R)Us[el][1][node], (R)Us[el][2][node], (R)Us[el][3][node]};
+#pragma unroll
+      for (int v = 0; v < 4; ++v) Cs[el][v][node] = c[v];
+      cons_to_prim_mixed(c, (double)Us[el][4][node], gas, prim, srho);
+    } else {
+      const S u[5] = {Us[el][0][node], Us[el][1][node], Us[el][2][node], Us[el][3][node], Us[el][4][node]};
+      cons_to_prim_d(u, gas, prim, srho);
+    }
     R* P = Pvol + (size_t)(e0 + el) * 7 * n3 + node;
 #pragma unroll
     for (int c = 0; c < 6; ++c) P[c * n3] = prim[c];
     P[6 * n3] = srho;
   }
+  if constexpr (C32) __syncthreads();
   // face traces
   for (int t = threadIdx.x; t < nloc * 6 * n2; t += blockDim.x) {
     int el = t / (6 * n2), r = t - el * 6 * n2;
@@ -154,28 +171,60 @@ k_prolong(const S* __restrict__ U, const int* __restrict__ E2S, const double* __
     int flip = E2S[(e * 6 + ls - 1) * 2 + 1];
     int a, b;
     s2v2(N, p, q, flip, ls, a, b);
-    S u[5];
-    if (!L.gauss) {
-      int node = face_node(n, ls, a, b, is_minus(ls) ? 0 : N);
-#pragma unroll
-      for (int v = 0; v < 5; ++v) u[v] = Us[el][v][node];
-    } else {
-      const double* Lv = is_minus(ls) ? sb.Lm : sb.Lp;
-#pragma unroll
-      for (int v = 0; v < 5; ++v) {
-        S s = Us[el][v][face_node(n, ls, a, b, 0)] * Lv[0];
-#pragma unroll
-        for (int l = 1; l < n; ++l) s = s + Us[el][v][face_node(n, ls, a, b, l)] * Lv[l];
-        u[v] = s;
-      }
-    }
     R prim[6], srho;
-    cons_to_prim_d(u, gas, prim, srho);
+    R uo[5];
+    if constexpr (C32) {
+      R c[4];
+      double E;
+      if (!L.gauss) {
+        const int node = face_node(n, ls, a, b, is_minus(ls) ? 0 : N);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) c[v] = Cs[el][v][node];
+        E = Us[el][4][node];
+      } else {
+        const R* Lv = Lf[is_minus(ls) ? 0 : 1];
+        const double* Ld = is_minus(ls) ? sb.Lm : sb.Lp;
+        const int n0 = face_node(n, ls, a, b, 0);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) c[v] = Cs[el][v][n0] * Lv[0];
+        E = Us[el][4][n0] * Ld[0];
+#pragma unroll
+        for (int l = 1; l < n; ++l) {
+          const int nl = face_node(n, ls, a, b, l);
+#pragma unroll
+          for (int v = 0; v < 4; ++v) c[v] = c[v] + Cs[el][v][nl] * Lv[l];
+          E = E + Us[el][4][nl] * Ld[l];
+        }
+      }
+      cons_to_prim_mixed(c, E, gas, prim, srho);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) uo[v] = c[v];
+      uo[4] = (R)E;
+    } else {
+      S u[5];
+      if (!L.gauss) {
+        int node = face_node(n, ls, a, b, is_minus(ls) ? 0 : N);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) u[v] = Us[el][v][node];
+      } else {
+        const double* Lv = is_minus(ls) ? sb.Lm : sb.Lp;
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+          S s = Us[el][v][face_node(n, ls, a, b, 0)] * Lv[0];
+#pragma unroll
+          for (int l = 1; l < n; ++l) s = s + Us[el][v][face_node(n, ls, a, b, l)] * Lv[l];
+          u[v] = s;
+        }
+      }
+      cons_to_prim_d(u, gas, prim, srho);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) uo[v] = (R)u[v];
+    }
     const int slot = (flip == 0) ? 0 : 1;
     R* uf = Uf + ((size_t)slot * L.nSides + side) * 5 * n2 + pq;
     R* pf = Pf + ((size_t)slot * L.nSides + side) * 6 * n2 + pq;
 #pragma unroll
-    for (int v = 0; v < 5; ++v) uf[v * n2] = (R)u[v];
+    for (int v = 0; v < 5; ++v) uf[v * n2] = uo[v];
 #pragma unroll
     for (int c = 0; c < 6; ++c) pf[c * n2] = prim[c];
   }
@@ -218,8 +267,14 @@ k_bc_lift_ghost(R* __restrict__ Pf, const R* __restrict__ Fgeo, Gas<R> gas, Laun
 
 // V0 = 1 skips the density gradient, which no flux of the operator reads (EvalDiffFlux3D uses the
 // velocity and temperature gradients only); Gvol/Gf then hold no density entries.
+// FP32 (mixed form) blocks of at most 256 threads: four blocks per SM (at most 72 registers); the
+// FP32 kernel is latency bound, and at two blocks per SM (107 registers at N=5) only 14 warps hid it
+template <int NP, typename R> struct LiftMinBlocks {
+  static constexpr int v = (sizeof(R) == 4 && EPBof<NP>::v * NP * NP * NP <= 256) ? 4 : 2;
+};
+
 template <int NP, typename R, int V0 = 0>
-__global__ void __launch_bounds__(EPBof<NP>::v * NP * NP * NP, 2)
+__global__ void __launch_bounds__(EPBof<NP>::v * NP * NP * NP, LiftMinBlocks<NP, R>::v)
 k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restrict__ Pf, const R* __restrict__ Fgeo,
        const int* __restrict__ E2S, DevBasis<R> basis, Launch L, R* __restrict__ Gvol, R* __restrict__ Gf) {
   constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, EPB = EPBof<NP>::v, N = NP - 1;

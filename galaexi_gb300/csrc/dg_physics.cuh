@@ -28,6 +28,25 @@ template <typename R> struct Gas {
 template <typename R> struct OffsetOf { static constexpr bool v = false; };
 template <> struct OffsetOf<float> { static constexpr bool v = true; };
 
+// ConsToPrim of the mixed form from FP32 density and momenta c and the FP64 energy E: velocities and
+// kinetic energy in FP32 (relative error ~1e-7 of quantities that are themselves rounded to FP32), the
+// energy difference E - ke and p' = p - p_ref in FP64, where the cancellation at low Mach would lose
+// the pressure fluctuations
+template <typename R>
+__device__ __forceinline__ void cons_to_prim_mixed(const R c[4], double E, const Gas<R>& g, R prim[6], R& srho) {
+  const R sr = R(1) / c[0];
+  const R v1 = c[1] * sr, v2 = c[2] * sr, v3 = c[3] * sr;
+  const R ke = R(0.5) * (c[1] * v1 + c[2] * v2 + c[3] * v3);
+  const double p = g.kappaM1D * (E - (double)ke);
+  srho = sr;
+  prim[0] = c[0];
+  prim[1] = v1;
+  prim[2] = v2;
+  prim[3] = v3;
+  prim[4] = (R)(p - g.prefD);
+  prim[5] = (R)p * sr * g.sR;
+}
+
 // ConsToPrim (idealgas/eos.f90:212-239) from the FP64 state: rho, u, v, w, p (p' in the mixed form), T, 1/rho
 template <typename R, typename S>
 __device__ __forceinline__ void cons_to_prim_d(const S u[5], const Gas<R>& g, R prim[6], R& srho) {
@@ -40,21 +59,8 @@ __device__ __forceinline__ void cons_to_prim_d(const S u[5], const Gas<R>& g, R 
     prim[4] = g.kappaM1 * ((R)u[4] - R(0.5) * ((R)u[1] * prim[1] + (R)u[2] * prim[2] + (R)u[3] * prim[3]));
     prim[5] = prim[4] * srho * g.sR;
   } else {
-    // mixed form: velocities and kinetic energy in FP32 (relative error ~1e-7 of quantities that
-    // are themselves rounded to FP32), the energy difference E - ke and p' = p - p_ref in FP64,
-    // where the cancellation at low Mach would lose the pressure fluctuations
-    const R rho = (R)u[0], m1 = (R)u[1], m2 = (R)u[2], m3 = (R)u[3];
-    const R sr = R(1) / rho;
-    const R v1 = m1 * sr, v2 = m2 * sr, v3 = m3 * sr;
-    const R ke = R(0.5) * (m1 * v1 + m2 * v2 + m3 * v3);
-    const double p = g.kappaM1D * (u[4] - (double)ke);
-    srho = sr;
-    prim[0] = rho;
-    prim[1] = v1;
-    prim[2] = v2;
-    prim[3] = v3;
-    prim[4] = (R)(p - g.prefD);
-    prim[5] = (R)p * sr * g.sR;
+    const R c[4] = {(R)u[0], (R)u[1], (R)u[2], (R)u[3]};
+    cons_to_prim_mixed(c, (double)u[4], g, prim, srho);
   }
 }
 // absolute pressure from the stored one

@@ -104,3 +104,23 @@ def test_mixed_every_degree(N):
     err = rel(Ut.cpu().numpy(), ref)
     op.close()
     assert err <= 1e-5, (N, err)
+
+
+@pytest.mark.parametrize("lift", ["br1", "br2"])
+@pytest.mark.parametrize("N", [2, 5, 8, 9])
+def test_mixed_gauss_curved(N, lift):
+    """Mixed form on Gauss nodes (density and momenta interpolated to the faces in FP32, the energy in
+    FP64; N = 9 interpolates all in FP64) on a curved mesh, HLLC, against the FP64 oracle."""
+    R = 71.42857
+    kw = dict(NodeType="gauss", Riemann="hllc", parabolic=True, mu0=2e-3, Lifting=lift)
+    if lift == "br2":
+        kw["etaBR2"] = 2.0
+    m = gx.Mesh(N, 1, 3, 2, 2, (-math.pi,) * 3, (math.pi,) * 3, deform=0.05)
+    U = state(m, 200 + N, R)
+    ref = Oracle(gx.config(N=N, R=R, **kw), m).rhs(U)
+    op = gx.DG(gx.config(N=N, R=R, precision="mixed", **kw), m)
+    Ut = op.DGTimeDerivative_weakForm(0.0, torch.from_numpy(U.copy()).cuda())
+    torch.cuda.synchronize()
+    err = rel(Ut.cpu().numpy(), ref)
+    op.close()
+    assert err <= 1e-5, (N, lift, err)
