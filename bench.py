@@ -62,6 +62,8 @@ def parse():
                     help="central-difference check of the adjoint gradient along this many random directions")
     ap.add_argument("--adjoint-steps", type=int, default=None,
                     help="steps of the adjoint window (default 200 for the N=5 case, 50 for --only scale64)")
+    ap.add_argument("--curved-ne", type=int, default=32,
+                    help="elements per direction of the curved-box case (32; smaller for profiling)")
     ap.add_argument("--only", default=None, choices=["adjoint", "mixed_tgv", "mixed_curved", "scale64"],
                     help="run one of the extra measurements alone and print its JSON (profiling runs)")
     args = ap.parse_args()
@@ -343,15 +345,15 @@ def mixed_vs_fp64_tgv(workload, steps, stream):
     return res
 
 
-def mixed_vs_fp64_curved_br2(stream, steps=500):
+def mixed_vs_fp64_curved_br2(stream, steps=500, ne=32):
     """Mixed form against the FP64 form on the curved-box BR2 case: Navier-Stokes, N=5 Gauss nodes,
-    weak form, HLLC, BR2 (etaBR2 = 2), 32^3 elements on [0,1]^3 with every node displaced by
+    weak form, HLLC, BR2 (etaBR2 = 2), 32^3 elements (ne^3) on [0,1]^3 with every node displaced by
     0.05 sin(2 pi x) sin(2 pi y) sin(2 pi z), uniform flow rho=1, v=(0.3,0.2,0.1), p=1/1.4 plus
     seeded Gaussian noise 1e-3 on each conserved variable, mu=1e-3; 500 steps."""
     import numpy as np
     import torch
     import galaexi_gb300 as gx
-    N, ne = 5, 32
+    N = 5
     mesh = gx.Mesh(N, 1, ne, ne, ne, (0.0,) * 3, (1.0,) * 3, deform=0.05)
     U = gx.fill_ini(mesh, 1, [1.0, 0.3, 0.2, 0.1, 1.0 / 1.4])
     rng = np.random.default_rng(20261203)
@@ -374,7 +376,7 @@ def mixed_vs_fp64_curved_br2(stream, steps=500):
         Ur, K = U0.clone(), torch.zeros_like(U0)
         ms, _ = timed(lambda: op.TimeStepByLSERKW2(0.0, dt, Ur, K, nSteps=steps), stream)
         out[prec] = (ms, Ur, ops["fp64"].integrals(Ur))
-    res = {"workload": "curved_n5_gauss_32cube_weak_hllc_br2", "steps": steps, "dt": dt, "cfl": 0.9, "dfl": 0.45,
+    res = {"workload": "curved_n5_gauss_%dcube_weak_hllc_br2" % ne, "steps": steps, "dt": dt, "cfl": 0.9, "dfl": 0.45,
            "speedup": out["fp64"][0] / out["mixed"][0],
            "dof_stage_per_s_fp64": mesh.nDOF * 5 * steps / (out["fp64"][0] * 1e-3),
            "dof_stage_per_s_mixed": mesh.nDOF * 5 * steps / (out["mixed"][0] * 1e-3),
@@ -594,7 +596,7 @@ def main():
         elif args.only == "mixed_tgv":
             res = mixed_vs_fp64_tgv(args.workload, args.steps, stream)
         else:
-            res = mixed_vs_fp64_curved_br2(stream, steps=args.steps)
+            res = mixed_vs_fp64_curved_br2(stream, steps=args.steps, ne=args.curved_ne)
         if rank == 0:
             print(json.dumps({"only": args.only, **res}), flush=True)
         return
