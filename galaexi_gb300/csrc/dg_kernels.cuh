@@ -673,6 +673,30 @@ __device__ __forceinline__ int vsw(int node) {
 __host__ __device__ constexpr int vol_stage_slots(int split, int parab) {
   return split < 0 ? 15 : (parab ? 12 : (split == DG_SPLIT_PI ? 6 : 9));
 }
+// threads per 1D line in the split-form phase of k_volume: FP32 (mixed form) at N = 5..7 splits the
+// rows of each line's pair triangle between two threads (with their own accumulators), since the
+// FP32 phase is latency bound with one thread per line; FP64 keeps one thread (FP64-issue bound)
+template <int NP, typename R>
+__host__ __device__ constexpr int vol_line_threads() {
+  return (sizeof(R) == 4 && 6 * NP * NP <= NP * NP * NP && NP <= 8) ? 2 : 1;
+}
+// rows a of the pair triangle (a, b > a; n-1-a pairs) taken by the second thread of a line: r0 <= a < r1,
+// chosen to balance the pair counts of the two threads
+template <int NP>
+struct LineSplit {
+  static constexpr int pairs(int r0, int r1) { return r0 >= r1 ? 0 : (NP - 1 - r0) + pairs(r0 + 1, r1); }
+  static constexpr int cost(int r0, int r1) {
+    return pairs(r0, r1) > NP * (NP - 1) / 2 - pairs(r0, r1) ? pairs(r0, r1) : NP * (NP - 1) / 2 - pairs(r0, r1);
+  }
+  static constexpr int best(int which) {
+    int b0 = 0, b1 = 0, bc = 1 << 30;
+    for (int r0 = 0; r0 < NP; ++r0)
+      for (int r1 = r0; r1 < NP; ++r1)
+        if (cost(r0, r1) < bc) { bc = cost(r0, r1); b0 = r0; b1 = r1; }
+    return which == 0 ? b0 : b1;
+  }
+  static constexpr int r0 = best(0), r1 = best(1);
+};
 
 template <typename S>
 struct RKArgsT {
@@ -697,8 +721,9 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
   constexpr int S_RHO = 0, S_AUX = 1, S_U = 2, S_V = 3, S_W = 4, S_PM = 5, S_M1 = 6, S_M2 = 7, S_M3 = 8;
   __shared__ SBasis<NP, R> sb;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int NH = vol_line_threads<NP, R>();
   R* A = reinterpret_cast<R*>(smem_raw);             // [EPB][NA][n3]
-  R* AccD = A + (size_t)EPB * NA * n3;               // [EPB][3][5][n3]  (split form only)
+  R* AccD = A + (size_t)EPB * NA * n3;               // [EPB][NH][3][5][n3]  (split form only)
   load_basis(sb, basis);
   if constexpr (SPLIT == DG_SPLIT_PI) {
     // PI pair fluxes are evaluated as 8F (see phase B): fold the 1/8 into DVolSurf (exact scaling)
@@ -809,18 +834,19 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
         Ae[S_M2 * n3 + snode] = (R)Un[2];
         Ae[S_M3 * n3 + snode] = (R)Un[3];
       }
-      R* Ad = AccD + (size_t)el * 15 * n3;
+      R* Ad = AccD + (size_t)el * NH * 15 * n3;
 #pragma unroll
-      for (int c = 0; c < 15; ++c) Ad[c * n3 + snode] = R(0);
+      for (int c = 0; c < NH * 15; ++c) Ad[c * n3 + snode] = R(0);
     }
     __syncthreads();
-    const int lel = tid / (3 * n2);
-    const bool lactive = (lel < nloc) && (tid < EPB * 3 * n2);  // 3*n2 <= n3 for NP >= 3
+    const int lel = tid / (NH * 3 * n2);
+    const bool lactive = (lel < nloc) && (tid < EPB * NH * 3 * n2);  // 3*n2 <= n3 for NP >= 3; 6*n2 <= n3 if NH = 2
     if (lactive) {
-      const int lr = tid - lel * 3 * n2;
+      const int lh = tid - lel * NH * 3 * n2;
+      const int half = lh / (3 * n2), lr = lh - half * 3 * n2;
       const int dir = lr / n2, li = lr - dir * n2;
       const R* Al = A + (size_t)lel * NA * n3;
-      R* Ad = AccD + ((size_t)lel * 3 + dir) * 5 * n3;
+      R* Ad = AccD + (((size_t)lel * NH + half) * 3 + dir) * 5 * n3;
       int base, stride;  // nodes of the line: base + l*stride
       if (dir == 0) { base = n * li; stride = 1; }
       else if (dir == 1) { base = (li % n) + n2 * (li / n); stride = n; }
@@ -828,6 +854,9 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
       const R* Ml = Met + ((size_t)(e0 + lel) * 10 + 3 * dir) * n3;  // this direction's metric terms
 #pragma unroll 1
       for (int a = 0; a < NP - 1; ++a) {
+        if constexpr (NH == 2) {
+          if ((a >= LineSplit<NP>::r0 && a < LineSplit<NP>::r1) != (half == 1)) continue;
+        }
         const int na = base + a * stride, sna = vsw<NP>(na);
         PairNode<R> A_;
         A_.rho = Al[S_RHO * n3 + sna]; A_.aux = Al[S_AUX * n3 + sna];
@@ -882,10 +911,11 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
     }
     __syncthreads();
     if (active) {
-      const R* Ad = AccD + (size_t)el * 15 * n3;
+      const R* Ad = AccD + (size_t)el * NH * 15 * n3;
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
         R sv = Ad[v * n3 + snode] + Ad[(5 + v) * n3 + snode] + Ad[(10 + v) * n3 + snode];
+        if constexpr (NH == 2) sv = sv + (Ad[(15 + v) * n3 + snode] + Ad[(20 + v) * n3 + snode] + Ad[(25 + v) * n3 + snode]);
         if (SPLIT == DG_SPLIT_PI && v == 0) sv = sv * R(2);
         vacc[v] = vacc[v] + sv;
       }

@@ -1,0 +1,139 @@
+"""The benchmark configurations at their full sizes against the oracle, plus size-independent
+properties of the operator at those sizes.
+
+* Euler isentropic vortex, N=3 Gauss, weak form, LF, 8^3 elements on [0,10]^3 (32 768 DOF): 100
+  LSERK steps at CFL 0.9, FP64, against the oracle (<= 1e-10) and against the exact solution.
+* Navier-Stokes TGV (perturbed), N=7 Gauss-Lobatto, split PI, Roe, BR1, 24^3 elements (7.08 M DOF):
+  one RHS (<= 1e-12) and two LSERK steps (<= 1e-10) against the oracle.
+* Navier-Stokes, N=5 Gauss, weak, HLLC, BR2, 32^3 elements of the curved box (7.08 M DOF): one RHS
+  against the oracle (<= 1e-12), free-stream preservation.
+* Navier-Stokes TGV as above with N=5 and 16^3 elements (the adjoint case): one RHS (<= 1e-12).
+* Discrete conservation, FP64 and mixed form: the volume integrals of the mass, momentum and energy
+  rates vanish on the periodic boxes, |int Ut| <= tol * int |Ut|.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import galaexi_gb300 as gx
+from galaexi_gb300 import _native as nat
+from oracle.oracle import Oracle
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+TGV_R = 71.42857
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def gpu_rhs(op, U):
+    Ut = op.DGTimeDerivative_weakForm(0.0, torch.from_numpy(U.copy()).cuda())
+    torch.cuda.synchronize()
+    return Ut
+
+
+def tgv(N, ne):
+    """The TGV state with a seeded perturbation: the unperturbed TGV is nearly steady at t = 0 (its
+    momentum rates are O(mu) left over from cancelling O(p0) fluxes), so relative errors of its Ut
+    would measure that cancellation, not the operator."""
+    m = gx.Mesh(N, 2, ne, ne, ne, (-math.pi,) * 3, (math.pi,) * 3)
+    cfg = dict(N=N, Riemann="roe", SplitDG="pi", parabolic=True, mu0=1 / 1600, R=TGV_R)
+    U = gx.tgv_state(m, mach=0.1, R=TGV_R)
+    rng = np.random.default_rng(20261203)
+    U = U + 1e-2 * rng.standard_normal(U.shape) * np.abs(U).mean(axis=(0, 1, 2, 3))
+    return m, cfg, U
+
+
+def curved(ne=32, noise=True):
+    m = gx.Mesh(5, 1, ne, ne, ne, (0.0,) * 3, (1.0,) * 3, deform=0.05)
+    U = gx.fill_ini(m, 1, [1.0, 0.3, 0.2, 0.1, 1.0 / 1.4])
+    if noise:
+        U = U + 1e-3 * np.random.default_rng(20261203).standard_normal(U.size).reshape(U.shape)
+    cfg = dict(N=5, NodeType="gauss", Riemann="hllc", parabolic=True, mu0=1e-3, Lifting="br2", etaBR2=2.0)
+    return m, cfg, U
+
+
+def test_vortex_100_steps_full_size():
+    m = gx.Mesh(3, 1, 8, 8, 8, (0.0,) * 3, (10.0,) * 3)
+    prm = [1, 1, 1, 0, 1, 5, 5, 0, 0, 0, 1, 5, 1]  # RefState, IniCenter, IniAxis, beta, half-width
+    U0 = gx.fill_ini(m, nat.DG_EXACTFUNC_SHU_VORTEX, prm)
+    cfg = gx.config(N=3, NodeType="gauss", Riemann="lf")
+    o = Oracle(cfg, m)
+    dt_ref, _ = o.calc_timestep(U0, 0.9)
+    ref, _ = o.lserk_steps(U0, dt_ref, 100)
+    op = gx.DG(cfg, m)
+    U = torch.from_numpy(U0.copy()).cuda()
+    dt, err = op.CalcTimeStep(U, 0.9)
+    assert err == 0 and abs(dt - dt_ref) <= 1e-14 * dt_ref
+    op.TimeStepByLSERKW2(0.0, dt_ref, U, torch.zeros_like(U), nSteps=100)
+    torch.cuda.synchronize()
+    got = U.cpu().numpy()
+    op.close()
+    assert rel(got, ref) <= 1e-10
+    # the vortex is advected with (1, 1, 0); on 4 nodes per element and direction it stays within a few
+    # per cent of the exact solution over these 100 steps
+    exact = gx.fill_ini(m, nat.DG_EXACTFUNC_SHU_VORTEX, prm, t=100 * dt_ref)
+    assert rel(got, exact) < 5e-2
+
+
+def test_tgv_n7_24cube_rhs_and_steps_full_size():
+    m, kw, U0 = tgv(7, 24)
+    cfg = gx.config(**kw)
+    o = Oracle(cfg, m)
+    op = gx.DG(cfg, m)
+    assert rel(gpu_rhs(op, U0).cpu().numpy(), o.rhs(U0)) <= 1e-12
+    dt, _ = o.calc_timestep(U0, 0.8, 0.8)
+    ref, _ = o.lserk_steps(U0, dt, 2)
+    U = torch.from_numpy(U0.copy()).cuda()
+    op.TimeStepByLSERKW2(0.0, dt, U, torch.zeros_like(U), nSteps=2)
+    torch.cuda.synchronize()
+    assert rel(U.cpu().numpy(), ref) <= 1e-10
+    op.close()
+
+
+def test_tgv_n5_16cube_rhs_full_size():
+    m, kw, U0 = tgv(5, 16)
+    cfg = gx.config(**kw)
+    op = gx.DG(cfg, m)
+    assert rel(gpu_rhs(op, U0).cpu().numpy(), Oracle(cfg, m).rhs(U0)) <= 1e-12
+    op.close()
+
+
+def test_curved_gauss_br2_32cube_rhs_full_size():
+    m, kw, U0 = curved()
+    cfg = gx.config(**kw)
+    op = gx.DG(cfg, m)
+    assert rel(gpu_rhs(op, U0).cpu().numpy(), Oracle(cfg, m).rhs(U0)) <= 1e-12
+    # free stream: the constant state stays constant on the curved mesh up to round-off, which grows
+    # with the inverse Jacobian sJ ~ (2/h)^3 (the oracle: 2.4e-12 at 3^3, 1.7e-10 at 8^3, 9.4e-9 at 32^3
+    # elements, i.e. ~4e-14 sJ)
+    Uc = gx.fill_ini(m, 1, [1.0, 0.3, 0.2, 0.1, 1.0 / 1.4])
+    assert float(gpu_rhs(op, Uc).abs().max()) < 1e-12 * float(np.max(m.sJ))
+    op.close()
+
+
+CONSERVATION = [
+    ("tgv_n7_24cube", "fp64", 1e-12),
+    ("tgv_n7_24cube", "mixed", 1e-6),
+    ("curved_n5_gauss_32cube", "fp64", 1e-12),
+    ("curved_n5_gauss_32cube", "mixed", 1e-6),
+]
+
+
+@pytest.mark.parametrize("case,precision,tol", CONSERVATION, ids=["%s_%s" % c[:2] for c in CONSERVATION])
+def test_discrete_conservation_full_size(case, precision, tol):
+    """On a periodic box the DG operator conserves mass, momentum and energy discretely: the integrals
+    of the rates (FP64, with the solution quadrature) vanish up to round-off."""
+    m, kw, U0 = tgv(7, 24) if case.startswith("tgv") else curved()
+    op = gx.DG(gx.config(precision=precision, **kw), m)
+    Ut = gpu_rhs(op, U0)
+    net = op.integrals(Ut)[:5]
+    mag = op.integrals(Ut.abs())[:5]
+    op.close()
+    for v in range(5):
+        assert abs(net[v]) <= tol * mag[v], (v, net[v], mag[v])
