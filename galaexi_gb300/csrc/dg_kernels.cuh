@@ -669,9 +669,16 @@ __device__ __forceinline__ int vsw(int node) {
   }
 }
 
-// staging slots per node of k_volume (see there); shared by the kernel and its launch code
+// staging slots per node of k_volume (see there); shared by the kernel and its launch code.  FP32 (mixed
+// form) at N <= 7 also stages the metric terms of the split-form phase (9 slots after its node data),
+// which FP64 reads through L1 so that two blocks fit an SM
+template <int NP, typename R>
+__host__ __device__ constexpr bool vol_metrics_staged(int split) { return sizeof(R) == 4 && split >= 0 && NP <= 8; }
+template <int NP, typename R>
 __host__ __device__ constexpr int vol_stage_slots(int split, int parab) {
-  return split < 0 ? 15 : (parab ? 12 : (split == DG_SPLIT_PI ? 6 : 9));
+  const int base = split < 0 ? 15 : (parab ? 12 : (split == DG_SPLIT_PI ? 6 : 9));
+  const int met = vol_metrics_staged<NP, R>(split) ? (split == DG_SPLIT_PI ? 6 : 9) + 9 : 0;
+  return base > met ? base : met;
 }
 // threads per 1D line in the split-form phase of k_volume: FP32 (mixed form) at N = 5..7 splits the
 // rows of each line's pair triangle between two threads (with their own accumulators), since the
@@ -717,8 +724,10 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
   // staging slots per node: the flux-form fluxes of phase A (15; split form: the 12 non-zero viscous
   // ones), then the node data of phase B (PI: rho, aux, u, v, w, p; other split forms also m1..m3);
   // the metrics of phase B are read from global memory (L1), so that at N=7 two blocks fit an SM
-  constexpr int NA = vol_stage_slots(SPLIT, PARAB);
+  constexpr int NA = vol_stage_slots<NP, R>(SPLIT, PARAB);
   constexpr int S_RHO = 0, S_AUX = 1, S_U = 2, S_V = 3, S_W = 4, S_PM = 5, S_M1 = 6, S_M2 = 7, S_M3 = 8;
+  constexpr bool MST = vol_metrics_staged<NP, R>(SPLIT);        // metric terms of phase B staged
+  constexpr int S_MET = (SPLIT == DG_SPLIT_PI) ? 6 : 9;          // their slots: S_MET + 3*dir + c
   __shared__ SBasis<NP, R> sb;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int NH = vol_line_threads<NP, R>();
@@ -834,6 +843,11 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
         Ae[S_M2 * n3 + snode] = (R)Un[2];
         Ae[S_M3 * n3 + snode] = (R)Un[3];
       }
+      if constexpr (MST) {
+        const R* Mn = Met + (size_t)e * 10 * n3 + node;
+#pragma unroll
+        for (int c = 0; c < 9; ++c) Ae[(S_MET + c) * n3 + snode] = Mn[c * n3];
+      }
       R* Ad = AccD + (size_t)el * NH * 15 * n3;
 #pragma unroll
       for (int c = 0; c < NH * 15; ++c) Ad[c * n3 + snode] = R(0);
@@ -851,7 +865,8 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
       if (dir == 0) { base = n * li; stride = 1; }
       else if (dir == 1) { base = (li % n) + n2 * (li / n); stride = n; }
       else { base = li; stride = n2; }
-      const R* Ml = Met + ((size_t)(e0 + lel) * 10 + 3 * dir) * n3;  // this direction's metric terms
+      // this direction's metric terms: staged (indexed by shared-memory position) or through L1
+      const R* Ml = MST ? Al + (S_MET + 3 * dir) * n3 : Met + ((size_t)(e0 + lel) * 10 + 3 * dir) * n3;
 #pragma unroll 1
       for (int a = 0; a < NP - 1; ++a) {
         if constexpr (NH == 2) {
@@ -866,7 +881,8 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
         } else {
           A_.m1 = A_.m2 = A_.m3 = R(0);
         }
-        const R ma0 = Ml[na], ma1 = Ml[n3 + na], ma2 = Ml[2 * n3 + na];
+        const int ma = MST ? sna : na;
+        const R ma0 = Ml[ma], ma1 = Ml[n3 + ma], ma2 = Ml[2 * n3 + ma];
         R sa[5];
 #pragma unroll
         for (int v = 0; v < 5; ++v) sa[v] = Ad[v * n3 + sna];
@@ -881,7 +897,8 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
           } else {
             B_.m1 = B_.m2 = B_.m3 = R(0);
           }
-          const R Ms0 = ma0 + Ml[nb], Ms1 = ma1 + Ml[n3 + nb], Ms2 = ma2 + Ml[2 * n3 + nb];
+          const int mb = MST ? snb : nb;
+          const R Ms0 = ma0 + Ml[mb], Ms1 = ma1 + Ml[n3 + mb], Ms2 = ma2 + Ml[2 * n3 + mb];
           R F[5];
           if constexpr (SPLIT == DG_SPLIT_PI) {
             // 8 x the PI flux of split_pair_flux, with the density row at 4 x (its accumulators are

@@ -26,7 +26,7 @@ constexpr int EPB = gx::EPBof<NP>::v;
 constexpr int NT = EPB * NP * NP * NP;  // threads per element block
 
 template <typename R, int SPL, int PAR> constexpr size_t volume_smem() {
-  return sizeof(R) * (size_t)EPB * (gx::vol_stage_slots(SPL, PAR) + (SPL >= 0 ? 15 * gx::vol_line_threads<NP, R>() : 0)) *
+  return sizeof(R) * (size_t)EPB * (gx::vol_stage_slots<NP, R>(SPL, PAR) + (SPL >= 0 ? 15 * gx::vol_line_threads<NP, R>() : 0)) *
          NP * NP * NP;
 }
 template <typename R> constexpr size_t lift_smem() {
