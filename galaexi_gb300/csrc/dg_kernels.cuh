@@ -6,8 +6,10 @@
 //   k_face     thread-per-face-node Riemann solver + BR1 viscous flux + SurfElem
 //   k_volume   element-per-block   volume integral (weak or split form, viscous part), surface
 //                                  integral, sign, Jacobian, and optionally the LSERK-W2 stage update
-// (k_lift is skipped for the Euler equations.)  The reference runs ~25-35 launches per stage with
-// full-size intermediates; here the element's state lives in shared memory inside each phase.
+// (k_lift is skipped for the Euler equations; a solution filter adds k_filter / k_filter_laf in front,
+// meshes with boundary sides add k_bc_lift_ghost before k_lift and k_bc_face beside k_face.)  The
+// reference runs ~25-35 launches per stage with full-size intermediates; here the element's state
+// lives in shared memory inside each phase.
 //
 // Layouts (internal, all per element contiguous so that element blocks load coalesced):
 //   Pvol [e][7][n^3]     rho,u,v,w,p,T,1/rho                 (compute type R)
