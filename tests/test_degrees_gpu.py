@@ -124,3 +124,22 @@ def test_mixed_gauss_curved(N, lift):
     err = rel(Ut.cpu().numpy(), ref)
     op.close()
     assert err <= 1e-5, (N, lift, err)
+
+
+@pytest.mark.parametrize("split", ["sd", "mo", "du", "kg", "pi"])
+@pytest.mark.parametrize("N", [5, 6, 7])
+def test_mixed_split_forms(N, split):
+    """Mixed form of every split flux at the degrees whose FP32 split-form phase runs two threads per
+    line and reads staged metric terms, Euler and Navier-Stokes, against the FP64 oracle."""
+    R = 71.42857
+    for parabolic in (False, True):
+        kw = dict(Riemann="roe", SplitDG=split, parabolic=parabolic, mu0=2e-3)
+        m = gx.Mesh(N, 2, 3, 2, 1, (-math.pi,) * 3, (math.pi,) * 3, deform=0.03)
+        U = state(m, 300 + N, R)
+        ref = Oracle(gx.config(N=N, R=R, **kw), m).rhs(U)
+        op = gx.DG(gx.config(N=N, R=R, precision="mixed", **kw), m)
+        Ut = op.DGTimeDerivative_weakForm(0.0, torch.from_numpy(U.copy()).cuda())
+        torch.cuda.synchronize()
+        err = rel(Ut.cpu().numpy(), ref)
+        op.close()
+        assert err <= 1e-5, (N, split, parabolic, err)
