@@ -271,10 +271,14 @@ int need_fp64(dg_ctx* ctx, const char* what) {
 
 int tlm_setup(dg_ctx* ctx) {
   if (int rc = need_fp64(ctx, "tangent-linear operator")) return rc;
-  if (ctx->nBCSides) { set_error("tangent-linear operator: periodic meshes only"); return DG_ERR_UNSUPPORTED; }
   if (ctx->cfg.filter_type) { set_error("tangent-linear operator: no solution filter"); return DG_ERR_UNSUPPORTED; }
   if (ctx->cfg.split_dg != DG_SPLIT_NONE && ctx->cfg.split_dg != DG_SPLIT_PI && ctx->cfg.split_dg != DG_SPLIT_KG) {
     set_error("tangent-linear operator: split forms PI and KG only"); return DG_ERR_UNSUPPORTED;
+  }
+  if (ctx->nBCSides && !ctx->bcref_t.p) {  // (again after dg_set_boundaries)
+    if (!ctx->bcref_t.alloc(ctx->bcref_d.n)) { set_error("cudaMalloc tangent-linear boundary states"); return DG_ERR_ALLOC; }
+    k_to_dual<<<grid_for(ctx->bcref_d.n), 256>>>(ctx->bcref_d.p, ctx->bcref_t.p, ctx->bcref_d.n);
+    CUDA_TRY(cudaDeviceSynchronize(), "tangent-linear boundary states");
   }
   if (ctx->t_ok) return DG_OK;
   const gxc::NPTable* T = table_for(ctx->n);
@@ -457,7 +461,7 @@ int dg_ctx_destroy(dg_ctx* ctx) {
   ctx->red.release();
   ctx->bad.release();
   ctx->S2E.release(); ctx->wq.release();
-  ctx->bctype.release(); ctx->bcstate.release(); ctx->bcref_d.release(); ctx->bcref_f.release();
+  ctx->bctype.release(); ctx->bcstate.release(); ctx->bcref_d.release(); ctx->bcref_f.release(); ctx->bcref_t.release();
   ctx->t.release(); ctx->Ud.release(); ctx->Utd.release();
   ctx->UfB.release(); ctx->GfB.release(); ctx->JB.release(); ctx->UBv.release(); ctx->part.release();
   ctx->acc.release(); ctx->W.release(); ctx->K.release(); ctx->tape.store.release();
@@ -554,7 +558,7 @@ int dg_set_mesh(dg_ctx* ctx, int nElems, int nSides, int nBCSides, const double*
   CUDA_TRY(cudaMemcpy(ctx->wq.p, ctx->B.w.data(), n * sizeof(double), cudaMemcpyHostToDevice), "upload weights");
   ctx->nBCSides = nBCSides;
   ctx->bc_ok = nBCSides == 0;
-  ctx->bctype.release(); ctx->bcstate.release(); ctx->bcref_d.release(); ctx->bcref_f.release();
+  ctx->bctype.release(); ctx->bcstate.release(); ctx->bcref_d.release(); ctx->bcref_f.release(); ctx->bcref_t.release();
   ctx->t_ok = false;
   ctx->tape.ok = false;
   ctx->t.release(); ctx->Ud.release(); ctx->Utd.release();

@@ -94,6 +94,7 @@ struct dg_ctx {
   gxc::DBuf<int> bctype, bcstate;
   gxc::DBuf<double> bcref_d;
   gxc::DBuf<float> bcref_f;
+  gxc::DBuf<gx::Dual<1>> bcref_t;  // the reference states for the tangent-linear kernels (zero tangents)
   bool bc_ok = false;
   gxh::Basis1D B;
   gxc::PrecData<double> d;

@@ -2,6 +2,8 @@
 // with GX_NP defined, so the kernels of every degree compile in their own translation unit.
 #pragma once
 #include "dg_ctx.h"
+#include <type_traits>
+
 #include "dg_filter.cuh"
 
 #ifndef GX_NP
@@ -103,7 +105,8 @@ template <typename R, typename S = double, int V0 = 0>
 void rhs_front(dg_ctx* ctx, PrecData<R>& P, const S* U, const gx::Gas<R>& gas, cudaStream_t st, cudaEvent_t* ev,
                bool face) {
   const int grid = (ctx->nElems + EPB - 1) / EPB;
-  const gx::Launch L = gxc::make_launch(ctx);
+  gx::Launch L = gxc::make_launch(ctx);
+  if constexpr (std::is_same<R, gx::Dual<1>>::value) L.bcref = ctx->bcref_t.p;  // boundary states, zero tangents
   const gx::DevBasis<R> b = gxc::dev_basis(P, NP);
   const gx::DevBasis<double> bd = gxc::dev_basis(ctx->d, NP);  // FP64 face interpolation in every form
   gx::k_prolong<NP, R, S><<<grid, NT, 0, st>>>(U, ctx->E2S.p, bd.Lm, bd.Lp, gas, L, P.Pvol.p, P.Uf.p, P.Pf.p);

@@ -269,14 +269,53 @@ def test_gpu_reproduces_cavity_regression():
 
 
 @pytest.mark.gpu
-def test_bc_meshes_rejected_by_tangent_and_adjoint():
+def test_bc_meshes_rejected_by_adjoint():
     torch = pytest.importorskip("torch")
     m, bnd = cavity_case()
     op = gx.DG(cavity_config(), m, boundaries=bnd)
     U = torch.from_numpy(cavity_initial(m)).cuda()
     with pytest.raises(gx.DGError):
-        op.rhs_jvp(U, torch.zeros_like(U))
+        op.rhs_vjp(U, torch.zeros_like(U))
     op.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cname,ckw,nt", CONFIGS, ids=[c[0] for c in CONFIGS])
+@pytest.mark.parametrize("mname,path,bcs,N", MESHES, ids=[m[0] for m in MESHES])
+def test_bc_tangent_linear_vs_central_differences(cname, ckw, nt, mname, path, bcs, N):
+    """The tangent-linear operator (the forward kernels on dual numbers, the boundary kernels
+    included) on meshes with boundary sides: its primal equals the plain RHS, its tangent equals
+    central differences of the plain RHS along a seeded direction and a viscosity change."""
+    torch = pytest.importorskip("torch")
+    cfg = gx.config(N=N, R=RGAS, kappa=KAPPA, **ckw)
+    m = gx.Mesh.from_hopr(path, N, nt)
+    bnd = m.boundaries(FLOW_REFSTATES, bcs)
+    seed = zlib.crc32((cname + mname + "tlm").encode())
+    rng = np.random.default_rng(seed)
+    # node noise on top of the smooth flow: at nodes on y = z = 0 the smooth state's normal velocity on
+    # the outflow boundary equals the reference state's exactly, a tie of the Lax-Friedrichs wave-speed
+    # maximum where the operator has only one-sided derivatives (the dual numbers take one side,
+    # central differences average the two)
+    U0 = flow_state(m, seed)
+    U = torch.from_numpy(U0 * (1.0 + 1e-3 * rng.standard_normal(U0.shape))).cuda()
+    v = torch.from_numpy(rng.standard_normal(tuple(U.shape))).cuda()
+    v = v * U.abs().mean(dim=(0, 1, 2, 3)) * 1e-2
+    mu_dot = 1e-3 if cfg.parabolic else 0.0
+    op = gx.DG(cfg, m, boundaries=bnd)
+    Ut = op.DGTimeDerivative_weakForm(0.0, U.clone())
+    Ut2, Jv = op.rhs_jvp(U, v, mu_dot)
+    op.close()
+    assert float((Ut2 - Ut).norm() / Ut.norm()) <= 1e-13
+    eps = 1e-6
+    fd = []
+    for sgn in (1.0, -1.0):
+        kw = dict(ckw, mu0=ckw["mu0"] + sgn * eps * mu_dot) if cfg.parabolic else ckw
+        o2 = gx.DG(gx.config(N=N, R=RGAS, kappa=KAPPA, **kw), m, boundaries=bnd)
+        fd.append(o2.DGTimeDerivative_weakForm(0.0, U + sgn * eps * v))
+        o2.close()
+    fd = (fd[0] - fd[1]) / (2 * eps)
+    err = float((fd - Jv).norm() / Jv.norm())
+    assert err <= 1e-6, (cname, mname, err)
 
 
 @pytest.mark.gpu
