@@ -118,7 +118,7 @@ __host__ __device__ constexpr int lift_ps_slots(int NP) { return 5 * NP * NP * N
 // blocks per SM: 0.57 -> 0.38 ms per stage at N=7, 24^3 elements)
 // =====================================================================================
 template <int NP, typename R, typename S = double>
-__global__ void __launch_bounds__(EPBof<NP>::v * NP * NP * NP, 2)
+__global__ void __launch_bounds__(EPBof<NP>::v * NP * NP * NP, OffsetOf<R>::v ? 3 : 2)
 k_prolong(const S* __restrict__ U, const int* __restrict__ E2S, const double* __restrict__ Lm,
           const double* __restrict__ Lp, Gas<R> gas, Launch L, R* __restrict__ Pvol, R* __restrict__ Uf,
           R* __restrict__ Pf) {
@@ -144,26 +144,64 @@ k_prolong(const S* __restrict__ U, const int* __restrict__ E2S, const double* __
     Us[el][r % 5][r / 5] = Ub[t];
   }
   __syncthreads();
-  // volume prims
+  // Volume prims.  On Gauss-Lobatto nodes a face trace is the face node's own state, so the node's
+  // thread writes the traces of the faces it lies on (the same bits as a second ConsToPrim of the
+  // copied trace, without its FP64 work).
   for (int t = threadIdx.x; t < nloc * n3; t += blockDim.x) {
     int el = t / n3, node = t - el * n3;
     R prim[6], srho;
+    R uo[5];
     if constexpr (C32) {
-      const R c[4] = {(R)Us[el][0][node], (R)Us[el][1][node], (R)Us[el][2][node], (R)Us[el][3][node]};
+      const R c[4] = {narrow<R>(Us[el][0][node]), narrow<R>(Us[el][1][node]), narrow<R>(Us[el][2][node]),
+                      narrow<R>(Us[el][3][node])};
+      if (L.gauss) {
 #pragma unroll
-      for (int v = 0; v < 4; ++v) Cs[el][v][node] = c[v];
-      cons_to_prim_mixed(c, (double)Us[el][4][node], gas, prim, srho);
+        for (int v = 0; v < 4; ++v) Cs[el][v][node] = c[v];
+      }
+      const double E = Us[el][4][node];
+      cons_to_prim_mixed(c, E, gas, prim, srho);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) uo[v] = c[v];
+      uo[4] = R(0);
+      if (!L.gauss) uo[4] = narrow<R>(E);
     } else {
       const S u[5] = {Us[el][0][node], Us[el][1][node], Us[el][2][node], Us[el][3][node], Us[el][4][node]};
       cons_to_prim_d(u, gas, prim, srho);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) uo[v] = (R)u[v];
     }
     R* P = Pvol + (size_t)(e0 + el) * 7 * n3 + node;
 #pragma unroll
     for (int c = 0; c < 6; ++c) P[c * n3] = prim[c];
     P[6 * n3] = srho;
+    if (!L.gauss) {
+      const int i = node % n, j = (node / n) % n, k = node / n2;
+      const int e = e0 + el;
+      // local side ls, face coordinates (a,b) of this node on it (face_node(n, ls, a, b, 0 or N) == node)
+      auto put = [&](int ls, int a, int b) {
+        const int side = E2S[(e * 6 + ls - 1) * 2 + 0];
+        const int flip = E2S[(e * 6 + ls - 1) * 2 + 1];
+        int p, q;
+        s2v2_inv(N, a, b, flip, ls, p, q);
+        const int slot = (flip == 0) ? 0 : 1;
+        R* uf = Uf + ((size_t)slot * L.nSides + side) * 5 * n2 + p + n * q;
+        R* pf = Pf + ((size_t)slot * L.nSides + side) * 6 * n2 + p + n * q;
+#pragma unroll
+        for (int v = 0; v < 5; ++v) uf[v * n2] = uo[v];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) pf[c * n2] = prim[c];
+      };
+      if (i == 0) put(L_XI_MINUS, j, k);
+      if (i == N) put(L_XI_PLUS, j, k);
+      if (j == 0) put(L_ETA_MINUS, i, k);
+      if (j == N) put(L_ETA_PLUS, i, k);
+      if (k == 0) put(L_ZETA_MINUS, i, j);
+      if (k == N) put(L_ZETA_PLUS, i, j);
+    }
   }
+  if (!L.gauss) return;
   if constexpr (C32) __syncthreads();
-  // face traces
+  // Gauss nodes: face traces interpolated with L_minus / L_plus (ProlongToFace), then ConsToPrim
   for (int t = threadIdx.x; t < nloc * 6 * n2; t += blockDim.x) {
     int el = t / (6 * n2), r = t - el * 6 * n2;
     int ls = r / n2 + 1, pq = r - (ls - 1) * n2;
@@ -176,47 +214,33 @@ k_prolong(const S* __restrict__ U, const int* __restrict__ E2S, const double* __
     R prim[6], srho;
     R uo[5];
     if constexpr (C32) {
+      const R* Lv = Lf[is_minus(ls) ? 0 : 1];
+      const double* Ld = is_minus(ls) ? sb.Lm : sb.Lp;
+      const int n0 = face_node(n, ls, a, b, 0);
       R c[4];
-      double E;
-      if (!L.gauss) {
-        const int node = face_node(n, ls, a, b, is_minus(ls) ? 0 : N);
 #pragma unroll
-        for (int v = 0; v < 4; ++v) c[v] = Cs[el][v][node];
-        E = Us[el][4][node];
-      } else {
-        const R* Lv = Lf[is_minus(ls) ? 0 : 1];
-        const double* Ld = is_minus(ls) ? sb.Lm : sb.Lp;
-        const int n0 = face_node(n, ls, a, b, 0);
+      for (int v = 0; v < 4; ++v) c[v] = Cs[el][v][n0] * Lv[0];
+      double E = Us[el][4][n0] * Ld[0];
 #pragma unroll
-        for (int v = 0; v < 4; ++v) c[v] = Cs[el][v][n0] * Lv[0];
-        E = Us[el][4][n0] * Ld[0];
+      for (int l = 1; l < n; ++l) {
+        const int nl = face_node(n, ls, a, b, l);
 #pragma unroll
-        for (int l = 1; l < n; ++l) {
-          const int nl = face_node(n, ls, a, b, l);
-#pragma unroll
-          for (int v = 0; v < 4; ++v) c[v] = c[v] + Cs[el][v][nl] * Lv[l];
-          E = E + Us[el][4][nl] * Ld[l];
-        }
+        for (int v = 0; v < 4; ++v) c[v] = c[v] + Cs[el][v][nl] * Lv[l];
+        E = E + Us[el][4][nl] * Ld[l];
       }
       cons_to_prim_mixed(c, E, gas, prim, srho);
 #pragma unroll
       for (int v = 0; v < 4; ++v) uo[v] = c[v];
-      uo[4] = (R)E;
+      uo[4] = narrow<R>(E);
     } else {
       S u[5];
-      if (!L.gauss) {
-        int node = face_node(n, ls, a, b, is_minus(ls) ? 0 : N);
+      const double* Lv = is_minus(ls) ? sb.Lm : sb.Lp;
 #pragma unroll
-        for (int v = 0; v < 5; ++v) u[v] = Us[el][v][node];
-      } else {
-        const double* Lv = is_minus(ls) ? sb.Lm : sb.Lp;
+      for (int v = 0; v < 5; ++v) {
+        S s = Us[el][v][face_node(n, ls, a, b, 0)] * Lv[0];
 #pragma unroll
-        for (int v = 0; v < 5; ++v) {
-          S s = Us[el][v][face_node(n, ls, a, b, 0)] * Lv[0];
-#pragma unroll
-          for (int l = 1; l < n; ++l) s = s + Us[el][v][face_node(n, ls, a, b, l)] * Lv[l];
-          u[v] = s;
-        }
+        for (int l = 1; l < n; ++l) s = s + Us[el][v][face_node(n, ls, a, b, l)] * Lv[l];
+        u[v] = s;
       }
       cons_to_prim_d(u, gas, prim, srho);
 #pragma unroll
@@ -771,7 +795,7 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
       if (SPLIT < 0) {
         // EvalTransformedEulerFlux3D_fast (flux.f90:137-186) / EvalTransformedEulerDiffFlux3D (:509-614)
         const S* Un = U + ((size_t)e * n3 + node) * 5;
-        const R m1 = (R)Un[1], m2 = (R)Un[2], m3 = (R)Un[3], E = (R)Un[4];
+        const R m1 = narrow<R>(Un[1]), m2 = narrow<R>(Un[2]), m3 = narrow<R>(Un[3]), E = narrow<R>(Un[4]);
         const R p = P[4 * n3], srho = P[6 * n3];  // p: momentum pressure (p' in the mixed form)
         const R Ep = (E + p_abs(p, gas)) * srho;
 #pragma unroll
@@ -832,7 +856,7 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
     if (active) {
       const S* Un = U + ((size_t)e * n3 + node) * 5;
       const R* P = Pvol + (size_t)e * 7 * n3 + node;
-      const R E = (R)Un[4];
+      const R E = narrow<R>(Un[4]);
       const R rho = P[0], uu = P[n3], vv = P[2 * n3], ww = P[3 * n3], pm = P[4 * n3];
       Ae[S_RHO * n3 + snode] = rho;
       Ae[S_AUX * n3 + snode] = pair_aux<SPLIT, R>(rho, uu, vv, ww, E, p_abs(pm, gas), P[6 * n3]);
@@ -841,9 +865,9 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
       Ae[S_W * n3 + snode] = ww;
       Ae[S_PM * n3 + snode] = (SPLIT == DG_SPLIT_PI) ? R(4) * pm : pm;  // PI: 4p (exact scaling)
       if constexpr (SPLIT != DG_SPLIT_PI) {
-        Ae[S_M1 * n3 + snode] = (R)Un[1];
-        Ae[S_M2 * n3 + snode] = (R)Un[2];
-        Ae[S_M3 * n3 + snode] = (R)Un[3];
+        Ae[S_M1 * n3 + snode] = narrow<R>(Un[1]);
+        Ae[S_M2 * n3 + snode] = narrow<R>(Un[2]);
+        Ae[S_M3 * n3 + snode] = narrow<R>(Un[3]);
       }
       if constexpr (MST) {
         const R* Mn = Met + (size_t)e * 10 * n3 + node;
@@ -1038,9 +1062,9 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
     val = val * R(-1);
     val = val * sj;
     if (rkmode == 0) {
-      rk.Ut[g + v] = (S)val;
+      rk.Ut[g + v] = widen<S>(val);
     } else {
-      const S utmp = rk.Ut_tmp[g + v] * rk.mRKA + (S)val;
+      const S utmp = rk.Ut_tmp[g + v] * rk.mRKA + widen<S>(val);
       rk.Ut_tmp[g + v] = utmp;
       rk.U[g + v] = rk.U[g + v] + utmp * rk.b_dt;
     }

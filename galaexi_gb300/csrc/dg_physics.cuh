@@ -9,8 +9,10 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
+#include <type_traits>
 #include "../../include/galaexi_gb300.h"
 #include "dg_dual.cuh"
+#include "dg_convert.cuh"
 
 namespace gx {
 
@@ -28,6 +30,17 @@ template <typename R> struct Gas {
 template <typename R> struct OffsetOf { static constexpr bool v = false; };
 template <> struct OffsetOf<float> { static constexpr bool v = true; };
 
+// compute type R from a state value of type S (FP64, or dual numbers in the tangent-linear operator)
+template <typename R, typename S> __device__ __forceinline__ R narrow(const S& x) {
+  if constexpr (OffsetOf<R>::v && std::is_same<S, double>::value) return f64_to_f32_rn(x);
+  else return (R)x;
+}
+// state type S from a compute-type value x
+template <typename S, typename R> __device__ __forceinline__ S widen(const R& x) {
+  if constexpr (std::is_same<R, float>::value && std::is_same<S, double>::value) return f32_to_f64(x);
+  else return (S)x;
+}
+
 // ConsToPrim of the mixed form from FP32 density and momenta c and the FP64 energy E: velocities and
 // kinetic energy in FP32 (relative error ~1e-7 of quantities that are themselves rounded to FP32), the
 // energy difference E - ke and p' = p - p_ref in FP64, where the cancellation at low Mach would lose
@@ -37,14 +50,14 @@ __device__ __forceinline__ void cons_to_prim_mixed(const R c[4], double E, const
   const R sr = R(1) / c[0];
   const R v1 = c[1] * sr, v2 = c[2] * sr, v3 = c[3] * sr;
   const R ke = R(0.5) * (c[1] * v1 + c[2] * v2 + c[3] * v3);
-  const double p = g.kappaM1D * (E - (double)ke);
+  const double p = g.kappaM1D * (E - f32_to_f64(ke));
   srho = sr;
   prim[0] = c[0];
   prim[1] = v1;
   prim[2] = v2;
   prim[3] = v3;
-  prim[4] = (R)(p - g.prefD);
-  prim[5] = (R)p * sr * g.sR;
+  prim[4] = f64_to_f32_rn(p - g.prefD);
+  prim[5] = f64_to_f32_rn(p) * sr * g.sR;
 }
 
 // ConsToPrim (idealgas/eos.f90:212-239) from the FP64 state: rho, u, v, w, p (p' in the mixed form), T, 1/rho
@@ -59,7 +72,7 @@ __device__ __forceinline__ void cons_to_prim_d(const S u[5], const Gas<R>& g, R 
     prim[4] = g.kappaM1 * ((R)u[4] - R(0.5) * ((R)u[1] * prim[1] + (R)u[2] * prim[2] + (R)u[3] * prim[3]));
     prim[5] = prim[4] * srho * g.sR;
   } else {
-    const R c[4] = {(R)u[0], (R)u[1], (R)u[2], (R)u[3]};
+    const R c[4] = {narrow<R>(u[0]), narrow<R>(u[1]), narrow<R>(u[2]), narrow<R>(u[3])};
     cons_to_prim_mixed(c, (double)u[4], g, prim, srho);
   }
 }
