@@ -114,8 +114,9 @@ template <int NP> struct EPBof { static constexpr int v = (NP * NP * NP >= 128) 
 __host__ __device__ constexpr int lift_ps_slots(int NP) { return 5 * NP * NP * NP > 30 * NP * NP ? 5 * NP * NP * NP : 30 * NP * NP; }
 
 // =====================================================================================
-// k_prolong: ConsToPrim_Volume + ProlongToFace_CUDA + GetPrimitiveStateSurface (at least two
-// blocks per SM: 0.57 -> 0.38 ms per stage at N=7, 24^3 elements)
+// k_prolong: ConsToPrim_Volume + ProlongToFace_CUDA + GetPrimitiveStateSurface.  At least two
+// blocks per SM for the FP64 form (FP64-issue bound); three for the mixed form, whose FP64 work is
+// only E - ke and p - p_ref once its conversions run on the integer pipes (latency bound).
 // =====================================================================================
 template <int NP, typename R, typename S = double>
 __global__ void __launch_bounds__(EPBof<NP>::v * NP * NP * NP, OffsetOf<R>::v ? 3 : 2)
