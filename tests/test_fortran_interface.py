@@ -3,8 +3,10 @@
 No Fortran compiler exists in this image, so the module is checked by reading it: every function the C
 header declares has exactly one BIND(C) procedure with the same number of arguments, exported by
 libgalaexi_gb300.so; the BIND(C) dg_config type lists the C struct's fields in the same order with
-matching kinds; the integer parameters equal the header's #define constants, all of which are
-present; and every line fits Fortran's 132-character free-form limit.
+matching kinds; every argument is passed as its C parameter expects (scalars by value, pointers
+by reference to data of the same kind or as TYPE(C_PTR) values); the integer parameters equal
+the header's #define constants, all of which are present; and every line fits Fortran's
+132-character free-form limit.
 """
 import os
 import re
@@ -106,3 +108,66 @@ def test_constants_and_line_length():
     assert f_codes == c_codes
     for i, line in enumerate(open(F90), 1):
         assert len(line.rstrip("\n")) <= 132, "line %d longer than 132 characters" % i
+
+
+def _c_param(decl):
+    """(base type, pointer depth) of a C parameter declaration such as 'const double* d_U'."""
+    depth = decl.count("*")
+    words = [w for w in re.split(r"[\s\*]+", decl) if w and w != "const"]
+    return " ".join(words[:-1]), depth
+
+
+def _fortran_interfaces():
+    """{C name: (result kind or None, [(dummy, type spec, has VALUE)])} of the interface block."""
+    out, cur = {}, None
+    for st in _fortran_statements():
+        m = re.match(r"(?:(.+?)\s+)?(FUNCTION|SUBROUTINE)\s+(\w+)\s*\(([^)]*)\)\s*BIND\s*\(\s*C\s*,\s*NAME\s*=\s*'(\w+)'",
+                     st, flags=re.I)
+        if m:
+            dummies = [a.strip() for a in m.group(4).split(",") if a.strip()]
+            cur = {"result": (m.group(1) or "").upper() or None, "dummies": dummies, "decl": {}}
+            out[m.group(5)] = cur
+            continue
+        if cur is None or re.match(r"(IMPORT|END\s)", st, flags=re.I):
+            if re.match(r"END\s+(FUNCTION|SUBROUTINE)", st, flags=re.I):
+                cur = None
+            continue
+        spec, names = st.split("::")
+        attrs = [a.strip().upper() for a in spec.split(",")]
+        for nm in re.split(r",(?![^(]*\))", names):
+            cur["decl"][re.match(r"\s*(\w+)", nm).group(1).lower()] = (attrs[0], "VALUE" in attrs[1:])
+    return {k: (v["result"], [(d, *v["decl"][d.lower()]) for d in v["dummies"]]) for k, v in out.items()}
+
+
+def test_bind_c_argument_passing_matches_c_types():
+    """Each dummy is passed as the C parameter expects: scalars by value, pointers either by reference
+    (host data of the same kind) or as a TYPE(C_PTR) value (device or opaque pointers)."""
+    text, decls = _c_declarations()
+    rets = {m.group(2): m.group(1).splitlines()[-1].replace("const", "").strip()
+            for m in re.finditer(r"\b([A-Za-z_][\w\s\*]*?)\b(dg_\w+)\s*\([^;{}]*?\)\s*;", text)}
+    kind = {"int": "INTEGER(C_INT)", "double": "REAL(C_DOUBLE)", "size_t": "INTEGER(C_SIZE_T)",
+            "long long": "INTEGER(C_LONG_LONG)", "char": "CHARACTER(KIND=C_CHAR)"}
+    ifaces = _fortran_interfaces()
+    assert sorted(ifaces) == sorted(decls)
+    for cname, (result, dummies) in ifaces.items():
+        ret = rets[cname]
+        if ret == "void":
+            assert result is None, cname
+        elif ret.replace(" ", "") == "char*":
+            assert result == "TYPE(C_PTR)", cname
+        else:
+            assert result == kind[ret], (cname, ret, result)
+        for (dname, ftype, by_value), cdecl in zip(dummies, decls[cname]):
+            base, depth = _c_param(cdecl)
+            what = (cname, dname, cdecl, ftype, by_value)
+            if depth == 0:
+                assert ftype == kind[base] and by_value, what
+            elif base in ("void", "dg_ctx") and depth == 1:
+                assert ftype == "TYPE(C_PTR)" and by_value, what
+            elif base == "dg_ctx" and depth == 2:
+                assert ftype == "TYPE(C_PTR)" and not by_value, what
+            elif base == "dg_config":
+                assert ftype == "TYPE(DG_CONFIG)" and not by_value, what
+            else:
+                assert depth == 1, what
+                assert (ftype == kind[base] and not by_value) or (ftype == "TYPE(C_PTR)" and by_value), what
