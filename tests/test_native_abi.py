@@ -129,3 +129,39 @@ def test_fill_ini_tgv_and_vortex():
     r2 = (xv[..., 0] - 5) ** 2 + (xv[..., 1] - 5) ** 2
     du = -5 / (2 * math.pi) * np.exp((1 - r2) / 2) * (xv[..., 1] - 5)
     assert np.allclose(V[..., 1] / V[..., 0], 1 + du)
+
+
+def test_ctypes_signatures_match_header():
+    """The ctypes argtypes/restype of every entry point agree with the C declaration: same count,
+    scalars with the matching ctypes type, pointers as pointers (c_void_p, c_char_p or POINTER(...))."""
+    import ctypes
+    import re
+    from galaexi_gb300 import _native as nat
+    text = re.sub(r"/\*.*?\*/", " ", open(os.path.join(ROOT, "include", "galaexi_gb300.h")).read(), flags=re.S)
+    decls = {}
+    for m in re.finditer(r"\b([A-Za-z_][\w\s\*]*?)\b(dg_\w+)\s*\(([^;{}]*?)\)\s*;", text):
+        args = [a.strip() for a in m.group(3).split(",") if a.strip() and a.strip() != "void"]
+        decls[m.group(2)] = (m.group(1).splitlines()[-1].replace("const", "").strip(), args)
+    assert sorted(decls) == sorted(nat._SIGS)
+    scalar = {"int": ctypes.c_int, "double": ctypes.c_double, "size_t": ctypes.c_size_t,
+              "long long": ctypes.c_longlong}
+
+    def is_pointer(t):
+        return t in (ctypes.c_void_p, ctypes.c_char_p) or (isinstance(t, type) and issubclass(t, ctypes._Pointer))
+
+    for name, (res, args) in nat._SIGS.items():
+        ret, cargs = decls[name]
+        if ret == "void":
+            assert res is None, name
+        elif "*" in ret:
+            assert is_pointer(res), name
+        else:
+            assert res is scalar[ret], (name, ret)
+        assert len(args) == len(cargs), name
+        for a, c in zip(args, cargs):
+            words = [w for w in re.split(r"[\s\*]+", c) if w and w != "const"]
+            base = " ".join(words[:-1])
+            if "*" in c:
+                assert is_pointer(a), (name, c, a)
+            else:
+                assert a is scalar[base], (name, c, a)
