@@ -174,7 +174,9 @@ def test_window_checkpoint_plans_agree(nSteps):
 
 def test_window_end_state_over_start_state_and_scratch_size():
     """The end state may be written over the start state; the scratch estimate covers what the
-    adjoint allocates besides its checkpoints."""
+    adjoint allocates besides its checkpoints.  The memory check reads the device's free memory, so
+    it needs the GPU to itself: with other processes allocating on the same device (a parallel
+    pytest run, for instance) their allocations count as used."""
     cfg, m, op, U0, dt, rng = window_case()
     nSteps = 6
     state = U0.numel() * 8
