@@ -115,11 +115,15 @@ __host__ __device__ constexpr int lift_ps_slots(int NP) { return 5 * NP * NP * N
 
 // =====================================================================================
 // k_prolong: ConsToPrim_Volume + ProlongToFace_CUDA + GetPrimitiveStateSurface.  At least two
-// blocks per SM for the FP64 form (FP64-issue bound); three for the mixed form, whose FP64 work is
-// only E - ke and p - p_ref once its conversions run on the integer pipes (latency bound).
+// blocks per SM for the FP64 form (FP64-issue bound); three for the mixed form up to N = 7, whose FP64
+// work is only E - ke and p - p_ref once its conversions run on the integer pipes (latency bound).
 // =====================================================================================
+template <int NP, typename R> struct ProlongMinBlocks {
+  // three blocks per SM where they fit the SM's 2048 threads (the mixed form up to N = 7), else two
+  static constexpr int v = (OffsetOf<R>::v && 3 * EPBof<NP>::v * NP * NP * NP <= 2048) ? 3 : 2;
+};
 template <int NP, typename R, typename S = double>
-__global__ void __launch_bounds__(EPBof<NP>::v * NP * NP * NP, OffsetOf<R>::v ? 3 : 2)
+__global__ void __launch_bounds__(EPBof<NP>::v * NP * NP * NP, ProlongMinBlocks<NP, R>::v)
 k_prolong(const S* __restrict__ U, const int* __restrict__ E2S, const double* __restrict__ Lm,
           const double* __restrict__ Lp, Gas<R> gas, Launch L, R* __restrict__ Pvol, R* __restrict__ Uf,
           R* __restrict__ Pf) {
