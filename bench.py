@@ -20,6 +20,8 @@ import sys
 import threading
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -34,11 +36,17 @@ WORKLOADS = {
 ALG_FLOPS_N7 = {"prolong": 14.0, "lift": 30 * 8 + 75 + 270 / 8 + 15, "face": 1200 / 8,
                 "volume": 135 * 7 + 115 + 30 * 8 + 60 / 8 + 30}
 ALG_BYTES_N7 = 510.0  # compulsory HBM bytes per DOF-stage of a fully fused implementation (FP64)
-# ncu on the 16^3 case of the same kernels (profiles/dgsem_fp64_kernels_tgv_n7_16cube.md): DRAM bytes
-# and executed FP64 thread-instructions (DFMA+DADD+DMUL) per DOF for one k_volume launch; traffic
-# grows with the number of elements, so it is scaled to a launch by nDOF
+# DRAM traffic and executed FP64 instructions are not measurable inside this process; they come from
+# one ncu capture of the same kernels on the 16^3 case of this workload (2 097 152 DOF; traffic grows
+# with the number of elements, so it is scaled per DOF), taken with the source tree of this file.
+#   FP64 k_volume: dram__bytes_read.sum + dram__bytes_write.sum per DOF of one launch, and the executed
+#   FP64 thread-instructions (DFMA + DADD + DMUL) per DOF
 KVOL_DRAM_BYTES_PER_DOF = (670.293248e6 + 143.461888e6) / 2097152
 KVOL_FP64_INSTR_PER_DOF = 519.0
+KVOL_CAPTURE = "ncu --set full, one k_volume launch, tgv_n7_16cube, 2026-12-03"
+#   mixed form: the four kernels of one stage (k_prolong, k_lift, k_face, k_volume), bytes per DOF
+MIXED_STAGE_DRAM_BYTES_PER_DOF = (84e6 + 72e6 + 165e6 + 129e6 + 145e6 + 9e6 + 419e6 + 127e6) / 2097152
+MIXED_TRAFFIC_SOURCE = "ncu dram__bytes_read+write of the four mixed-form kernels of one stage, tgv_n7_16cube, 2026-12-03"
 FP64_ISSUE_PER_CYCLE = 304  # sm__sass_thread_inst_executed_op_dfma_pred_on.sum.peak_sustained (152 SMs x 2)
 TGV_R = 71.42857
 CFL = 0.8  # CFLscale / DFLscale of the reference's TGV regression (regressioncheck/checks/tgv/split/parameter.ini)
@@ -58,8 +66,9 @@ def parse():
     ap.add_argument("--no-profile", action="store_true", help="skip the per-kernel event timing and peak kernels")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the mixed-precision comparisons and the adjoint measurement")
-    ap.add_argument("--adjoint-fd", type=int, default=0,
+    ap.add_argument("--adjoint-fd", type=int, default=16,
                     help="central-difference check of the adjoint gradient along this many random directions")
+    ap.add_argument("--no-scale64", action="store_true", help="skip the 64^3 scale case among the extras")
     ap.add_argument("--adjoint-steps", type=int, default=None,
                     help="steps of the adjoint window (default 200 for the N=5 case, 50 for --only scale64)")
     ap.add_argument("--curved-ne", type=int, default=32,
@@ -139,52 +148,75 @@ def max_over_ranks(world, x, device=None):
     return float(t.item())
 
 
+def reference_setup(workload):
+    """The workload's oracle, mesh and initial state built without the product library (oracle/
+    standalone.py: periodic box with the oracle's own metrics, numpy TGV state)."""
+    from oracle.oracle import Oracle
+    from oracle.standalone import PeriodicBox, config, tgv_state
+    w = WORKLOADS[workload]
+    cfg = config(w["N"], "gauss-lobatto", w["Riemann"], w["SplitDG"], parabolic=w["parabolic"], R=TGV_R, mu0=w["mu0"])
+    box = PeriodicBox(w["N"], 2, w["ne"], (-math.pi,) * 3, (math.pi,) * 3)
+    U0 = tgv_state(box.Elem_xGP, mach=0.1, R=TGV_R)
+    return Oracle(cfg, box, geometry="mesh"), box, U0
+
+
 def cpu_baseline(workload, threads=None, target_s=12.0, warmup=1):
-    """The oracle (CPU restatement of the reference formulas, OpenMP) on a bounded sample:
-    full LSERK steps on an 8^3-element box of the same N/form (a 1/27 slice of the 24^3 workload)."""
-    import numpy as np  # noqa: F401
-    import galaexi_gb300 as gx
-    from oracle.oracle import Oracle, set_threads
+    """The oracle (CPU restatement of the reference formulas, OpenMP) on a bounded sample of the
+    workload itself: as many full LSERK steps of the whole mesh as fit in about target_s."""
+    from oracle.oracle import set_threads
     w = WORKLOADS[workload]
     nthreads = set_threads(threads or os.cpu_count() or 1)
-    ne = 8
-    cfg = gx.config(N=w["N"], NodeType="gauss-lobatto", Riemann=w["Riemann"], SplitDG=w["SplitDG"],
-                    parabolic=w["parabolic"], mu0=w["mu0"], R=TGV_R)
-    mesh = gx.Mesh(w["N"], 2, ne, ne, ne, (-math.pi,) * 3, (math.pi,) * 3)
-    U0 = gx.tgv_state(mesh, mach=0.1, R=TGV_R)
-    o = Oracle(cfg, mesh)
+    o, box, U0 = reference_setup(workload)
     dt, _ = o.calc_timestep(U0, CFL, DFL)
-    # untimed warm-up steps; the last one sizes the timed sample
-    U, Ut = U0, None
+    U, Ut = np.array(U0), np.zeros_like(U0)
     for _ in range(max(1, warmup)):
         t0 = time.perf_counter()
-        U, Ut = o.lserk_steps(U, dt, 1, Ut_tmp=Ut)
+        o.lserk_steps_inplace(U, Ut, dt, 1)
         one = time.perf_counter() - t0
     steps = max(1, min(2000, int(target_s / max(one, 1e-3))))
     t0 = time.perf_counter()
-    U, Ut = o.lserk_steps(U, dt, steps, Ut_tmp=Ut)
+    o.lserk_steps_inplace(U, Ut, dt, steps)
     el = time.perf_counter() - t0
-    val = mesh.nDOF * 5 * steps / el
+    o.close()
+    val = box.nDOF * 5 * steps / el
     return {"value": val, "unit": "DOF-stage/s", "cores": nthreads, "kind": "port",
-            "sample": "%d LSERK steps (5 stages) on %d^3 elements N=%d (%d DOF), %.1f s" % (
-                steps, ne, w["N"], mesh.nDOF, el)}
+            "sample": "%d LSERK steps (5 stages) of the whole %d^3-element N=%d mesh (%d DOF), %.1f s" % (
+                steps, w["ne"], w["N"], box.nDOF, el),
+            "pid_s": nthreads * el / (box.nDOF * 5 * steps)}
 
 
 def run_reference(args, world, rank):
     """Reference arm: the CPU restatement of the reference's formulas (the reference itself is CUDA
-    Fortran and has no CPU build; it cannot be compiled here), all host threads, same metric."""
+    Fortran and has no CPU build; it cannot be compiled here), all host threads, on the workload
+    itself: W untimed and K timed LSERK steps of the whole mesh.  Mesh, metrics and state come from
+    the oracle and numpy (no part of the product library is loaded)."""
     if rank != 0:
         return
+    from oracle.oracle import set_threads
     w = WORKLOADS[args.workload]
-    res = cpu_baseline(args.workload, target_s=max(5.0, 2.0 * args.steps), warmup=args.warmup)
-    line = {"metric": "DOF-stage updates/s", "value": res["value"], "unit": "DOF-stage/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic TGV state",
-            "impl": "reference",
-            "config": {"workload": args.workload, "N": w["N"], "elements_per_dir": w["ne"], "form": "split PI",
-                       "riemann": w["Riemann"], "lifting": "BR1"},
+    nthreads = set_threads(os.cpu_count() or 1)
+    o, box, U0 = reference_setup(args.workload)
+    dt, _ = o.calc_timestep(U0, CFL, DFL)
+    U, Ut = np.array(U0), np.zeros_like(U0)
+    o.lserk_steps_inplace(U, Ut, dt, max(0, args.warmup))
+    t0 = time.perf_counter()
+    o.lserk_steps_inplace(U, Ut, dt, args.steps)
+    el = time.perf_counter() - t0
+    o.close()
+    val = box.nDOF * 5 * args.steps / el
+    res = {"value": val, "unit": "DOF-stage/s", "cores": nthreads, "kind": "port",
+           "sample": "%d timed LSERK steps (after %d untimed) of the whole %d^3-element N=%d mesh (%d DOF), %.1f s"
+                     % (args.steps, args.warmup, w["ne"], w["N"], box.nDOF, el),
+           "pid_s": nthreads * el / (box.nDOF * 5 * args.steps)}
+    line = {"metric": "DOF-stage updates/s", "value": val, "unit": "DOF-stage/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (TGV initial state, generated mesh)", "impl": "reference",
+            "config": {"workload": args.workload, "N": w["N"], "elements_per_dir": w["ne"], "nDOF": box.nDOF,
+                       "form": "split PI", "riemann": w["Riemann"], "lifting": "BR1", "precision": "fp64",
+                       "dt": dt},
             "cpu_baseline": res,
-            "e2e": {"value": res["value"], "unit": "DOF-stage/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": val, "unit": "DOF-stage/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
@@ -281,9 +313,14 @@ def run_ours(args, world, rank, local):
         cpu = cpu_baseline(args.workload)
     extras = {}
     if not args.no_extras and args.precision == "fp64":
-        extras["mixed_vs_fp64"] = mixed_vs_fp64_tgv(args.workload, args.steps, stream)
+        # the mixed form over the workload's 200 steps, with its own roofline
+        extras["mixed_vs_fp64"] = mixed_vs_fp64_tgv(args.workload, 200, stream, roofline=not args.no_profile)
         extras["mixed_vs_fp64_curved_br2"] = mixed_vs_fp64_curved_br2(stream)
+        # the discrete adjoint of 200 steps on the N=5 16^3 TGV, checked along 16 seeded directions
         extras["adjoint"] = adjoint_tgv(stream, steps=args.adjoint_steps or 200, fd_dirs=args.adjoint_fd)
+        if not args.no_scale64:
+            # the 64^3 scale case: 100 steps per form, the adjoint of a 50-step window in <= 180 GB
+            extras["scale64"] = scale_c5(stream)
     if rank == 0:
         line = {"metric": "DOF-stage updates/s", "value": value, "unit": "DOF-stage/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -311,9 +348,16 @@ def timed(fn, stream):
     return e0.elapsed_time(e1), r
 
 
-def mixed_vs_fp64_tgv(workload, steps, stream):
+# Compulsory HBM bytes per DOF-stage of the mixed form (FP32 bulk) for a fully fused implementation at
+# N=7: U and Ut_tmp read and written in FP64 (160), FP32 volume metrics and sJ (40), FP32 face geometry
+# (10 values x 3 faces per n^3 nodes: 120/n = 15), the 15 FP32 lifted gradients written and read (120)
+ALG_BYTES_N7_MIXED = 160.0 + 40.0 + 120.0 / 8 + 120.0
+
+
+def mixed_vs_fp64_tgv(workload, steps, stream, roofline=False):
     """Mixed form against the FP64 form on the TGV workload: same initial state, same dt, `steps`
-    LSERK steps each; kinetic-energy and L2 differences of the end states, DOF-stage/s ratio."""
+    LSERK steps each; kinetic-energy, mass and L2 differences of the end states, DOF-stage/s ratio;
+    with roofline=True the mixed stage's per-kernel times and its HBM / FP32 roofline."""
     import torch
     import galaexi_gb300 as gx
     w = WORKLOADS[workload]
@@ -339,10 +383,46 @@ def mixed_vs_fp64_tgv(workload, steps, stream):
            "ke_rel_err": abs(kem - ke64) / abs(ke64),
            "l2_rel": float((out["mixed"][1] - out["fp64"][1]).norm() / out["fp64"][1].norm()),
            "mass_rel_diff": abs(out["mixed"][2][0] - out["fp64"][2][0]) / abs(out["fp64"][2][0]),
-           "reference": "FP64 path of this library (matches the oracle to <=1e-12 per evaluation)"}
+           "reference": "FP64 path of this library (equal to the oracle to <=1e-12 per evaluation and "
+                        "<=1e-10 after 100 steps of this workload)"}
+    if roofline:
+        res["roofline"] = mixed_roofline(ops["mixed"], U0, dt, stream, mesh.nDOF)
     for op in ops.values():
         op.close()
     return res
+
+
+def mixed_roofline(op, U0, dt, stream, nDOF):
+    """Per-kernel CUDA-event times of one mixed-form stage (dg_profile_stage) and the stage's rooflines:
+    HBM on the compulsory FP32-bulk bytes, FP32 on the algorithmic flops."""
+    import ctypes
+    import torch
+    from galaexi_gb300 import _native as nat
+    out = (ctypes.c_double * 5)()
+    Up, Utp = U0.clone(), torch.zeros_like(U0)
+    nat.check(nat.lib().dg_profile_stage(op._h, ctypes.c_void_p(Up.data_ptr()), ctypes.c_void_p(Utp.data_ptr()),
+                                         dt, 20, out, ctypes.c_void_p(stream.cuda_stream)), "dg_profile_stage")
+    kms = {"prolong": out[0], "lift": out[1], "face": out[2], "volume": out[3], "stage": out[4]}
+    peak32 = ctypes.c_double()
+    nat.check(nat.lib().dg_measure_fma_peak(1, ctypes.byref(peak32)), "fma peak fp32")
+    hbm_peak = measured_peaks().get("hbm_gbs")
+    stage_s = kms["stage"] * 1e-3
+    gbs = ALG_BYTES_N7_MIXED * nDOF / stage_s * 1e-9
+    tflops = sum(ALG_FLOPS_N7.values()) * nDOF / stage_s * 1e-12
+    return {"bound": "hbm", "unit": "GB/s", "alg_bytes_per_dof_stage": ALG_BYTES_N7_MIXED, "achieved": gbs,
+            "peak": hbm_peak, "frac": gbs / hbm_peak if hbm_peak else None,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)",
+            "traffic_per_dof_stage": MIXED_STAGE_DRAM_BYTES_PER_DOF, "traffic_source": MIXED_TRAFFIC_SOURCE,
+            "fp32_achieved_tflops": tflops, "fp32_peak_tflops_measured": peak32.value * 1e-3,
+            "fp32_frac": tflops / (peak32.value * 1e-3), "kernel_ms": kms}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
 
 
 def mixed_vs_fp64_curved_br2(stream, steps=500, ne=32):
@@ -498,8 +578,11 @@ def adjoint_tgv(stream, steps=200, fd_dirs=0):
         for _ in range(fd_dirs):
             v = torch.from_numpy(rng.standard_normal(tuple(U0.shape))).cuda()
             dirs.append(v / v.norm())
-        # central differences at eps = 1e-6 (and 1e-4 to show the round-off share of the difference)
-        for eps in (1e-6, 1e-4):
+        # central differences at the specified eps = 1e-6 and at larger eps: along a unit direction of
+        # the 4.4 M-dimensional state J changes by ~1e-4 eps, so at small eps the round-off of J (and of
+        # the two trajectories) dominates the difference quotient; the sweep shows where round-off and
+        # truncation balance
+        for eps in (1e-6, 1e-5, 1e-4, 1e-3):
             errs = []
             for v in dirs:
                 Jp = op.kinetic_energy(fwd(op, U0 + eps * v))
@@ -508,6 +591,7 @@ def adjoint_tgv(stream, steps=200, fd_dirs=0):
                 ad = float((G * v).sum())
                 errs.append(abs(fd - ad) / abs(ad))
             res["fd_max_rel_err_eps%.0e" % eps] = max(errs)
+            res["fd_median_rel_err_eps%.0e" % eps] = float(np.median(errs))
         res["fd_directions"] = fd_dirs
         # exact directional derivatives from the tangent-linear model (dual numbers through the same
         # 200 steps): <dJ/dU(t_end), Udot(t_end)> against <dJ/dU0, v>
@@ -552,11 +636,7 @@ def profile_roofline(args, op, U, dt, stream, nDOF):
     peak = peak64.value if args.precision == "fp64" else peak32.value
     vol_flops = ALG_FLOPS_N7["volume"] * nDOF
     achieved = vol_flops / (kms["volume"] * 1e-3) * 1e-12
-    mp = {}
-    try:
-        mp = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
+    mp = measured_peaks()
     hbm_peak = mp.get("hbm_gbs", 6800.0)
     stage_s = kms["stage"] * 1e-3
     roofline = {
@@ -566,7 +646,7 @@ def profile_roofline(args, op, U, dt, stream, nDOF):
         "peak_source": "FMA-chain microkernel measured in this run (no FP64/FP32 CUDA-core peak in MEASURED_PEAKS.json)",
         "alg_flops_per_dof": ALG_FLOPS_N7["volume"],
         "traffic": KVOL_DRAM_BYTES_PER_DOF * nDOF if args.precision == "fp64" else None,
-        "traffic_source": "ncu dram__bytes_read+write of one k_volume launch on 16^3, scaled by nDOF",
+        "traffic_source": "dram__bytes_read+write per DOF of one k_volume launch, scaled by nDOF (%s)" % KVOL_CAPTURE,
         "exec_fp64_issue_frac": (KVOL_FP64_INSTR_PER_DOF * nDOF / (kms["volume"] * 1e-3))
                                 / (FP64_ISSUE_PER_CYCLE * 2.07e9) if args.precision == "fp64" else None,
         "kernel_ms": kms,
@@ -574,7 +654,9 @@ def profile_roofline(args, op, U, dt, stream, nDOF):
                   "achieved_tflops": sum(ALG_FLOPS_N7.values()) * nDOF / stage_s * 1e-12,
                   "alg_bytes_per_dof_stage": ALG_BYTES_N7,
                   "hbm_gbs_alg": ALG_BYTES_N7 * nDOF / stage_s * 1e-9,
-                  "hbm_peak_gbs": hbm_peak, "hbm_frac_of_measured": ALG_BYTES_N7 * nDOF / stage_s * 1e-9 / hbm_peak},
+                  "hbm_peak_gbs": hbm_peak,
+                  "hbm_peak_source": "MEASURED_PEAKS.json" if "hbm_gbs" in mp else "fallback 6.8 TB/s",
+                  "hbm_frac_of_measured": ALG_BYTES_N7 * nDOF / stage_s * 1e-9 / hbm_peak},
         "fp64_peak_tflops_measured": peak64.value * 1e-3,
         "fp32_peak_tflops_measured": peak32.value * 1e-3,
     }

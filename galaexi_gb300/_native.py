@@ -99,7 +99,7 @@ _SIGS = {
     "dg_last_error": (ctypes.c_char_p, []),
     "dg_basis": (_I, [_I, _I] + [_P] * 10),
     "dg_mesh_cartesian_sizes": (_I, [_I, _I, _I, _IP, _IP]),
-    "dg_mesh_cartesian": (_I, [_I, _I, _I, _I, _I, _P, _P, _D] + [_P] * 11),
+    "dg_mesh_cartesian": (_I, [_I, _I, _I, _I, _I, _I, _P, _P, _D] + [_P] * 12),
     "dg_fill_ini": (_I, [_I, _P, _I, ctypes.c_longlong, _P, _D, _D, _D, _P]),
     "dg_profile_stage": (_I, [_P, _P, _P, _D, _I, _DP, _P]),
     "dg_measure_fma_peak": (_I, [_I, _DP]),

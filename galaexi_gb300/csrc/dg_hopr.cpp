@@ -203,7 +203,10 @@ struct MetricOps {
     V_eq_clG = vdm(eqG, clG);
     V_clG_clN = vdm(clG, clN);
     V_clG_ref = vdm(clG, ref);
-    V_ref_N = vdm(ref, sol);
+    // the Jacobian of degree 3 NGeo to the solution nodes: modal projection for N < NGeoRef (the
+    // modal Vandermonde of metrics.f90:289, which keeps the element volume), interpolation otherwise
+    if (N < NGeoRef) gxh::modal_projection(NGeoRef, ref.x.data(), ref.wb.data(), N, sol.x.data(), V_ref_N);
+    else V_ref_N = vdm(ref, sol);
     V_clN_N = vdm(clN, sol);
     // BuildCoords: Vdm_EQNGeo_CLN then MATMUL(Vdm_CLN_N, .) -> EQ(NGeo) -> solution nodes
     const std::vector<double> V_eq_clN = vdm(eqG, clN);
@@ -218,8 +221,8 @@ struct MetricOps {
   }
 };
 
-void flexi_metrics(const MetricOps& O, const double* nodes, int e, double* elem_xgp, double* Mf, double* Mg,
-                   double* Mh, double* sJ, std::vector<double>& JaCL) {
+int flexi_metrics(const MetricOps& O, const double* nodes, int e, double* elem_xgp, double* Mf, double* Mg,
+                  double* Mh, double* sJ, std::vector<double>& JaCL) {
   const int N = O.N, NGeo = O.NGeo, n = N + 1, g = NGeo + 1, n3 = n * n * n, g3 = g * g * g, r = O.NGeoRef + 1;
   std::vector<double> XG(3 * g3), XN(3 * n3), dXG(9 * g3), dXN(9 * n3), tmpG(3 * g3), tmpN(3 * n3);
   change_basis_3d(3, NGeo, NGeo, O.V_eq_clG, nodes, XG.data());
@@ -255,7 +258,14 @@ void flexi_metrics(const MetricOps& O, const double* nodes, int e, double* elem_
              X(3, 1) * (X(1, 2) * X(2, 3) - X(2, 2) * X(1, 3));
   }
   change_basis_3d(1, O.NGeoRef, N, O.V_ref_N, det.data(), detN.data());
-  for (int t = 0; t < n3; ++t) sJ[(size_t)e * n3 + t] = 1. / detN[t];
+  // scaled-Jacobian check of metrics.f90:340-353 (the reference aborts below 0.01)
+  int bad = 0;
+  const double mx = *std::max_element(detN.begin(), detN.end());
+  for (int t = 0; t < n3; ++t) {
+    sJ[(size_t)e * n3 + t] = 1. / detN[t];
+    if (!(detN[t] > 0.)) bad = -1;
+    else if (bad >= 0 && detN[t] / mx < 0.01) bad++;
+  }
   // dXCL_N: interpolated from NGeo (N >= NGeo) or differentiated on CL(N)
   auto NI = [&](int i, int j, int k) { return (size_t)i + n * (j + (size_t)n * k); };
   if (N >= NGeo) {
@@ -312,6 +322,7 @@ void flexi_metrics(const MetricOps& O, const double* nodes, int e, double* elem_
       for (int nn = 0; nn < 3; ++nn) tmpN[3 * t + nn] = JaCL[9 * t + dd * 3 + nn];
     change_basis_3d(3, N, N, O.V_clN_N, tmpN.data(), outs[dd] + (size_t)3 * n3 * e);
   }
+  return bad;
 }
 
 // CalcSurfMetrics (metrics.f90:596-750) for one master side: JaCL_N on the face plane, ChangeBasis2D
@@ -340,6 +351,25 @@ void flexi_surface(const MetricOps& O, const std::vector<double>& JaCL, int loc,
   gxh::surface_metrics(N, loc, JaFace.data(), side, nvec, t1vec, t2vec, surfelem);
 }
 }  // namespace
+
+int gxh::metrics_from_nodes(int N, int node_type, int NGeo, int nElems, const double* nodes, const int* E2S,
+                            double* elem_xgp, double* Mf, double* Mg, double* Mh, double* sJ, double* nvec,
+                            double* t1vec, double* t2vec, double* surfelem) {
+  const MetricOps O(N, NGeo, node_type);
+  const size_t ng3 = (size_t)(NGeo + 1) * (NGeo + 1) * (NGeo + 1);
+  std::vector<double> JaCL;
+  int bad = 0;
+  for (int e = 0; e < nElems; ++e) {
+    const int b = flexi_metrics(O, nodes + ng3 * 3 * e, e, elem_xgp, Mf, Mg, Mh, sJ, JaCL);
+    if (b < 0 || bad < 0) bad = -1;
+    else bad += b;
+    for (int ls = 1; ls <= 6; ++ls) {
+      const int* p = E2S + 3 * ((size_t)e * 6 + ls - 1);
+      if (p[1] == 0) flexi_surface(O, JaCL, ls, (size_t)(p[0] - 1), nvec, t1vec, t2vec, surfelem);
+    }
+  }
+  return bad;
+}
 
 extern "C" int dg_mesh_hopr_sizes(const char* path, int* nElems, int* nSides, int* nBCSides, int* NGeo) {
   if (!nElems || !nSides || !nBCSides || !NGeo) { set_error("dg_mesh_hopr_sizes: null argument"); return DG_ERR_ARG; }
@@ -448,7 +478,6 @@ extern "C" int dg_mesh_hopr(const char* path, int N, int node_type, double* elem
   }
   Hopr H;
   if (!read_hopr(path, H, true)) return DG_ERR_ARG;
-  const int n = N + 1, n2 = n * n, ng = H.NGeo + 1;
   // ElemToSide(3,6,nElems): side (1-based), flip, master flag; SideToElem(5,nSides)
   for (int s = 0; s < H.nSides; ++s)
     for (int c = 0; c < 5; ++c) S2E[(size_t)s * 5 + c] = c >= 2 ? 0 : -1;
@@ -468,14 +497,11 @@ extern "C" int dg_mesh_hopr(const char* path, int N, int node_type, double* elem
     if (q[1] < 0) q[1] = 0;  // BC side: no neighbour
   }
   // geometry: CalcMetrics / CalcSurfMetrics / BuildCoords of the reference, element by element
-  const MetricOps O(N, H.NGeo, node_type);
-  std::vector<double> JaCL;
-  for (int e = 0; e < H.nElems; ++e) {
-    flexi_metrics(O, &H.nodes[(size_t)e * ng * ng * ng * 3], e, elem_xgp, Mf, Mg, Mh, sJ, JaCL);
-    for (int ls = 1; ls <= 6; ++ls) {
-      const size_t slot = (size_t)e * 6 + ls - 1;
-      if (H.master[slot]) flexi_surface(O, JaCL, ls, (size_t)H.side[slot], nvec, t1vec, t2vec, surfelem);
-    }
+  const int bad = gxh::metrics_from_nodes(N, node_type, H.NGeo, H.nElems, H.nodes.data(), E2S, elem_xgp, Mf, Mg, Mh, sJ,
+                                          nvec, t1vec, t2vec, surfelem);
+  if (bad != 0) {
+    set_error(bad < 0 ? "HOPR mesh: negative Jacobian" : "HOPR mesh: scaled Jacobian below 0.01");
+    return DG_ERR_ARG;
   }
   return DG_OK;
 }

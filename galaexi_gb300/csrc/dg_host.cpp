@@ -228,6 +228,39 @@ int filter_matrix(const dg_config& c, std::vector<double>& F) {
   return 0;
 }
 
+// Modal projection from degree N on the nodes x to degree M < N on the points y: keep the Legendre
+// modes 0..M of the interpolant (the modal branch of GetVandermonde, interpolation.f90:373-374,
+// Vdm_Leg_Out * sVdm_Leg_In(0:M,0:N)).  The modes of the Lagrange basis come from Gauss quadrature
+// with N+1 points, exact for the degree-2N products.
+void modal_projection(int N, const double* x, const double* wb, int M, const double* y, std::vector<double>& V) {
+  Basis1D G;
+  basis_1d(N, DG_NODETYPE_GAUSS, G);
+  std::vector<double> Vlag;
+  vandermonde(N, x, wb, N, G.x.data(), Vlag);  // Vlag(g,i) = l_i(xGauss_g)
+  std::vector<double> sV((size_t)(M + 1) * (N + 1), 0.);
+  for (int m = 0; m <= M; ++m)
+    for (int i = 0; i <= N; ++i) {
+      double acc = 0.;
+      for (int g = 0; g <= N; ++g) {
+        double L, dL;
+        legendre(m, G.x[g], L, dL);
+        acc += L * G.w[g] * Vlag[g + (N + 1) * i];
+      }
+      sV[m + (M + 1) * i] = acc;
+    }
+  V.assign((size_t)(M + 1) * (N + 1), 0.);
+  for (int o = 0; o <= M; ++o)
+    for (int i = 0; i <= N; ++i) {
+      double acc = 0.;
+      for (int m = 0; m <= M; ++m) {
+        double L, dL;
+        legendre(m, y[o], L, dL);
+        acc += L * sV[m + (M + 1) * i];
+      }
+      V[o + (M + 1) * i] = acc;
+    }
+}
+
 // interpolation matrix V(i,j) = l_j(y_i) from nodes x (degree N) to points y (m+1 points)
 void vandermonde(int N, const double* x, const double* wb, int M, const double* y, std::vector<double>& V) {
   V.assign((size_t)(M + 1) * (N + 1), 0.);
@@ -434,91 +467,6 @@ struct Mapping {
 };
 
 
-// Metric terms of one element from its coordinates X (3 per node, i fastest) at the
-// Chebyshev-Gauss-Lobatto points of degree N: conservative curl form (metrics.f90:451-485), then
-// interpolation to the solution nodes (metrics.f90:497-507); sJ = 1/det(dX/dxi) at the solution
-// nodes; JaFace[loc-1][a][b][nn][dd] the metric terms on the six face planes at the solution face
-// nodes (volume face coordinates a, b).
-void curl_metrics(int N, const Basis1D& C, const std::vector<double>& Vcl, const double* X, int e, double* Mf,
-                  double* Mg, double* Mh, double* sJ, double* JaFace) {
-  const int n = N + 1, n2 = n * n;
-  std::vector<double> dX((size_t)9 * n * n2), Rcl((size_t)9 * n * n2), Ja((size_t)9 * n * n2);
-  std::vector<double> JaN((size_t)9 * n * n2), dXN((size_t)9 * n * n2);
-  auto I3 = [&](int i, int j, int k) { return (size_t)i + n * (j + (size_t)n * k); };
-  auto to_nodes = [&](const std::vector<double>& src, std::vector<double>& dst) {
-    std::vector<double> a(src.size()), b(src.size());
-    for (int c = 0; c < 9; ++c)
-      for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
-        double s = 0.; for (int l = 0; l < n; ++l) s += Vcl[i + n * l] * src[c + 9 * I3(l, j, k)]; a[c + 9 * I3(i, j, k)] = s;
-      }
-    for (int c = 0; c < 9; ++c)
-      for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
-        double s = 0.; for (int l = 0; l < n; ++l) s += Vcl[j + n * l] * a[c + 9 * I3(i, l, k)]; b[c + 9 * I3(i, j, k)] = s;
-      }
-    for (int c = 0; c < 9; ++c)
-      for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
-        double s = 0.; for (int l = 0; l < n; ++l) s += Vcl[k + n * l] * b[c + 9 * I3(i, j, l)]; dst[c + 9 * I3(i, j, k)] = s;
-      }
-  };
-  // dX(dd, nn) = d X_nn / d xi_dd
-  for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
-    double* d = &dX[9 * I3(i, j, k)];
-    for (int t = 0; t < 9; ++t) d[t] = 0.;
-    for (int l = 0; l < n; ++l)
-      for (int nn = 0; nn < 3; ++nn) {
-        d[0 * 3 + nn] += C.D[i + n * l] * X[nn + 3 * I3(l, j, k)];
-        d[1 * 3 + nn] += C.D[j + n * l] * X[nn + 3 * I3(i, l, k)];
-        d[2 * 3 + nn] += C.D[k + n * l] * X[nn + 3 * I3(i, j, l)];
-      }
-  }
-  // R(dd, nn) = 1/2 (X_{nn+2} dX_{nn+1}/dxi_dd - X_{nn+1} dX_{nn+2}/dxi_dd)
-  for (size_t t = 0; t < (size_t)n * n2; ++t)
-    for (int dd = 0; dd < 3; ++dd)
-      for (int nn = 0; nn < 3; ++nn) {
-        const int n1 = (nn + 1) % 3, n2_ = (nn + 2) % 3;
-        Rcl[t * 9 + dd * 3 + nn] = 0.5 * (X[n2_ + 3 * t] * dX[t * 9 + dd * 3 + n1] - X[n1 + 3 * t] * dX[t * 9 + dd * 3 + n2_]);
-      }
-  // Ja(dd, nn) = -(d/dxi_{dd+1} R(dd+2, nn) - d/dxi_{dd+2} R(dd+1, nn))
-  for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
-    double* J = &Ja[9 * I3(i, j, k)];
-    for (int t = 0; t < 9; ++t) J[t] = 0.;
-    for (int q = 0; q < n; ++q)
-      for (int nn = 0; nn < 3; ++nn) {
-        J[0 * 3 + nn] += -C.D[j + n * q] * Rcl[9 * I3(i, q, k) + 2 * 3 + nn] + C.D[k + n * q] * Rcl[9 * I3(i, j, q) + 1 * 3 + nn];
-        J[1 * 3 + nn] += -C.D[k + n * q] * Rcl[9 * I3(i, j, q) + 0 * 3 + nn] + C.D[i + n * q] * Rcl[9 * I3(q, j, k) + 2 * 3 + nn];
-        J[2 * 3 + nn] += -C.D[i + n * q] * Rcl[9 * I3(q, j, k) + 1 * 3 + nn] + C.D[j + n * q] * Rcl[9 * I3(i, q, k) + 0 * 3 + nn];
-      }
-  }
-  to_nodes(Ja, JaN);
-  to_nodes(dX, dXN);
-  for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
-    const size_t t = I3(i, j, k), g = vidx(n, i, j, k, e);
-    const double* J = &JaN[9 * t];
-    for (int d = 0; d < 3; ++d) { Mf[d + 3 * g] = J[0 * 3 + d]; Mg[d + 3 * g] = J[1 * 3 + d]; Mh[d + 3 * g] = J[2 * 3 + d]; }
-    const double* a = &dXN[9 * t];
-    const double det = a[0] * (a[4] * a[8] - a[5] * a[7]) - a[1] * (a[3] * a[8] - a[5] * a[6]) +
-                       a[2] * (a[3] * a[7] - a[4] * a[6]);
-    sJ[g] = 1. / det;
-  }
-  // face metrics: JaCL on the face planes (xi = -+1 are CL end points), interpolated in 2D
-  for (int loc = 1; loc <= 6; ++loc)
-    for (int b = 0; b < n; ++b)
-      for (int a = 0; a < n; ++a) {
-        double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-        for (int qb = 0; qb < n; ++qb)
-          for (int qa = 0; qa < n; ++qa) {
-            size_t src;
-            const int pl = (loc == XI_MINUS || loc == ETA_MINUS || loc == ZETA_MINUS) ? 0 : N;
-            if (loc == XI_MINUS || loc == XI_PLUS) src = I3(pl, qa, qb);
-            else if (loc == ETA_MINUS || loc == ETA_PLUS) src = I3(qa, pl, qb);
-            else src = I3(qa, qb, pl);
-            const double wgt = Vcl[a + n * qa] * Vcl[b + n * qb];
-            for (int c = 0; c < 9; ++c) acc[c] += wgt * Ja[9 * src + c];
-          }
-        for (int c = 0; c < 9; ++c) JaFace[((size_t)(loc - 1) * n2 + a + n * b) * 9 + c] = acc[c];
-      }
-}
-
 // SurfMetricsFromJa (metrics.f90:752-789) for a master side (flip 0) of local side loc: the side
 // node (p,q) sits at the volume face coordinates CGNS_SideToVol2(p,q,loc) (mappings.f90:388-425).
 void surface_metrics(int N, int loc, const double* JaFace, size_t side, double* nvec, double* t1vec, double* t2vec,
@@ -549,13 +497,18 @@ void surface_metrics(int N, int loc, const double* JaFace, size_t side, double* 
 }
 }  // namespace gxh
 
-extern "C" int dg_mesh_cartesian(int N, int node_type, int nx, int ny, int nz, const double* x0, const double* x1,
-                                 double deform_amp, double* elem_xgp, double* Mf, double* Mg, double* Mh, double* sJ,
-                                 double* nvec, double* t1vec, double* t2vec, double* surfelem, int* E2S, int* S2E) {
+extern "C" int dg_mesh_cartesian(int N, int node_type, int NGeo, int nx, int ny, int nz, const double* x0,
+                                 const double* x1, double deform_amp, double* node_coords, double* elem_xgp, double* Mf,
+                                 double* Mg, double* Mh, double* sJ, double* nvec, double* t1vec, double* t2vec,
+                                 double* surfelem, int* E2S, int* S2E) {
   int nElems, nSides;
   if (dg_mesh_cartesian_sizes(nx, ny, nz, &nElems, &nSides) != DG_OK) return DG_ERR_ARG;
   if (N < 1 || N > DG_MAX_N) { set_error("mesh: N out of range"); return DG_ERR_ARG; }
-  const int n = N + 1, n2 = n * n;
+  if (NGeo < 1 || NGeo > DG_MAX_N) { set_error("mesh: NGeo out of range"); return DG_ERR_ARG; }
+  if (!Mf || !Mg || !Mh || !sJ || !nvec || !t1vec || !t2vec || !surfelem || !E2S || !S2E) {
+    set_error("dg_mesh_cartesian: null argument"); return DG_ERR_ARG;
+  }
+  const int n = N + 1, n2 = n * n, g = NGeo + 1;
   Basis1D B;
   basis_1d(N, node_type, B);
   Mapping map;
@@ -592,61 +545,58 @@ extern "C" int dg_mesh_cartesian(int N, int node_type, int nx, int ny, int nz, c
           p[0] = e + 1; p[1] = nb[d] + 1; p[2] = mloc[d]; p[3] = sloc[d]; p[4] = flips[d];
         }
       }
-  // node coordinates
+  // element node coordinates on NGeo+1 equidistant points per direction, as a HOPR file holds them;
+  // the displacement moves these nodes (as the reference's meshdeform does, mesh.f90:224-234)
+  std::vector<double> nodes((size_t)3 * g * g * g * nElems);
   for (int e = 0; e < nElems; ++e) {
     int e3[3] = {e % nx, (e / nx) % ny, e / (nx * ny)};
-    for (int k = 0; k <= N; ++k)
-      for (int j = 0; j <= N; ++j)
-        for (int i = 0; i <= N; ++i) {
-          const double xi[3] = {B.x[i], B.x[j], B.x[k]};
-          double X[3];
-          map(e3, xi, X);
-          if (elem_xgp)
-            for (int d = 0; d < 3; ++d) elem_xgp[d + 3 * vidx(n, i, j, k, e)] = X[d];
+    for (int k = 0; k < g; ++k)
+      for (int j = 0; j < g; ++j)
+        for (int i = 0; i < g; ++i) {
+          const double xi[3] = {2. * (double)i / (double)NGeo - 1., 2. * (double)j / (double)NGeo - 1.,
+                                2. * (double)k / (double)NGeo - 1.};
+          map(e3, xi, &nodes[3 * vidx(g, i, j, k, e)]);
         }
   }
-  // volume metrics Ja^1 = Mf, Ja^2 = Mg, Ja^3 = Mh (Ja(nn,dd) = J a^nn_dd) and sJ
-  // face metrics (nn,dd) at every face node, indexed [e][loc][a][b] in volume face coordinates
-  std::vector<double> JaFace((size_t)nElems * 6 * n2 * 9, 0.);
-  if (deform_amp == 0.) {
-    const double h[3] = {map.L[0] / nx, map.L[1] / ny, map.L[2] / nz};
-    const double Ja[3] = {0.25 * h[1] * h[2], 0.25 * h[0] * h[2], 0.25 * h[0] * h[1]};
-    const double s = 8. / (h[0] * h[1] * h[2]);
-    for (size_t t = 0; t < (size_t)nElems * n * n2; ++t) {
-      for (int d = 0; d < 3; ++d) {
-        Mf[d + 3 * t] = d == 0 ? Ja[0] : 0.;
-        Mg[d + 3 * t] = d == 1 ? Ja[1] : 0.;
-        Mh[d + 3 * t] = d == 2 ? Ja[2] : 0.;
-      }
-      sJ[t] = s;
-    }
-    for (size_t t = 0; t < (size_t)nElems * 6 * n2; ++t)
-      for (int nn = 0; nn < 3; ++nn)
-        for (int dd = 0; dd < 3; ++dd) JaFace[t * 9 + nn * 3 + dd] = (nn == dd) ? Ja[nn] : 0.;
-  } else {
-    // Curved: conservative curl form of the metric terms on Chebyshev-Gauss-Lobatto points of
-    // degree N (metrics.f90:451-485), then interpolation to the solution nodes (metrics.f90:497-507).
-    Basis1D C;
-    basis_1d(N, 99, C);  // Chebyshev-Gauss-Lobatto
-    std::vector<double> Vcl;  // CL -> solution nodes
-    vandermonde(N, C.x.data(), C.wb.data(), N, B.x.data(), Vcl);
-    std::vector<double> X((size_t)3 * n * n2);
-    auto I3 = [&](int i, int j, int k) { return (size_t)i + n * (j + (size_t)n * k); };
+  if (node_coords) std::memcpy(node_coords, nodes.data(), nodes.size() * sizeof(double));
+  if (deform_amp != 0.) {
+    // curved: BuildCoords + CalcMetrics + CalcSurfMetrics of the reference on the node coordinates
+    const int bad = metrics_from_nodes(N, node_type, NGeo, nElems, nodes.data(), E2S, elem_xgp, Mf, Mg, Mh, sJ, nvec,
+                                       t1vec, t2vec, surfelem);
+    if (bad != 0) { set_error("mesh: the displacement folds elements (bad Jacobian)"); return DG_ERR_ARG; }
+    return DG_OK;
+  }
+  // affine: the exact mapping at the solution nodes and constant metric terms
+  if (elem_xgp)
     for (int e = 0; e < nElems; ++e) {
       int e3[3] = {e % nx, (e / nx) % ny, e / (nx * ny)};
-      for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
-        const double xi[3] = {C.x[i], C.x[j], C.x[k]};
-        map(e3, xi, &X[3 * I3(i, j, k)]);
-      }
-      curl_metrics(N, C, Vcl, X.data(), e, Mf, Mg, Mh, sJ, &JaFace[(size_t)e * 6 * n2 * 9]);
+      for (int k = 0; k <= N; ++k)
+        for (int j = 0; j <= N; ++j)
+          for (int i = 0; i <= N; ++i) {
+            const double xi[3] = {B.x[i], B.x[j], B.x[k]};
+            map(e3, xi, &elem_xgp[3 * vidx(n, i, j, k, e)]);
+          }
     }
+  const double h[3] = {map.L[0] / nx, map.L[1] / ny, map.L[2] / nz};
+  const double Ja[3] = {0.25 * h[1] * h[2], 0.25 * h[0] * h[2], 0.25 * h[0] * h[1]};
+  const double s = 8. / (h[0] * h[1] * h[2]);
+  for (size_t t = 0; t < (size_t)nElems * n * n2; ++t) {
+    for (int d = 0; d < 3; ++d) {
+      Mf[d + 3 * t] = d == 0 ? Ja[0] : 0.;
+      Mg[d + 3 * t] = d == 1 ? Ja[1] : 0.;
+      Mh[d + 3 * t] = d == 2 ? Ja[2] : 0.;
+    }
+    sJ[t] = s;
   }
   // SurfMetricsFromJa (metrics.f90:752-789) on the master sides (every element is master of its
-  // three plus sides)
+  // three plus sides) from the constant face metric terms
+  std::vector<double> JaFace((size_t)6 * n2 * 9, 0.);
+  for (size_t t = 0; t < (size_t)6 * n2; ++t)
+    for (int nn = 0; nn < 3; ++nn)
+      for (int dd = 0; dd < 3; ++dd) JaFace[t * 9 + nn * 3 + dd] = (nn == dd) ? Ja[nn] : 0.;
   for (int e = 0; e < nElems; ++e) {
     const int locs[3] = {XI_PLUS, ETA_PLUS, ZETA_PLUS};
-    for (int d = 0; d < 3; ++d)
-      surface_metrics(N, locs[d], &JaFace[(size_t)e * 6 * n2 * 9], (size_t)(3 * e + d), nvec, t1vec, t2vec, surfelem);
+    for (int d = 0; d < 3; ++d) surface_metrics(N, locs[d], JaFace.data(), (size_t)(3 * e + d), nvec, t1vec, t2vec, surfelem);
   }
   return DG_OK;
 }

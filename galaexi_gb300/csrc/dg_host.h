@@ -28,9 +28,16 @@ void set_error(const std::string& s);
 // the M+1 points y, column-major (0:M, 0:N)
 void vandermonde(int N, const double* x, const double* wb, int M, const double* y, std::vector<double>& V);
 inline size_t vidx(int n, int i, int j, int k, int e) { return (size_t)i + n * (j + n * (k + (size_t)n * e)); }
-// element metric terms from coordinates at the CGL points of degree N (dg_host.cpp)
-void curl_metrics(int N, const Basis1D& C, const std::vector<double>& Vcl, const double* X, int e, double* Mf,
-                  double* Mg, double* Mh, double* sJ, double* JaFace);
+// modal projection (Legendre modes 0..M) from degree N on the nodes x to degree M < N on the points y,
+// column-major (0:M, 0:N)
+void modal_projection(int N, const double* x, const double* wb, int M, const double* y, std::vector<double>& V);
+// BuildCoords + CalcMetrics + CalcSurfMetrics (dg_hopr.cpp) from the equidistant element node coordinates
+// nodes (3,0:NGeo,0:NGeo,0:NGeo,nElems) and ElemToSide (3,6,nElems, 1-based side IDs); the master
+// sides (flip 0) receive the side vectors.  elem_xgp may be null.  Returns the count of solution nodes
+// with a scaled Jacobian below 0.01, or -1 for a non-positive Jacobian.
+int metrics_from_nodes(int N, int node_type, int NGeo, int nElems, const double* nodes, const int* E2S,
+                       double* elem_xgp, double* Mf, double* Mg, double* Mh, double* sJ, double* nvec,
+                       double* t1vec, double* t2vec, double* surfelem);
 // normal, tangents and surface element of a master side from the element's face metric terms
 void surface_metrics(int N, int loc, const double* JaFace, size_t side, double* nvec, double* t1vec, double* t2vec,
                      double* surfelem);

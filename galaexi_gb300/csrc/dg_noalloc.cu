@@ -7,7 +7,6 @@
 #include <cuda_runtime.h>
 #include <cmath>
 #include <cstring>
-#include <mutex>
 #include <string>
 
 #include "../../include/galaexi_gb300.h"
@@ -20,26 +19,17 @@ namespace {
 constexpr int kTail = 32;  // doubles after the per-element pairs: [0] dt_conv, [1] dt_visc, [2] bad counter
 static __device__ __align__(256) double g_noalloc_scratch[2 * (size_t)DG_NOALLOC_MAX_ELEMS + kTail];
 
-// device address of g_noalloc_scratch per device (the host-side name is not a device address)
-std::mutex g_mu;
-void* g_scratch_dev[256] = {nullptr};
-
+// Device address of g_noalloc_scratch in the current device's context.  The host-side name of the
+// array is not a device address; the address is looked up on every call (a host-side table lookup),
+// so that a context torn down and created again (cudaDeviceReset) never leaves a stale address.
 int scratch_ptr(double** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) { set_error(std::string("cudaGetDevice: ") + cudaGetErrorString(e)); return DG_ERR_CUDA; }
-  if (dev < 0 || dev >= 256) { set_error("device index out of range"); return DG_ERR_CUDA; }
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch_dev[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-      set_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-      return DG_ERR_CUDA;
-    }
-    g_scratch_dev[dev] = p;
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p) {
+    set_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    return DG_ERR_CUDA;
   }
-  *out = static_cast<double*>(g_scratch_dev[dev]);
+  *out = static_cast<double*>(p);
   return DG_OK;
 }
 

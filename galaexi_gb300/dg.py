@@ -115,7 +115,9 @@ class Mesh:
       ElemToSide (nElems,6,3)   SideToElem (nSides,5)   (1-based IDs)
     """
 
-    def __init__(self, N, node_type, nx, ny, nz, x0=(0.0, 0.0, 0.0), x1=(1.0, 1.0, 1.0), deform=0.0):
+    def __init__(self, N, node_type, nx, ny, nz, x0=(0.0, 0.0, 0.0), x1=(1.0, 1.0, 1.0), deform=0.0, NGeo=None):
+        """NGeo: degree of the element mapping (node coordinates on NGeo+1 equidistant points per
+        direction, displaced by `deform`); default 1 for the affine box, 2 for a displaced one."""
         L = nat.lib()
         ne, ns = ctypes.c_int(), ctypes.c_int()
         nat.check(L.dg_mesh_cartesian_sizes(nx, ny, nz, ctypes.byref(ne), ctypes.byref(ns)), "mesh sizes")
@@ -123,12 +125,16 @@ class Mesh:
         self.nElems, self.nSides = ne.value, ns.value
         self.nx, self.ny, self.nz = nx, ny, nz
         self.x0, self.x1, self.deform = tuple(x0), tuple(x1), deform
-        self.nBCSides, self.NGeo = 0, None
+        self.NGeo = int(NGeo) if NGeo is not None else (2 if deform != 0.0 else 1)
+        self.nBCSides = 0
         self._alloc()
+        g = self.NGeo + 1
+        self.NodeCoords = np.zeros((self.nElems, g, g, g, 3))
         a0 = np.asarray(x0, dtype=np.float64)
         a1 = np.asarray(x1, dtype=np.float64)
-        nat.check(L.dg_mesh_cartesian(N, node_type, nx, ny, nz, _ptr(a0), _ptr(a1), float(deform),
-                                      _ptr(self.Elem_xGP), _ptr(self.Metrics_fTilde), _ptr(self.Metrics_gTilde),
+        nat.check(L.dg_mesh_cartesian(N, node_type, self.NGeo, nx, ny, nz, _ptr(a0), _ptr(a1), float(deform),
+                                      _ptr(self.NodeCoords), _ptr(self.Elem_xGP), _ptr(self.Metrics_fTilde),
+                                      _ptr(self.Metrics_gTilde),
                                       _ptr(self.Metrics_hTilde), _ptr(self.sJ), _ptr(self.NormVec),
                                       _ptr(self.TangVec1), _ptr(self.TangVec2), _ptr(self.SurfElem),
                                       _ptr(self.ElemToSide), _ptr(self.SideToElem)), "dg_mesh_cartesian")
@@ -153,6 +159,9 @@ class Mesh:
                                  _ptr(self.TangVec1), _ptr(self.TangVec2), _ptr(self.SurfElem), _ptr(self.ElemToSide),
                                  _ptr(self.SideToElem), _ptr(self.BCIndex)), "dg_mesh_hopr")
         self.BCIndex = self.BCIndex[:self.nBCSides]
+        g = self.NGeo + 1
+        # the file's equidistant element node coordinates NodeCoords(3,0:NGeo,0:NGeo,0:NGeo,nElems)
+        self.NodeCoords = read_h5(path, "NodeCoords").reshape(self.nElems, g, g, g, 3)
         nbc = ctypes.c_int()
         nat.check(L.dg_mesh_hopr_bcs(p, ctypes.byref(nbc), None, 0, None), "dg_mesh_hopr_bcs")
         NL = 256

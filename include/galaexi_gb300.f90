@@ -345,14 +345,15 @@ INTERFACE
     INTEGER(C_INT), INTENT(OUT) :: nElems, nSides
   END FUNCTION dg_mesh_cartesian_sizes
 
-  ! a periodic box [x0,x1] of nx*ny*nz elements, optionally displaced (deform_amp), in the dg_set_mesh layouts
-  INTEGER(C_INT) FUNCTION dg_mesh_cartesian(N, node_type, nx, ny, nz, x0, x1, deform_amp, xgp, Mf, Mg, Mh, sJ, &
-                                            nv, t1, t2, se, E2S, S2E) BIND(C,NAME='dg_mesh_cartesian')
+  ! a periodic box [x0,x1] of nx*ny*nz elements of mapping degree NGeo, optionally displaced (deform_amp), in the
+  ! dg_set_mesh layouts plus NodeCoords(3,0:NGeo,0:NGeo,0:NGeo,nElems) and Elem_xGP
+  INTEGER(C_INT) FUNCTION dg_mesh_cartesian(N, node_type, NGeo, nx, ny, nz, x0, x1, deform_amp, nodes, xgp, Mf, Mg, &
+                                            Mh, sJ, nv, t1, t2, se, E2S, S2E) BIND(C,NAME='dg_mesh_cartesian')
     IMPORT :: C_INT, C_DOUBLE
-    INTEGER(C_INT), VALUE :: N, node_type, nx, ny, nz
+    INTEGER(C_INT), VALUE :: N, node_type, NGeo, nx, ny, nz
     REAL(C_DOUBLE), INTENT(IN) :: x0(3), x1(3)
     REAL(C_DOUBLE), VALUE :: deform_amp
-    REAL(C_DOUBLE), INTENT(OUT) :: xgp(*), Mf(*), Mg(*), Mh(*), sJ(*), nv(*), t1(*), t2(*), se(*)
+    REAL(C_DOUBLE), INTENT(OUT) :: nodes(*), xgp(*), Mf(*), Mg(*), Mh(*), sJ(*), nv(*), t1(*), t2(*), se(*)
     INTEGER(C_INT), INTENT(OUT) :: E2S(*), S2E(*)
   END FUNCTION dg_mesh_cartesian
 

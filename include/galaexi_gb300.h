@@ -191,12 +191,13 @@ int dg_calc_timestep(dg_ctx* ctx, const double* d_U, double cfl_scale, double df
  * scratch comes from a static device array of the library (DG_NOALLOC_MAX_ELEMS eigenvalue pairs,
  * 8 MiB, held on every GPU that loads the library until the process exits).
  *   - nElems above DG_NOALLOC_MAX_ELEMS is rejected with DG_ERR_ARG.
- *   - The first call on a device looks up the device address of the static array for that device
- *     (cudaGetSymbolAddress); make that first call before any stream capture on that device.
+ *   - Each call looks up the device address of the static array in the current device's context
+ *     (cudaGetSymbolAddress): call it with the device that holds the arrays current.
  *   - Every call uses the same static array; the previous call's contents stay in it (the error
  *     counter is cleared at the start of each call).  Calls whose work overlaps on the GPU (other
  *     streams, other host threads) race on that array: serialise them.
- * Synchronises the stream; returns DG_ERR_NAN for NaN/Inf or non-positive density/pressure. */
+ * Copies dt to the host and synchronises the stream; returns DG_ERR_NAN for NaN/Inf or non-positive
+ * density/pressure. */
 #define DG_NOALLOC_MAX_ELEMS (1 << 19)
 int dg_calc_timestep_noalloc(int N, int node_type, int nElems, int parabolic, double kappa, double mu0, double Pr,
                              const double* d_U, const double* d_metrics_f, const double* d_metrics_g,
@@ -325,17 +326,22 @@ int dg_basis(int N, int node_type, double* xGP, double* wGP, double* wBary,
 /* Sizes of a periodic Cartesian box of nx*ny*nz hexahedra. */
 int dg_mesh_cartesian_sizes(int nx, int ny, int nz, int* nElems, int* nSides);
 
-/* Build a periodic box [x0,x1]^3 with nx*ny*nz elements, optionally displaced
- * by x_i += deform_amp * sin(2 pi xh) sin(2 pi yh) sin(2 pi zh) with
- * (xh,yh,zh) the coordinates normalised to [0,1] (deform_amp = 0: affine).
- * Outputs in the layouts of dg_set_mesh plus the node coordinates
- * Elem_xGP(3,0:N,0:N,0:N,nElems).  Metrics use the conservative curl form
- * (metrics.f90:171-560) on the solution nodes; face vectors follow
- * SurfMetricsFromJa (metrics.f90:752-789).  Every element is master of its
- * XI_PLUS, ETA_PLUS and ZETA_PLUS sides. */
-int dg_mesh_cartesian(int N, int node_type, int nx, int ny, int nz,
+/* Build a periodic box [x0,x1]^3 with nx*ny*nz elements.  Each element's mapping is
+ * given, as in a HOPR mesh file, by node coordinates on NGeo+1 equidistant points per
+ * direction, optionally displaced by x_i += deform_amp * sin(2 pi xh) sin(2 pi yh)
+ * sin(2 pi zh) with (xh,yh,zh) the coordinates normalised to [0,1] (the node
+ * displacement of the reference's meshdeform, mesh.f90:224-234).  deform_amp = 0:
+ * affine box, with the exact (constant) metric terms and the exact node positions
+ * Elem_xGP; otherwise BuildCoords + CalcMetrics + CalcSurfMetrics of the reference
+ * (metrics.f90:85-750: curl form on the Chebyshev-Gauss-Lobatto points, the
+ * Jacobian on 3 NGeo nodes projected to N) on the node coordinates.  Outputs in the
+ * layouts of dg_set_mesh plus NodeCoords(3,0:NGeo,0:NGeo,0:NGeo,nElems) and
+ * Elem_xGP(3,0:N,0:N,0:N,nElems) (either may be NULL).  Every element is master of
+ * its XI_PLUS, ETA_PLUS and ZETA_PLUS sides.  A displacement that folds an element
+ * (scaled Jacobian below 0.01, the reference's abort criterion) is DG_ERR_ARG. */
+int dg_mesh_cartesian(int N, int node_type, int NGeo, int nx, int ny, int nz,
                       const double* x0, const double* x1, double deform_amp,
-                      double* elem_xgp,
+                      double* node_coords, double* elem_xgp,
                       double* metrics_f, double* metrics_g, double* metrics_h, double* sJ,
                       double* normvec, double* tangvec1, double* tangvec2, double* surfelem,
                       int* elem_to_side, int* side_to_elem);

@@ -1576,6 +1576,254 @@ static void ChangeBasis3D_XYZ(int nVar, int NIn, int NOut, const double* Vx, con
             X_Out[v + nVar * (iO + no * (jO + (size_t)no * kO))] + Vz[kO + no * kI] * B2[v + nVar * (iO + no * (jO + (size_t)no * kI))];
 }
 
+// ---------------------------------------------------------------------------------------
+// Geometry: src/mesh/metrics.f90 (BuildCoords, CalcMetrics, CalcSurfMetrics, SurfMetricsFromJa)
+// for the default path of the reference: no octree (interpolateFromTree = F), curl-form metrics
+// (crossProductMetrics = F, mesh.f90:65-67), 3D, no mortars.  Arrays in Fortran layout:
+// NodeCoords(3,0:NGeo,0:NGeo,0:NGeo,nElems), XCL(3,0:N,0:N,0:N), dXCL(3,3,...) = (dd,nn),
+// JaCL(3,3,...) = (dd,nn).
+// ---------------------------------------------------------------------------------------
+// ChangeBasis2D  changeBasis.t90:101-143 (Dim1 variables per node)
+static void ChangeBasis2D(int Dim1, int NIn, int NOut, const double* Vdm, const double* X_In, double* X_Out) {
+  const int ni = NIn + 1, no = NOut + 1;
+  std::vector<double> B1((size_t)Dim1 * no * ni, 0.);
+  for (int jI = 0; jI < ni; ++jI) for (int iI = 0; iI < ni; ++iI)
+    for (int iO = 0; iO < no; ++iO)
+      for (int v = 0; v < Dim1; ++v)
+        B1[v + Dim1 * (iO + no * jI)] = B1[v + Dim1 * (iO + no * jI)] + Vdm[iO + no * iI] * X_In[v + Dim1 * (iI + ni * jI)];
+  for (size_t t = 0; t < (size_t)Dim1 * no * no; ++t) X_Out[t] = 0.;
+  for (int jI = 0; jI < ni; ++jI) for (int jO = 0; jO < no; ++jO)
+    for (int iO = 0; iO < no; ++iO)
+      for (int v = 0; v < Dim1; ++v)
+        X_Out[v + Dim1 * (iO + no * jO)] = X_Out[v + Dim1 * (iO + no * jO)] + Vdm[jO + no * jI] * B1[v + Dim1 * (iO + no * jI)];
+}
+// ChangeBasisVolume = ChangeBasis3D (changeBasis.t90:237-283): one Vandermonde in all three directions
+static void ChangeBasis3D(int Dim1, int NIn, int NOut, const double* Vdm, const double* X_In, double* X_Out) {
+  ChangeBasis3D_XYZ(Dim1, NIn, NOut, Vdm, Vdm, Vdm, X_In, X_Out);
+}
+// GetDerivativeMatrix  interpolation.f90:401-416
+static void GetDerivativeMatrix(int N_in, int node_type, double* D) {
+  std::vector<double> x(N_in + 1);
+  GetNodesAndWeights(N_in, node_type, x.data(), nullptr, nullptr);
+  PolynomialDerivativeMatrix(N_in, x.data(), D);
+}
+
+static const int kNormalDirs[7] = {0, 3, 2, 1, 2, 1, 3};           // mesh_vars.f90:111 (1-based local side)
+static const int kTangDirs[7] = {0, 1, 3, 2, 3, 2, 1};             // mesh_vars.f90:113
+static const double kNormalSigns[7] = {0., -1., -1., 1., 1., -1., 1.};  // mesh_vars.f90:118
+
+// SurfMetricsFromJa  metrics.f90:752-789 for one side: Ja_Face(3,3,0:N,0:N) -> NormVec, TangVec1,
+// TangVec2 (3,0:N,0:N), SurfElem (0:N,0:N)
+static void SurfMetricsFromJa(int Nloc, int NormalDir, int TangDir, double NormalSign, const double* Ja_Face,
+                              double* NormVec, double* TangVec1, double* TangVec2, double* SurfElem) {
+  const int n = Nloc + 1;
+  auto J = [&](int dd, int nn, int p, int q) { return Ja_Face[(dd - 1) + 3 * ((nn - 1) + 3 * (p + n * q))]; };
+  for (int q = 0; q <= Nloc; ++q)
+    for (int p = 0; p <= Nloc; ++p) {
+      const size_t f = (size_t)p + n * q;
+      double s = 0.;
+      for (int c = 1; c <= 3; ++c) s = s + sq(J(NormalDir, c, p, q));
+      SurfElem[f] = std::sqrt(s);
+      double* nv = NormVec + 3 * f;
+      for (int c = 1; c <= 3; ++c) nv[c - 1] = NormalSign * J(NormalDir, c, p, q) / SurfElem[f];
+      double dot = 0.;
+      for (int c = 1; c <= 3; ++c) dot = dot + J(TangDir, c, p, q) * nv[c - 1];
+      double* t1 = TangVec1 + 3 * f;
+      for (int c = 1; c <= 3; ++c) t1[c - 1] = J(TangDir, c, p, q) - dot * nv[c - 1];
+      double tn = 0.;
+      for (int c = 0; c < 3; ++c) tn = tn + sq(t1[c]);
+      tn = std::sqrt(tn);
+      for (int c = 0; c < 3; ++c) t1[c] = t1[c] / tn;
+      double* t2 = TangVec2 + 3 * f;  // CROSS (mathtools.f90:153-165)
+      t2[0] = nv[1] * t1[2] - nv[2] * t1[1];
+      t2[1] = nv[2] * t1[0] - nv[0] * t1[2];
+      t2[2] = nv[0] * t1[1] - nv[1] * t1[0];
+    }
+}
+
+// Volume node of the face-plane position (a,b) of local side iLocSide (the planes of metrics.f90:663-676)
+static size_t face_plane_node(int Nloc, int iLocSide, int a, int b) {
+  const int n = Nloc + 1;
+  int i, j, k;
+  switch (iLocSide) {
+    case XI_MINUS: i = 0; j = a; k = b; break;
+    case XI_PLUS: i = Nloc; j = a; k = b; break;
+    case ETA_MINUS: i = a; j = 0; k = b; break;
+    case ETA_PLUS: i = a; j = Nloc; k = b; break;
+    case ZETA_MINUS: i = a; j = b; k = 0; break;
+    default: i = a; j = b; k = Nloc; break;
+  }
+  return (size_t)i + n * (j + (size_t)n * k);
+}
+
+struct MetricsOut {
+  double *Elem_xGP, *Mf, *Mg, *Mh, *sJ, *NormVec, *TangVec1, *TangVec2, *SurfElem, *Face_xGP;
+};
+
+// BuildCoords (metrics.f90:85-160) + CalcMetrics (:171-560) + CalcSurfMetrics (:596-750); returns the
+// number of solution nodes with a scaled Jacobian below 0.01 (the reference aborts on those,
+// metrics.f90:345-352) or -1 for a negative one
+static int CalcMetrics(int N, int NodeType, int NGeo, int nElems, const double* NodeCoords, const int* ElemToSide,
+                       const MetricsOut& o) {
+  const int NGeoRef = 3 * NGeo;  // mesh.f90:370
+  const int n = N + 1, g = NGeo + 1, r = NGeoRef + 1, n3 = n * n * n, g3 = g * g * g, r3 = r * r * r;
+  const int CL = 3, VISU = 4;
+  // 1.a-1.f, 2., 2.d: Vandermonde and derivative matrices (column-major (0:N_out,0:N_in))
+  std::vector<double> Vdm_EQNGeo_CLNGeo(g * g), Vdm_CLNGeo_CLN(n * g), DCL_NGeo(g * g), Vdm_CLNGeo_NGeoRef(r * g),
+      Vdm_NGeoRef_N(n * r), DCL_N(n * n), Vdm_CLN_N(n * n);
+  GetVandermonde(NGeo, VISU, NGeo, CL, Vdm_EQNGeo_CLNGeo.data(), nullptr, false);
+  GetVandermonde(NGeo, CL, N, CL, Vdm_CLNGeo_CLN.data(), nullptr, false);
+  GetDerivativeMatrix(NGeo, CL, DCL_NGeo.data());
+  GetVandermonde(NGeo, CL, NGeoRef, NodeType, Vdm_CLNGeo_NGeoRef.data(), nullptr, false);
+  GetVandermonde(NGeoRef, NodeType, N, NodeType, Vdm_NGeoRef_N.data(), nullptr, true);
+  GetDerivativeMatrix(N, CL, DCL_N.data());
+  GetVandermonde(N, CL, N, NodeType, Vdm_CLN_N.data(), nullptr, false);
+  // BuildCoords: Vdm_EQNGeo_CLNloc = MATMUL(Vdm_CLNloc_Nloc, Vdm_EQNGeo_CLNloc)
+  std::vector<double> Vdm_EQNGeo_CLNloc(n * g), Vdm_BC(n * g), Vdm_CLNloc_Nloc(n * n);
+  GetVandermonde(NGeo, VISU, N, CL, Vdm_EQNGeo_CLNloc.data(), nullptr, false);
+  GetVandermonde(N, CL, N, NodeType, Vdm_CLNloc_Nloc.data(), nullptr, false);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < g; ++j) {
+      double acc = 0.;
+      for (int k = 0; k < n; ++k) acc = acc + Vdm_CLNloc_Nloc[i + n * k] * Vdm_EQNGeo_CLNloc[k + n * j];
+      Vdm_BC[i + n * j] = acc;
+    }
+  int bad = 0;
+  std::vector<double> XCL_NGeo(3 * g3), XCL_N(3 * n3), dXCL_NGeo(9 * g3), dX_NGeoRef(9 * r3), detJac_Ref(r3),
+      DetJac_N(n3), dXCL_N(9 * n3), R_CL_N(9 * n3), JaCL_N(9 * n3), slice_g(3 * g3), slice_r(3 * r3), slice_n(3 * n3);
+  std::vector<double> tmp(3 * n * n), tmp2(3 * n * n), Ja_Face_l(9 * n * n);
+  auto G = [&](int i, int j, int k) { return (size_t)i + g * (j + (size_t)g * k); };
+  auto NI = [&](int i, int j, int k) { return (size_t)i + n * (j + (size_t)n * k); };
+  for (int iElem = 0; iElem < nElems; ++iElem) {
+    const double* NC = NodeCoords + (size_t)3 * g3 * iElem;
+    if (o.Elem_xGP) ChangeBasis3D(3, NGeo, N, Vdm_BC.data(), NC, o.Elem_xGP + (size_t)3 * n3 * iElem);
+    // 1.a, 1.b
+    ChangeBasis3D(3, NGeo, NGeo, Vdm_EQNGeo_CLNGeo.data(), NC, XCL_NGeo.data());
+    ChangeBasis3D(3, NGeo, N, Vdm_CLNGeo_CLN.data(), XCL_NGeo.data(), XCL_N.data());
+    // 1.c dXCL_NGeo(dd,nn,i,j,k)
+    std::fill(dXCL_NGeo.begin(), dXCL_NGeo.end(), 0.);
+    for (int k = 0; k < g; ++k) for (int j = 0; j < g; ++j) for (int i = 0; i < g; ++i) {
+      double* d = &dXCL_NGeo[9 * G(i, j, k)];
+      for (int ll = 0; ll < g; ++ll)
+        for (int nn = 0; nn < 3; ++nn) {
+          d[0 + 3 * nn] = d[0 + 3 * nn] + DCL_NGeo[i + g * ll] * XCL_NGeo[nn + 3 * G(ll, j, k)];
+          d[1 + 3 * nn] = d[1 + 3 * nn] + DCL_NGeo[j + g * ll] * XCL_NGeo[nn + 3 * G(i, ll, k)];
+          d[2 + 3 * nn] = d[2 + 3 * nn] + DCL_NGeo[k + g * ll] * XCL_NGeo[nn + 3 * G(i, j, ll)];
+        }
+    }
+    // 1.d dX_NGeoRef(:,nn,...) = ChangeBasisVolume of dXCL_NGeo(:,nn,...)
+    for (int nn = 0; nn < 3; ++nn) {
+      for (int t = 0; t < g3; ++t)
+        for (int dd = 0; dd < 3; ++dd) slice_g[dd + 3 * t] = dXCL_NGeo[dd + 3 * nn + 9 * t];
+      ChangeBasis3D(3, NGeo, NGeoRef, Vdm_CLNGeo_NGeoRef.data(), slice_g.data(), slice_r.data());
+      for (int t = 0; t < r3; ++t)
+        for (int dd = 0; dd < 3; ++dd) dX_NGeoRef[dd + 3 * nn + 9 * t] = slice_r[dd + 3 * t];
+    }
+    // 1.e detJac_Ref (left to right, from the initial 0)
+    for (int t = 0; t < r3; ++t) {
+      auto X = [&](int a, int b) { return dX_NGeoRef[(a - 1) + 3 * (b - 1) + 9 * t]; };
+      detJac_Ref[t] = 0. + X(1, 1) * (X(2, 2) * X(3, 3) - X(3, 2) * X(2, 3)) +
+                      X(2, 1) * (X(3, 2) * X(1, 3) - X(1, 2) * X(3, 3)) + X(3, 1) * (X(1, 2) * X(2, 3) - X(2, 2) * X(1, 3));
+    }
+    // 1.f modal projection NGeoRef -> N, sJ, scaled-Jacobian check
+    ChangeBasis3D(1, NGeoRef, N, Vdm_NGeoRef_N.data(), detJac_Ref.data(), DetJac_N.data());
+    double mx = DetJac_N[0];
+    for (int t = 1; t < n3; ++t) mx = std::max(mx, DetJac_N[t]);
+    for (int t = 0; t < n3; ++t) {
+      o.sJ[(size_t)n3 * iElem + t] = 1. / DetJac_N[t];
+      if (DetJac_N[t] <= 0.) bad = -1;
+      else if (bad >= 0 && DetJac_N[t] / mx < 0.01) bad++;
+    }
+    // 2.a dXCL_N
+    std::fill(dXCL_N.begin(), dXCL_N.end(), 0.);
+    if (N >= NGeo) {
+      for (int nn = 0; nn < 3; ++nn) {
+        for (int t = 0; t < g3; ++t)
+          for (int dd = 0; dd < 3; ++dd) slice_g[dd + 3 * t] = dXCL_NGeo[dd + 3 * nn + 9 * t];
+        ChangeBasis3D(3, NGeo, N, Vdm_CLNGeo_CLN.data(), slice_g.data(), slice_n.data());
+        for (int t = 0; t < n3; ++t)
+          for (int dd = 0; dd < 3; ++dd) dXCL_N[dd + 3 * nn + 9 * t] = slice_n[dd + 3 * t];
+      }
+    } else {
+      for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
+        double* d = &dXCL_N[9 * NI(i, j, k)];
+        for (int ll = 0; ll < n; ++ll)
+          for (int nn = 0; nn < 3; ++nn) {
+            d[0 + 3 * nn] = d[0 + 3 * nn] + DCL_N[i + n * ll] * XCL_N[nn + 3 * NI(ll, j, k)];
+            d[1 + 3 * nn] = d[1 + 3 * nn] + DCL_N[j + n * ll] * XCL_N[nn + 3 * NI(i, ll, k)];
+            d[2 + 3 * nn] = d[2 + 3 * nn] + DCL_N[k + n * ll] * XCL_N[nn + 3 * NI(i, j, ll)];
+          }
+      }
+    }
+    // 2.b curl form: R_CL_N(dd,nn) = 1/2 (XCL_N x d/dxi_dd XCL_N)_nn, JaCL_N = -(curl R)
+    for (int t = 0; t < n3; ++t) {
+      const double* x = &XCL_N[3 * t];
+      const double* d = &dXCL_N[9 * t];
+      double* R = &R_CL_N[9 * t];
+      for (int dd = 0; dd < 3; ++dd) {
+        R[dd + 3 * 0] = 0.5 * (x[2] * d[dd + 3 * 1] - x[1] * d[dd + 3 * 2]);
+        R[dd + 3 * 1] = 0.5 * (x[0] * d[dd + 3 * 2] - x[2] * d[dd + 3 * 0]);
+        R[dd + 3 * 2] = 0.5 * (x[1] * d[dd + 3 * 0] - x[0] * d[dd + 3 * 1]);
+      }
+    }
+    std::fill(JaCL_N.begin(), JaCL_N.end(), 0.);
+    for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
+      double* Ja = &JaCL_N[9 * NI(i, j, k)];
+      for (int q = 0; q < n; ++q)
+        for (int nn = 0; nn < 3; ++nn) {
+          Ja[0 + 3 * nn] = Ja[0 + 3 * nn] - DCL_N[j + n * q] * R_CL_N[2 + 3 * nn + 9 * NI(i, q, k)];
+          Ja[1 + 3 * nn] = Ja[1 + 3 * nn] - DCL_N[k + n * q] * R_CL_N[0 + 3 * nn + 9 * NI(i, j, q)];
+          Ja[2 + 3 * nn] = Ja[2 + 3 * nn] - DCL_N[i + n * q] * R_CL_N[1 + 3 * nn + 9 * NI(q, j, k)];
+        }
+      for (int q = 0; q < n; ++q)
+        for (int nn = 0; nn < 3; ++nn) {
+          Ja[0 + 3 * nn] = Ja[0 + 3 * nn] + DCL_N[k + n * q] * R_CL_N[1 + 3 * nn + 9 * NI(i, j, q)];
+          Ja[1 + 3 * nn] = Ja[1 + 3 * nn] + DCL_N[i + n * q] * R_CL_N[2 + 3 * nn + 9 * NI(q, j, k)];
+          Ja[2 + 3 * nn] = Ja[2 + 3 * nn] + DCL_N[j + n * q] * R_CL_N[0 + 3 * nn + 9 * NI(i, q, k)];
+        }
+    }
+    // 2.c Metrics_fTilde/gTilde/hTilde = ChangeBasisVolume(Vdm_CLN_N) of JaCL_N(dd,1:3,...)
+    double* outs[3] = {o.Mf, o.Mg, o.Mh};
+    for (int dd = 0; dd < 3; ++dd) {
+      for (int t = 0; t < n3; ++t)
+        for (int nn = 0; nn < 3; ++nn) slice_n[nn + 3 * t] = JaCL_N[dd + 3 * nn + 9 * t];
+      ChangeBasis3D(3, N, N, Vdm_CLN_N.data(), slice_n.data(), outs[dd] + (size_t)3 * n3 * iElem);
+    }
+    // CalcSurfMetrics: master sides (flip 0) of this element
+    for (int iLocSide = 1; iLocSide <= 6; ++iLocSide) {
+      const int* es = ElemToSide + 3 * ((iLocSide - 1) + 6 * (size_t)iElem);
+      if (es[1] != 0) continue;
+      const size_t SideID = (size_t)es[0] - 1;
+      auto sidemap = [&](int p, int q, int& a, int& b) { SideToVol2(N, p, q, 0, iLocSide, a, b); };
+      if (o.Face_xGP) {
+        for (int b = 0; b < n; ++b) for (int a = 0; a < n; ++a)
+          for (int c = 0; c < 3; ++c) tmp[c + 3 * (a + n * b)] = XCL_N[c + 3 * face_plane_node(N, iLocSide, a, b)];
+        ChangeBasis2D(3, N, N, Vdm_CLN_N.data(), tmp.data(), tmp2.data());
+        for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
+          int a, b;
+          sidemap(p, q, a, b);
+          for (int c = 0; c < 3; ++c) o.Face_xGP[c + 3 * (p + n * (q + (size_t)n * SideID))] = tmp2[c + 3 * (a + n * b)];
+        }
+      }
+      std::fill(Ja_Face_l.begin(), Ja_Face_l.end(), 0.);
+      for (int dd = 0; dd < 3; ++dd) {
+        for (int b = 0; b < n; ++b) for (int a = 0; a < n; ++a)
+          for (int nn = 0; nn < 3; ++nn) tmp[nn + 3 * (a + n * b)] = JaCL_N[dd + 3 * nn + 9 * face_plane_node(N, iLocSide, a, b)];
+        ChangeBasis2D(3, N, N, Vdm_CLN_N.data(), tmp.data(), tmp2.data());
+        for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
+          int a, b;
+          sidemap(p, q, a, b);
+          for (int nn = 0; nn < 3; ++nn) Ja_Face_l[dd + 3 * (nn + 3 * (p + n * q))] = tmp2[nn + 3 * (a + n * b)];
+        }
+      }
+      const size_t f0 = (size_t)n * n * SideID;
+      SurfMetricsFromJa(N, kNormalDirs[iLocSide], kTangDirs[iLocSide], kNormalSigns[iLocSide], Ja_Face_l.data(),
+                        o.NormVec + 3 * f0, o.TangVec1 + 3 * f0, o.TangVec2 + 3 * f0, o.SurfElem + f0);
+    }
+  }
+  return bad;
+}
+
 // InitFilter (filter.f90:100-222) with HestFilter (:231-263) and buildLegendreVdm (basis.f90:100-160)
 static int InitFilter(Ctx& C) {
   const dg_config& c = C.cfg;
@@ -2076,6 +2324,17 @@ int orc_change_basis_3d(int nVar, int NIn, int NOut, const double* Vx, const dou
                         const double* X_In, double* X_Out) {
   ChangeBasis3D_XYZ(nVar, NIn, NOut, Vx, Vy, Vz, X_In, X_Out);
   return 0;
+}
+
+// The oracle's own geometry: BuildCoords + CalcMetrics + CalcSurfMetrics from the equidistant NodeCoords
+// (3,0:NGeo,0:NGeo,0:NGeo,nElems) and ElemToSide(3,6,nElems) (1-based side IDs; the master sides, flip
+// 0, receive the side vectors).  Elem_xGP and Face_xGP may be null.  Returns the count of solution
+// nodes with a scaled Jacobian below 0.01, or -1 for a non-positive Jacobian.
+int orc_calc_metrics(int N, int node_type, int NGeo, int nElems, const double* NodeCoords, const int* ElemToSide,
+                     double* Elem_xGP, double* Mf, double* Mg, double* Mh, double* sJ, double* NormVec, double* TangVec1,
+                     double* TangVec2, double* SurfElem, double* Face_xGP) {
+  MetricsOut o{Elem_xGP, Mf, Mg, Mh, sJ, NormVec, TangVec1, TangVec2, SurfElem, Face_xGP};
+  return CalcMetrics(N, node_type, NGeo, nElems, NodeCoords, ElemToSide, o);
 }
 
 int orc_laf_state(orc_handle* h, double* lim, double* eRatio, double* r) {

@@ -41,6 +41,8 @@ def lib():
         L.orc_rhs.argtypes = [_P, _P, _P]
         L.orc_get_work.argtypes = [_P, ctypes.c_int, _P]
         L.orc_lserk_steps.argtypes = [_P, ctypes.c_double, ctypes.c_double, ctypes.c_int, _P, _P]
+        L.orc_calc_metrics.restype = ctypes.c_int
+        L.orc_calc_metrics.argtypes = [ctypes.c_int] * 4 + [_P] * 12
         L.orc_calc_timestep.restype = ctypes.c_double
         L.orc_calc_timestep.argtypes = [_P, _P, ctypes.c_double, ctypes.c_double, ctypes.POINTER(ctypes.c_int)]
         _lib = L
@@ -103,11 +105,62 @@ def change_basis_3d(X, Vx, Vy=None, Vz=None):
     return out
 
 
+def calc_metrics(N, node_type, NGeo, NodeCoords, ElemToSide, nSides):
+    """The oracle's own geometry (BuildCoords + CalcMetrics + CalcSurfMetrics) from the equidistant
+    node coordinates NodeCoords (nElems, NGeo+1, NGeo+1, NGeo+1, 3) (C order of the Fortran
+    (3,0:NGeo,0:NGeo,0:NGeo,nElems)) and ElemToSide (nElems, 6, 3).  Returns a dict with the mesh
+    arrays of the reference (Elem_xGP, Metrics_f/g/hTilde, sJ, NormVec, TangVec1/2, SurfElem,
+    Face_xGP) in the same shapes as galaexi_gb300.Mesh, and "bad_nodes" (scaled Jacobian < 0.01)."""
+    NC = np.ascontiguousarray(NodeCoords, dtype=np.float64)
+    E2S = np.ascontiguousarray(ElemToSide, dtype=np.int32)
+    E, n = NC.shape[0], N + 1
+    out = {"Elem_xGP": np.zeros((E, n, n, n, 3)), "Metrics_fTilde": np.zeros((E, n, n, n, 3)),
+           "Metrics_gTilde": np.zeros((E, n, n, n, 3)), "Metrics_hTilde": np.zeros((E, n, n, n, 3)),
+           "sJ": np.zeros((E, n, n, n)), "NormVec": np.zeros((nSides, n, n, 3)), "TangVec1": np.zeros((nSides, n, n, 3)),
+           "TangVec2": np.zeros((nSides, n, n, 3)), "SurfElem": np.zeros((nSides, n, n)),
+           "Face_xGP": np.zeros((nSides, n, n, 3))}
+    keys = ("Elem_xGP", "Metrics_fTilde", "Metrics_gTilde", "Metrics_hTilde", "sJ", "NormVec", "TangVec1", "TangVec2",
+            "SurfElem", "Face_xGP")
+    out["bad_nodes"] = lib().orc_calc_metrics(int(N), int(node_type), int(NGeo), E, _p(NC), _p(E2S),
+                                              *[_p(out[k]) for k in keys])
+    return out
+
+
+class _Geometry:
+    """Mesh arrays from the oracle's own metric computation, with the connectivity of a mesh."""
+
+    def __init__(self, mesh):
+        g = calc_metrics(mesh.N, mesh.node_type, mesh.NGeo, mesh.NodeCoords, mesh.ElemToSide, mesh.nSides)
+        if g["bad_nodes"] != 0:
+            raise ValueError("oracle metrics: %d nodes with a bad Jacobian" % g["bad_nodes"])
+        for k, v in g.items():
+            setattr(self, k, v)
+        for k in ("N", "node_type", "NGeo", "nElems", "nSides", "ElemToSide", "SideToElem", "NodeCoords"):
+            setattr(self, k, getattr(mesh, k))
+        self.nBCSides = getattr(mesh, "nBCSides", 0)
+
+    @property
+    def nDOF(self):
+        return self.nElems * (self.N + 1) ** 3
+
+
 class Oracle:
     """CPU restatement of DGTimeDerivative_weakForm / TimeStepByLSERKW2 on one mesh."""
 
-    def __init__(self, cfg, mesh, boundaries=None):
-        """boundaries: (bc_type, bc_state, refstates) of the mesh's BC sides, as for the DG operator."""
+    def __init__(self, cfg, mesh, boundaries=None, geometry="auto"):
+        """boundaries: (bc_type, bc_state, refstates) of the mesh's BC sides, as for the DG operator.
+        geometry: "own" computes the metric arrays here from the mesh's node coordinates
+        (calc_metrics) and takes only its connectivity; "mesh" takes the metric arrays of the mesh
+        object; "auto" is "own" for curved and file meshes and "mesh" for the affine generated box,
+        whose metric terms are exact constants (the curl form of the reference reproduces them up
+        to round-off, ~4e-14 relative, which the tests pin separately)."""
+        if geometry == "auto":
+            affine_box = getattr(mesh, "deform", None) == 0.0 and not hasattr(mesh, "path")
+            geometry = "mesh" if (affine_box or not hasattr(mesh, "NodeCoords")) else "own"
+        if geometry == "own":
+            mesh = _Geometry(mesh)
+        elif geometry != "mesh":
+            raise ValueError("geometry: 'auto', 'mesh' or 'own'")
         self.cfg, self.mesh = cfg, mesh
         m = mesh
         self._keep = [m.Metrics_fTilde, m.Metrics_gTilde, m.Metrics_hTilde, m.sJ, m.NormVec, m.TangVec1, m.TangVec2,
@@ -163,6 +216,13 @@ class Oracle:
         Ut_tmp = np.zeros_like(U) if Ut_tmp is None else np.array(Ut_tmp, dtype=np.float64, copy=True)
         lib().orc_lserk_steps(self._h, float(t), float(dt), int(nSteps), _p(U), _p(Ut_tmp))
         return U, Ut_tmp
+
+    def lserk_steps_inplace(self, U, Ut_tmp, dt, nSteps, t=0.0):
+        """lserk_steps on C-contiguous float64 arrays U and Ut_tmp, updated in place."""
+        for a in (U, Ut_tmp):
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous):
+                raise ValueError("lserk_steps_inplace needs C-contiguous float64 arrays")
+        lib().orc_lserk_steps(self._h, float(t), float(dt), int(nSteps), _p(U), _p(Ut_tmp))
 
     def calc_timestep(self, U, cfl, dfl=0.0):
         U = np.ascontiguousarray(U, dtype=np.float64)

@@ -1,4 +1,5 @@
-"""The Fortran interface module (include/galaexi_gb300.f90) against the C header and the library.
+"""The Fortran interface modules (include/galaexi_gb300.f90, and the CUDA Fortran module
+include/galaexi_gb300_cuf.cuf) against the C header and the library.
 
 No Fortran compiler exists in this image, so the module is checked by reading it: every function the C
 header declares has exactly one BIND(C) procedure with the same number of arguments, exported by
@@ -16,10 +17,10 @@ F90 = os.path.join(ROOT, "include", "galaexi_gb300.f90")
 HDR = os.path.join(ROOT, "include", "galaexi_gb300.h")
 
 
-def _fortran_statements():
+def _fortran_statements(path=F90):
     """Free-form statements with continuation lines joined and comments dropped."""
     out, cur = [], ""
-    for line in open(F90):
+    for line in open(path):
         code = line.split("!", 1)[0].rstrip()
         if not code.strip():
             continue
@@ -171,3 +172,81 @@ def test_bind_c_argument_passing_matches_c_types():
             else:
                 assert depth == 1, what
                 assert (ftype == kind[base] and not by_value) or (ftype == "TYPE(C_PTR)" and by_value), what
+
+
+CUF = os.path.join(ROOT, "include", "galaexi_gb300_cuf.cuf")
+INTEGRATION = os.path.join(ROOT, "INTEGRATION.md")
+STREAM_KIND = "INTEGER(KIND=CUDA_STREAM_KIND)"
+
+
+def _cuf_interfaces():
+    """{Fortran name: (C name, [(dummy, type spec, attributes)])} of MOD_GB300_CUF."""
+    out, cur = {}, None
+    for st in _fortran_statements(CUF):
+        m = re.match(r"(?:(.+?)\s+)?(FUNCTION|SUBROUTINE)\s+(\w+)\s*\(([^)]*)\)\s*BIND\s*\(\s*C\s*,\s*NAME\s*=\s*'(\w+)'",
+                     st, flags=re.I)
+        if m:
+            cur = {"c": m.group(5), "dummies": [a.strip() for a in m.group(4).split(",") if a.strip()], "decl": {}}
+            out[m.group(3).lower()] = cur
+            continue
+        if cur is None or re.match(r"(IMPORT|END\s)", st, flags=re.I):
+            if re.match(r"END\s+(FUNCTION|SUBROUTINE)", st, flags=re.I):
+                cur = None
+            continue
+        spec, names = st.split("::")
+        attrs = [a.strip().upper() for a in re.split(r",(?![^(]*\))", spec)]
+        for nm in re.split(r",(?![^(]*\))", names):
+            cur["decl"][re.match(r"\s*(\w+)", nm).group(1).lower()] = (attrs[0], set(attrs[1:]))
+    return {k: (v["c"], [(d, *v["decl"][d.lower()]) for d in v["dummies"]]) for k, v in out.items()}
+
+
+def test_cuda_fortran_interfaces_match_header():
+    """MOD_GB300_CUF binds every entry point that takes a stream; device-pointer parameters (d_*) are
+    DEVICE arrays, the stream is a CUDA_STREAM_KIND value, the context a TYPE(C_PTR) value, host
+    pointers are host data of the C parameter's kind, scalars are values."""
+    _, decls = _c_declarations()
+    kind = {"int": "INTEGER(C_INT)", "double": "REAL(C_DOUBLE)", "size_t": "INTEGER(C_SIZE_T)",
+            "long long": "INTEGER(C_LONG_LONG)"}
+    ifaces = _cuf_interfaces()
+    with_stream = {c for c, args in decls.items() if args and args[-1].replace(" ", "") == "void*stream"}
+    assert sorted(c for c, _ in ifaces.values()) == sorted(with_stream)
+    for fname, (cname, dummies) in ifaces.items():
+        assert fname == "gb300_" + cname[3:], fname
+        assert len(dummies) == len(decls[cname]), cname
+        for (dname, ftype, attrs), cdecl in zip(dummies, decls[cname]):
+            base, depth = _c_param(cdecl)
+            cvar = re.split(r"[\s\*]+", cdecl.strip())[-1]
+            what = (cname, dname, cdecl, ftype, attrs)
+            if cvar == "stream":
+                assert ftype == STREAM_KIND and "VALUE" in attrs, what
+            elif base == "dg_ctx":
+                assert ftype == "TYPE(C_PTR)" and "VALUE" in attrs, what
+            elif depth == 0:
+                assert ftype == kind[base] and "VALUE" in attrs, what
+            elif cvar.startswith("d_"):
+                assert ftype == kind[base] and "DEVICE" in attrs and "VALUE" not in attrs, what
+            else:
+                assert ftype == kind[base] and not attrs & {"DEVICE", "VALUE"}, what
+    for i, line in enumerate(open(CUF), 1):
+        assert len(line.rstrip("\n")) <= 132, "line %d longer than 132 characters" % i
+
+
+def test_integration_call_sites_use_the_cuda_fortran_interfaces():
+    """Every gb300_* call in the integration notes names a MOD_GB300_CUF interface with its argument
+    count and passes one of the reference's streams (MOD_GPU, gpu.f90:23-45)."""
+    ifaces = _cuf_interfaces()
+    text, calls = open(INTEGRATION).read(), []
+    for m in re.finditer(r"iErr = (gb300_\w+)\(", text):
+        depth, k = 1, m.end()
+        while depth:
+            depth += {"(": 1, ")": -1}.get(text[k], 0)
+            k += 1
+        calls.append((m.group(1), text[m.end():k - 1]))
+    assert {c for c, _ in calls} >= {"gb300_rhs", "gb300_lserk_step", "gb300_calc_timestep"}
+    streams = {"defaultstream"} | {"stream%d" % k for k in range(1, 7)}
+    for fname, arglist in calls:
+        args = [a.strip() for a in re.split(r",(?![^(]*\))", arglist)]
+        assert fname in ifaces, fname
+        assert len(args) == len(ifaces[fname][1]), (fname, args)
+        assert args[-1].lower() in streams, (fname, args[-1])
+        assert not any("C_DEVLOC" in a or "C_NULL_PTR" in a for a in args), (fname, args)

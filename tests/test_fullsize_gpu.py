@@ -4,7 +4,8 @@ properties of the operator at those sizes.
 * Euler isentropic vortex, N=3 Gauss, weak form, LF, 8^3 elements on [0,10]^3 (32 768 DOF): 100
   LSERK steps at CFL 0.9, FP64, against the oracle (<= 1e-10) and against the exact solution.
 * Navier-Stokes TGV (perturbed), N=7 Gauss-Lobatto, split PI, Roe, BR1, 24^3 elements (7.08 M DOF):
-  one RHS (<= 1e-12) and two LSERK steps (<= 1e-10) against the oracle.
+  one RHS (<= 1e-12), two LSERK steps and 100 LSERK steps (<= 1e-10) against the oracle; 100 steps
+  also from the unperturbed TGV state.
 * Navier-Stokes, N=5 Gauss, weak, HLLC, BR2, 32^3 elements of the curved box (7.08 M DOF): one RHS
   against the oracle (<= 1e-12), free-stream preservation.
 * Navier-Stokes TGV as above with N=5 and 16^3 elements (the adjoint case): one RHS (<= 1e-12).
@@ -94,6 +95,51 @@ def test_tgv_n7_24cube_rhs_and_steps_full_size():
     torch.cuda.synchronize()
     assert rel(U.cpu().numpy(), ref) <= 1e-10
     op.close()
+
+
+@pytest.mark.parametrize("state", ["perturbed", "tgv"])
+def test_tgv_n7_24cube_100_steps_full_size(state):
+    """The benchmark workload at full size (N=7 Gauss-Lobatto, split PI, Roe, BR1, 24^3 elements,
+    7.08 M DOF): 100 LSERK steps at CFLscale = DFLscale = 0.8 on the GPU and in the oracle, both from
+    the same state with the oracle's time step; relative L2 of the end states <= 1e-10.  "perturbed":
+    the seeded perturbed TGV state; "tgv": the unperturbed TGV initial state of the workload, for
+    which the relative L2 of the change U - U0 is reported as well (its flow is nearly steady, so that
+    change is small and its relative difference larger)."""
+    m, kw, U0 = tgv(7, 24)
+    if state == "tgv":
+        U0 = gx.tgv_state(m, mach=0.1, R=TGV_R)
+    cfg = gx.config(**kw)
+    o = Oracle(cfg, m)
+    dt, _ = o.calc_timestep(U0, 0.8, 0.8)
+    ref, _ = o.lserk_steps(U0, dt, 100)
+    o.close()
+    op = gx.DG(cfg, m)
+    U = torch.from_numpy(U0.copy()).cuda()
+    op.TimeStepByLSERKW2(0.0, dt, U, torch.zeros_like(U), nSteps=100)
+    torch.cuda.synchronize()
+    got = U.cpu().numpy()
+    op.close()
+    err, derr = rel(got, ref), rel(got - U0, ref - U0)
+    # the mixed form over the same 100 steps against the oracle's FP64 end state: kinetic energy,
+    # mass and relative L2 (north-star bar: kinetic energy <= 1e-6)
+    opm = gx.DG(gx.config(precision="mixed", **kw), m)
+    Um = torch.from_numpy(U0.copy()).cuda()
+    opm.TimeStepByLSERKW2(0.0, dt, Um, torch.zeros_like(Um), nSteps=100)
+    torch.cuda.synchronize()
+    opm.close()
+    op64 = gx.DG(cfg, m)
+    I_ref, I_mix = op64.integrals(torch.from_numpy(ref).cuda()), op64.integrals(Um)
+    op64.close()
+    ke_err = abs(I_mix[5] - I_ref[5]) / abs(I_ref[5])
+    mass_err = abs(I_mix[0] - I_ref[0]) / abs(I_ref[0])
+    l2_mixed = rel(Um.cpu().numpy(), ref)
+    print("C2 100 steps (%s): FP64 relative L2 of U %.3e, of U - U0 %.3e; mixed vs the oracle: kinetic "
+          "energy %.3e, mass %.3e, relative L2 %.3e" % (state, err, derr, ke_err, mass_err, l2_mixed))
+    assert err <= 1e-10, err
+    assert derr <= 1e-8, derr
+    assert ke_err <= 1e-6, ke_err
+    assert mass_err <= 1e-9, mass_err
+    assert l2_mixed <= 1e-5, l2_mixed
 
 
 def test_tgv_n5_16cube_rhs_full_size():

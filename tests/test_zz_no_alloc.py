@@ -51,6 +51,27 @@ def test_noalloc_timestep_matches_context_entry_point_twice():
         ref, err = op.CalcTimeStep(Ud, cfl, dfl)
         assert err == 0
         assert abs(dt - ref) <= RTOL * ref, (dt, ref)
+    op.close()
+
+
+def test_noalloc_timestep_allocates_nothing():
+    """After one call, further calls leave the device's free memory unchanged (cudaMemGetInfo): the
+    entry point allocates nothing, neither directly nor through a library."""
+    cfg = gx.config(N=5, Riemann="roe", SplitDG="pi", parabolic=True, mu0=1e-3, R=71.42857)
+    mesh = gx.Mesh(5, 2, 4, 4, 4, (-math.pi,) * 3, (math.pi,) * 3)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    Mf, Mg, Mh, sJ = dev(mesh.Metrics_fTilde), dev(mesh.Metrics_gTilde), dev(mesh.Metrics_hTilde), dev(mesh.sJ)
+    U = dev(gx.tgv_state(mesh, mach=0.1, R=71.42857))
+    rc, dt0 = noalloc_dt(cfg, mesh, U, Mf, Mg, Mh, sJ, 0.8, 0.8)
+    assert rc == nat.DG_OK
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(5):
+        rc, dt = noalloc_dt(cfg, mesh, U, Mf, Mg, Mh, sJ, 0.8, 0.8)
+        assert rc == nat.DG_OK and dt == dt0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
 
 
 def test_noalloc_timestep_reports_bad_state_and_limit():
