@@ -477,8 +477,12 @@ def scale_c5(stream, steps=100, adj_steps=50, budget_gb=180):
     steps from the TGV state, then the adjoint of an `adj_steps` window (kinetic-energy objective)
     with checkpoints in at most `budget_gb` of device memory (less if the operator, ~61 GB at this
     size, and the adjoint's work states and scratch leave less free)."""
+    import gc
     import torch
     import galaexi_gb300 as gx
+    # the checkpoint budget below is what the device has free: release what earlier measurements left
+    gc.collect()
+    torch.cuda.empty_cache()
     w = WORKLOADS["tgv_n7_64cube_split_pi_roe_br1"]
     N, ne = w["N"], w["ne"]
     mesh = gx.Mesh(N, 2, ne, ne, ne, (-math.pi,) * 3, (math.pi,) * 3)
@@ -522,13 +526,16 @@ def scale_c5(stream, steps=100, adj_steps=50, budget_gb=180):
         return U
 
     ms_f = timed(fwd, stream)[0]
+    gc.collect()
     torch.cuda.empty_cache()
     # checkpoint budget: at most budget_gb (decimal GB), and what is left of the device after the
     # operator, the adjoint's work states and scratch, the gradient tensor and a 2 GiB margin; the
     # end state is written over U0
-    free, _ = torch.cuda.mem_get_info()
+    free, total = torch.cuda.mem_get_info()
     state = U0.numel() * 8
     budget = int(min(budget_gb * 1e9, free - op.adjoint_scratch_bytes() - state - 2 * 2 ** 30))
+    res["device_free_gb_before_adjoint"] = free / 1e9
+    res["device_total_gb"] = total / 1e9
     Uf, plan = None, None
     t_rec, (Uf, plan) = timed(lambda: op.adjoint_forward(dt, adj_steps, U0, budget, out=U0), stream)
     J, G = op.kinetic_energy(Uf, grad=True)

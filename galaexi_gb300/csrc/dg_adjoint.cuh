@@ -23,9 +23,11 @@
 // The viscosity derivative <Ut_bar, dR/dmu> is accumulated on the way (R is linear in mu at fixed
 // Prandtl number): per-block partial sums, reduced in a fixed order by k_adj_sum.
 //
+//   ka_bc_face / ka_bc_jump   the boundary sides' flux and lifting ghost state, transposed through
+//                             local Jacobians on dual numbers (meshes with boundary sides)
 // Supported forms: Gauss or Gauss-Lobatto nodes; weak form or split form PI / KG; any Riemann solver;
 // Euler or Navier-Stokes with BR1 lifting in strong form (non-conservative or conservative volume
-// part).
+// part); periodic meshes and meshes with boundary sides of the types of dg_bc.cuh.
 #pragma once
 #include "dg_kernels.cuh"
 #include "dg_riemann_vjp.cuh"
@@ -53,6 +55,11 @@ struct AdjLaunch {
   double mu, lambda, lamc;  // mu, lambda, lambda/mu (the thermal conductivity per unit viscosity)
   double inv_mu;            // 1/mu, or 0 for mu = 0
   double kappa, sR;
+  // boundary sides (the first nBCSides sides): type, 0-based reference state, states [state][6]
+  int nBCSides;
+  const int* bctype;
+  const int* bcstate;
+  const double* bcref;
 };
 
 // Transpose of one directional BR1 viscous flux  f = normal_diff_flux(P, g, nv, mu, lambda)
@@ -140,7 +147,8 @@ ka_face(CotSrc cs, const double* __restrict__ Met, const double* __restrict__ Uf
         double* __restrict__ mupart) {
   constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, N = NP - 1;
   __shared__ double red[4];
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  // connected sides only (nBCSides .. nSides-1); the BC sides are ka_bc_face's
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x + (long long)L.nBCSides * n2;
   double mub = 0.;
   if (t < (long long)L.nSides * n2) {
     const int side = (int)(t / n2), pq = (int)(t - (long long)side * n2);
@@ -627,7 +635,8 @@ ka_volume(CotSrc cs, const double* __restrict__ U, const double* __restrict__ Pv
 // ---------------------------------------------------------------------------------------------
 static __global__ void __launch_bounds__(256)
 ka_jump(const double* __restrict__ Uf, const double* __restrict__ JB, AdjLaunch L, int n2, double* __restrict__ UfB) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  // connected sides only; the BC sides' lifting jump goes through the ghost state (ka_bc_jump)
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x + (long long)L.nBCSides * n2;
   if (t >= (long long)L.nSides * n2) return;
   const int side = (int)(t / n2), pq = (int)(t - (long long)side * n2);
   const size_t S = L.nSides;
@@ -649,6 +658,156 @@ ka_jump(const double* __restrict__ Uf, const double* __restrict__ JB, AdjLaunch 
 #pragma unroll
     for (int v = 0; v < 5; ++v) UfB[((size_t)slot * S + side) * 5 * n2 + v * n2 + pq] = fb[v];
   }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Boundary sides.  The forward boundary flux k_bc_face (GetBoundaryFlux_GPU, getboundaryflux.f90:
+// 542-838) and the lifting ghost state of k_bc_lift_ghost (Lifting_GetBoundaryFlux_Kernel, :945-1019)
+// depend on the master face state U_f (through ConsToPrim) and, for the flux, on the master face
+// gradients G_f and the viscosity.  Their transposes take the local Jacobians by forward-mode dual
+// numbers (the forward device code instantiated on Dual<K>): few face nodes are boundary nodes.
+// ---------------------------------------------------------------------------------------------
+template <int K>
+__device__ __forceinline__ Gas<Dual<K>> dual_gas(const Gas<double>& g, int mu_slot, double lamc) {
+  using D = Dual<K>;
+  Gas<D> r;
+  r.kappa = D(g.kappa); r.kappaM1 = D(g.kappaM1); r.sKappaM1 = D(g.sKappaM1); r.R_gas = D(g.R_gas);
+  r.mu = D(g.mu); r.lambda = D(g.lambda); r.sR = D(g.sR);
+  r.pref = D(0.); r.prefD = 0.; r.kappaM1D = g.kappaM1D; r.sRD = g.sRD;
+  if (mu_slot >= 0) { r.mu.d[mu_slot] = 1.; r.lambda.d[mu_slot] = lamc; }
+  return r;
+}
+
+// ka_bc_face: thread per BC face node.  Flux cotangent (transposed SurfInt of the master element,
+// times SurfElem) through the boundary flux's Jacobian with respect to U_f (5), the lifted gradients
+// of u, v, w, T in x, y, z (12) and mu (slot 17): cotangents of U_f and G_f of the master side and
+// the block's share of <Ut_bar, dR/dmu>.
+template <int NP>
+__global__ void __launch_bounds__(128)
+ka_bc_face(CotSrc cs, const double* __restrict__ Met, const double* __restrict__ Uf, const double* __restrict__ Gf,
+           const double* __restrict__ Fgeo, const int* __restrict__ S2E, DevBasis<double> basis, Gas<double> gas,
+           AdjLaunch L, double* __restrict__ UfB, double* __restrict__ GfB, double* __restrict__ mupart) {
+  constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, N = NP - 1;
+  using D = Dual<18>;
+  __shared__ double red[4];
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double mub = 0.;
+  if (t < (long long)L.nBCSides * n2) {
+    const int side = (int)(t / n2), pq = (int)(t - (long long)side * n2);
+    const int p = pq % n, q = pq / n;
+    const int e = S2E[(size_t)side * 5], ls = S2E[(size_t)side * 5 + 1];
+    int a, b;
+    s2v2(N, p, q, 0, ls, a, b);
+    const bool minus = is_minus(ls);
+    double Fb[5] = {0, 0, 0, 0, 0};
+    const int l0 = L.gauss ? 0 : (minus ? 0 : N), l1 = L.gauss ? N : l0;
+    for (int l = l0; l <= l1; ++l) {
+      const double Lh = L.gauss ? (minus ? basis.Lhm[l] : basis.Lhp[l]) : (minus ? basis.Lhm[0] : basis.Lhp[N]);
+      const int node = face_node(n, ls, a, b, l);
+      const double sj = Met[((size_t)e * 10 + 9) * n3 + node];
+      double ub[5];
+      cot_at(cs, ((size_t)e * n3 + node) * 5, ub);
+      const double w = -Lh * sj;
+#pragma unroll
+      for (int v = 0; v < 5; ++v) Fb[v] = Fb[v] + w * ub[v];
+    }
+    const double* fg = Fgeo + (size_t)side * 10 * n2 + pq;
+    const double se = fg[9 * n2];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) Fb[v] *= se;
+    // the boundary flux on dual numbers: seeds U_f (0..4), gradients of u, v, w, T (5..16), mu (17)
+    const Gas<D> g = dual_gas<18>(gas, 17, L.lamc);
+    D U[5], PL[6], srho, gx[5], gy[5], gz[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      U[v] = D(Uf[(size_t)side * 5 * n2 + v * n2 + pq]);
+      U[v].d[v] = 1.;
+    }
+    cons_to_prim_d(U, g, PL, srho);
+    const double* gm = Gf + (size_t)side * 15 * n2 + pq;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      gx[v] = D(L.parabolic ? gm[v * n2] : 0.);
+      gy[v] = D(L.parabolic ? gm[(5 + v) * n2] : 0.);
+      gz[v] = D(L.parabolic ? gm[(10 + v) * n2] : 0.);
+    }
+#pragma unroll
+    for (int v = 1; v < 5; ++v) { gx[v].d[4 + v] = 1.; gy[v].d[8 + v] = 1.; gz[v].d[12 + v] = 1.; }
+    const D nv[3] = {D(fg[0]), D(fg[n2]), D(fg[2 * n2])};
+    const D t1[3] = {D(fg[3 * n2]), D(fg[4 * n2]), D(fg[5 * n2])};
+    const D t2[3] = {D(fg[6 * n2]), D(fg[7 * n2]), D(fg[8 * n2])};
+    const double* rs = L.bcref + 6 * L.bcstate[side];
+    const D ref[6] = {D(rs[0]), D(rs[1]), D(rs[2]), D(rs[3]), D(rs[4]), D(rs[5])};
+    D F[5];
+    bc_face_flux(L.bctype[side], PL, gx, gy, gz, nv, t1, t2, ref, g, L.riemann, L.split, L.parabolic, F);
+    double ub[5] = {0, 0, 0, 0, 0}, gb[15];
+#pragma unroll
+    for (int c = 0; c < 15; ++c) gb[c] = 0.;
+#pragma unroll
+    for (int w = 0; w < 5; ++w) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) ub[v] += Fb[w] * F[w].d[v];
+#pragma unroll
+      for (int v = 1; v < 5; ++v) {
+        gb[v] += Fb[w] * F[w].d[4 + v];
+        gb[5 + v] += Fb[w] * F[w].d[8 + v];
+        gb[10 + v] += Fb[w] * F[w].d[12 + v];
+      }
+      mub += Fb[w] * F[w].d[17];
+    }
+#pragma unroll
+    for (int v = 0; v < 5; ++v) UfB[(size_t)side * 5 * n2 + v * n2 + pq] = ub[v];
+    if (L.parabolic) {
+#pragma unroll
+      for (int c = 0; c < 15; ++c) GfB[(size_t)side * 15 * n2 + c * n2 + pq] = gb[c];
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) mub += __shfl_xor_sync(0xffffffffu, mub, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mub;
+  __syncthreads();
+  if (threadIdx.x == 0) mupart[blockIdx.x] = red[0] + red[1] + red[2] + red[3];
+}
+
+// ka_bc_jump: thread per BC face node.  The master element's lifting used the jump ghost(P_m) - P_m of
+// the lifted variables (rho, u, v, w, T); its cotangent (the master share of JB) goes through that jump's
+// Jacobian with respect to U_f (ConsToPrim, GetBoundaryState, the ghost state) into the U_f cotangent.
+static __global__ void __launch_bounds__(256)
+ka_bc_jump(const double* __restrict__ Uf, const double* __restrict__ JB, const double* __restrict__ Fgeo,
+           Gas<double> gas, AdjLaunch L, int n2, double* __restrict__ UfB) {
+  using D = Dual<5>;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)L.nBCSides * n2) return;
+  const int side = (int)(t / n2), pq = (int)(t - (long long)side * n2);
+  const Gas<D> g = dual_gas<5>(gas, -1, 0.);
+  D U[5], Pm[6], srho, Pb[6], gh[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    U[v] = D(Uf[(size_t)side * 5 * n2 + v * n2 + pq]);
+    U[v].d[v] = 1.;
+  }
+  cons_to_prim_d(U, g, Pm, srho);
+  const double* fg = Fgeo + (size_t)side * 10 * n2 + pq;
+  const D nv[3] = {D(fg[0]), D(fg[n2]), D(fg[2 * n2])};
+  const D t1[3] = {D(fg[3 * n2]), D(fg[4 * n2]), D(fg[5 * n2])};
+  const D t2[3] = {D(fg[6 * n2]), D(fg[7 * n2]), D(fg[8 * n2])};
+  const double* rs = L.bcref + 6 * L.bcstate[side];
+  const D ref[6] = {D(rs[0]), D(rs[1]), D(rs[2]), D(rs[3]), D(rs[4]), D(rs[5])};
+  const int bt = L.bctype[side];
+  bc_state(bt, Pm, ref, nv, t1, t2, g.kappa, g.R_gas, Pb);
+  bc_lift_ghost(bt, Pm, Pb, gh);
+  const int liftc[5] = {0, 1, 2, 3, 5};
+  double ub[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) ub[v] = UfB[(size_t)side * 5 * n2 + v * n2 + pq];
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    const double jb = JB[(size_t)side * 5 * n2 + c * n2 + pq];
+    const D jump = gh[c] - Pm[liftc[c]];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) ub[v] += jb * jump.d[v];
+  }
+#pragma unroll
+  for (int v = 0; v < 5; ++v) UfB[(size_t)side * 5 * n2 + v * n2 + pq] = ub[v];
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -115,6 +115,10 @@ int alloc_prec(dg_ctx* ctx, gxc::PrecData<R>& P, const std::vector<double>& met,
   bool ok = P.Met.alloc(nE * 10 * n3) && P.Fgeo.alloc(nS * 10 * n2) && P.Pvol.alloc(nE * 7 * n3) &&
             P.Uf.alloc(2 * nS * 5 * n2) && P.Pf.alloc(2 * nS * 6 * n2) && P.Flux.alloc(nS * 5 * n2);
   if (ok && par) ok = P.Gvol.alloc(nE * 15 * n3) && P.Gf.alloc(2 * nS * 15 * n2);
+  // the mixed split form (SD, KG, PI) at N = 3..7 takes its split volume term from the line kernel
+  const int sp = ctx->cfg.split_dg;
+  if (ok && sizeof(R) == 4 && (sp == DG_SPLIT_SD || sp == DG_SPLIT_KG || sp == DG_SPLIT_PI) && ctx->n >= 4 && ctx->n <= 8)
+    ok = P.Vs.alloc(nE * 5 * n3);
   if (!ok) { set_error("cudaMalloc scratch"); return DG_ERR_ALLOC; }
   std::vector<R> hm(met.size()), hg(fgeo.size());
   for (size_t t = 0; t < met.size(); ++t) hm[t] = (R)met[t];
@@ -300,7 +304,6 @@ int tlm_setup(dg_ctx* ctx) {
 
 int adj_setup(dg_ctx* ctx) {
   if (int rc = need_fp64(ctx, "adjoint")) return rc;
-  if (ctx->nBCSides) { set_error("adjoint: periodic meshes only"); return DG_ERR_UNSUPPORTED; }
   if (ctx->cfg.filter_type) { set_error("adjoint: no solution filter"); return DG_ERR_UNSUPPORTED; }
   const dg_config& c = ctx->cfg;
   if (c.split_dg != DG_SPLIT_NONE && c.split_dg != DG_SPLIT_PI && c.split_dg != DG_SPLIT_KG) {
@@ -314,7 +317,8 @@ int adj_setup(dg_ctx* ctx) {
   if (int rc = T->configure_a()) return rc;
   const size_t nE = ctx->nElems, nS = ctx->nSides, n2 = ctx->n2, n3 = ctx->n3;
   const size_t epb = n3 >= 128 ? 1 : 256 / n3;
-  const size_t nparts = (nS * n2 + 127) / 128 + (nE + epb - 1) / epb;
+  // partial sums of dR/dmu: ka_face (connected sides), ka_volume, ka_bc_face (BC sides)
+  const size_t nparts = (nS * n2 + 127) / 128 + 1 + (nE + epb - 1) / epb;
   const size_t ipart = 6 * (size_t)grid_for(nE * n3);
   bool ok = ctx->UfB.alloc(2 * nS * 5 * n2) && ctx->JB.alloc(2 * nS * 5 * n2) && ctx->UBv.alloc(nE * 5 * n3) &&
             ctx->part.alloc(nparts > ipart ? nparts : ipart) && ctx->acc.alloc(8);

@@ -12,10 +12,15 @@
 
 namespace gxc {
 
+// device buffer, freed when it goes out of scope (or by release())
 template <typename T>
 struct DBuf {
   T* p = nullptr;
   size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() { release(); }
   bool alloc(size_t cnt) {
     release();
     if (cnt == 0) return true;
@@ -31,9 +36,10 @@ template <typename R>
 struct PrecData {
   DBuf<R> basis;  // D, DhatT, DVS (n^2 each), Lm, Lp, Lhm, Lhp (n each)
   DBuf<R> Met, Fgeo, Pvol, Gvol, Uf, Pf, Gf, Flux;
+  DBuf<R> Vs;     // [e][5][n^3] split-form volume term of the line kernel (mixed split form)
   void release() {
     basis.release(); Met.release(); Fgeo.release(); Pvol.release(); Gvol.release();
-    Uf.release(); Pf.release(); Gf.release(); Flux.release();
+    Uf.release(); Pf.release(); Gf.release(); Flux.release(); Vs.release();
   }
 };
 

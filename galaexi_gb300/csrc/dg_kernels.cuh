@@ -22,6 +22,7 @@
 #pragma once
 #include "dg_physics.cuh"
 #include "dg_bc.cuh"
+#include "dg_lines.cuh"
 
 namespace gx {
 
@@ -107,6 +108,21 @@ struct Launch {
   const int* bcstate;
   const void* bcref;
 };
+
+// Shared-memory position of node i + n(j + nk) in the element stagings of k_lift and k_volume.  N=7: the i and j bits
+// are XOR-swizzled with bits of j and k so that the x-, y- and z-line threads of phase B and the
+// node threads hit 32 distinct FP32 banks (two wavefronts per FP64 access); the plain layout gave
+// 8-way (FP32) and 16-way (FP64) conflicts on the x-lines.  An involution that permutes each block
+// of 32 consecutive nodes.
+template <int NP>
+__device__ __forceinline__ int vsw(int node) {
+  if constexpr (NP == 8) {
+    const int kk = (node >> 6) & 3;
+    return node ^ ((((node >> 5) & 1) << 2) | kk | (kk << 3));
+  } else {
+    return node;
+  }
+}
 
 template <int NP> struct EPBof { static constexpr int v = (NP * NP * NP >= 128) ? 1 : (256 / (NP * NP * NP)); };
 // k_lift: shared-memory slots per element of the region that holds the lifted primitives (5 n^3) and
@@ -322,7 +338,7 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
   for (int t = threadIdx.x; t < nloc * 5 * n3; t += blockDim.x) {
     int el = t / (5 * n3), r = t - el * 5 * n3;
     int c = r / n3, node = r - c * n3;
-    Ps[el][c][node] = Pvol[(size_t)(e0 + el) * 7 * n3 + liftc[c] * n3 + node];
+    Ps[el][c][vsw<NP>(node)] = Pvol[(size_t)(e0 + el) * 7 * n3 + liftc[c] * n3 + node];
   }
   __syncthreads();
   // thread per (element, node): the block has EPB * n^3 threads
@@ -346,9 +362,9 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
         const R dxi = sb.D[i + n * l], deta = sb.D[j + n * l], dzeta = sb.D[k + n * l];
 #pragma unroll
         for (int v = V0; v < 5; ++v) {
-          gxi[v] = gxi[v] + dxi * Ps[el][v][l + n * (j + n * k)];
-          geta[v] = geta[v] + deta * Ps[el][v][i + n * (l + n * k)];
-          gzeta[v] = gzeta[v] + dzeta * Ps[el][v][i + n * (j + n * l)];
+          gxi[v] = gxi[v] + dxi * Ps[el][v][vsw<NP>(l + n * (j + n * k))];
+          geta[v] = geta[v] + deta * Ps[el][v][vsw<NP>(i + n * (l + n * k))];
+          gzeta[v] = gzeta[v] + dzeta * Ps[el][v][vsw<NP>(i + n * (j + n * l))];
         }
       }
       const R mf[3] = {sj * M[0], sj * M[n3], sj * M[2 * n3]}, mg[3] = {sj * M[3 * n3], sj * M[4 * n3], sj * M[5 * n3]},
@@ -372,7 +388,8 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
           const int ni = l + n * (j + n * k), nj = i + n * (l + n * k), nk = i + n * (j + n * l);
           const R wf = ci * Me[(0 + d) * n3 + ni], wh = ck * Me[(6 + d) * n3 + nk], wg = cj * Me[(3 + d) * n3 + nj];
 #pragma unroll
-          for (int v = V0; v < 5; ++v) g[d][v] = g[d][v] + wf * Ps[el][v][ni] + wh * Ps[el][v][nk] + wg * Ps[el][v][nj];
+          for (int v = V0; v < 5; ++v)
+            g[d][v] = g[d][v] + wf * Ps[el][v][vsw<NP>(ni)] + wh * Ps[el][v][vsw<NP>(nk)] + wg * Ps[el][v][vsw<NP>(nj)];
         }
 #pragma unroll
         for (int v = V0; v < 5; ++v) g[d][v] = sj * g[d][v];
@@ -385,7 +402,7 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
 #pragma unroll
       for (int d = 0; d < 3; ++d)
 #pragma unroll
-        for (int v = V0; v < 5; ++v) Gs[el][d * 5 + v][node] = g[d][v];
+        for (int v = V0; v < 5; ++v) Gs[el][d * 5 + v][vsw<NP>(node)] = g[d][v];
     }
   }
   if (facepass) {
@@ -402,7 +419,7 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
         const int a = ab % n, b = ab / n;
         const int ls = dir == 0 ? (minus ? L_XI_MINUS : L_XI_PLUS)
                                 : (dir == 1 ? (minus ? L_ETA_MINUS : L_ETA_PLUS) : (minus ? L_ZETA_MINUS : L_ZETA_PLUS));
-        const int node = face_node(n, ls, a, b, minus ? 0 : N);
+        const int node = face_node(n, ls, a, b, minus ? 0 : N), snode = vsw<NP>(node);
         const int e = e0 + el;
         const R Lhat = minus ? sb.Lhm[0] : sb.Lhp[N];
         const int side = E2S[(e * 6 + ls - 1) * 2 + 0];
@@ -422,7 +439,7 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
           const int c = liftc[v];
           const R fl = sigflux * pm[c * n2] + ps[c * n2];
 #pragma unroll
-          for (int d = 0; d < 3; ++d) Gs[el][d * 5 + v][node] = Gs[el][d * 5 + v][node] + fl * nvv[d];
+          for (int d = 0; d < 3; ++d) Gs[el][d * 5 + v][snode] = Gs[el][d * 5 + v][snode] + fl * nvv[d];
         }
       }
       __syncthreads();
@@ -431,7 +448,7 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
       R* G = Gvol + (size_t)e * 15 * n3 + node;
 #pragma unroll
       for (int c = 0; c < 15; ++c)
-        if (c % 5 >= V0) G[c * n3] = Gs[el][c][node];
+        if (c % 5 >= V0) G[c * n3] = Gs[el][c][vsw<NP>(node)];
     }
   } else {
     // surface part (SurfInt_Device_Single_Flux, surfint.t90:591-725) of the BR1 flux
@@ -500,7 +517,7 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
 #pragma unroll
         for (int v = V0; v < 5; ++v) {
           const R val = g[d][v];
-          if (!L.br2) Gs[el][d * 5 + v][node] = val;
+          if (!L.br2) Gs[el][d * 5 + v][vsw<NP>(node)] = val;
           G[(d * 5 + v) * n3] = val;
         }
     }
@@ -540,12 +557,12 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
       if (c % 5 < V0) continue;
       R s;
       if (!L.gauss) {
-        s = Gs[el][c][face_node(n, ls, a, b, is_minus(ls) ? 0 : N)];
+        s = Gs[el][c][vsw<NP>(face_node(n, ls, a, b, is_minus(ls) ? 0 : N))];
       } else {
         const R* Lv = is_minus(ls) ? sb.Lm : sb.Lp;
-        s = Gs[el][c][face_node(n, ls, a, b, 0)] * Lv[0];
+        s = Gs[el][c][vsw<NP>(face_node(n, ls, a, b, 0))] * Lv[0];
 #pragma unroll
-        for (int l = 1; l < n; ++l) s = s + Gs[el][c][face_node(n, ls, a, b, l)] * Lv[l];
+        for (int l = 1; l < n; ++l) s = s + Gs[el][c][vsw<NP>(face_node(n, ls, a, b, l))] * Lv[l];
       }
       if (L.br2) {
         const int d = c / 5, v = c - 5 * d;
@@ -556,41 +573,20 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
   }
 }
 
-// k_bc_face: GetBoundaryFlux_GPU (getboundaryflux.f90:542-838) with the SurfElem factor of
-// FillFlux (fillflux.f90:162-170), thread per face node of the BC sides (a launch of its own, so
-// that the boundary code does not weigh on the registers of k_face)
+// GetBoundaryFlux_GPU (getboundaryflux.f90:542-838) at one face node, without the SurfElem factor:
+// PL the inner face state (momentum pressure in slot 4), g* the inner face gradients (clobbered by the
+// wall projections), ref the side's reference state.  Templated on the arithmetic type, so that the
+// adjoint obtains its local Jacobian by forward-mode dual numbers.
 template <typename R>
-__global__ void __launch_bounds__(256)
-k_bc_face(const R* __restrict__ Pf, const R* __restrict__ Gf, const R* __restrict__ Fgeo, Gas<R> gas, Launch L,
-          int n2, R* __restrict__ Flux) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)L.nBCSides * n2) return;
-  const int side = (int)(t / n2), pq = (int)(t - (long long)side * n2);
-  const int bt = L.bctype[side];
-  const R* ref = static_cast<const R*>(L.bcref) + 6 * L.bcstate[side];
-  const int riemann = L.riemann, split = L.split, parabolic = L.parabolic;
-  const R* pf = Pf + (size_t)side * 6 * n2 + pq;
-  const R* gm = Gf + (size_t)side * 15 * n2 + pq;
-  const R* fg = Fgeo + (size_t)side * 10 * n2 + pq;
-  R* out = Flux + (size_t)side * 5 * n2 + pq;
-  R PL[6];
-#pragma unroll
-  for (int c = 0; c < 6; ++c) PL[c] = pf[c * n2];
-  const R nv[3] = {fg[0], fg[n2], fg[2 * n2]};
-  const R t1[3] = {fg[3 * n2], fg[4 * n2], fg[5 * n2]};
-  const R t2[3] = {fg[6 * n2], fg[7 * n2], fg[8 * n2]};
-  const R se = fg[9 * n2];
-  R F[5];
+__device__ __forceinline__ void bc_face_flux(int bt, const R PL[6], R gx[5], R gy[5], R gz[5], const R nv[3],
+                                             const R t1[3], const R t2[3], const R* ref, const Gas<R>& gas,
+                                             int riemann, int split, int parabolic, R F[5]) {
   R Pm[6], Pb[6];
 #pragma unroll
   for (int c = 0; c < 6; ++c) Pm[c] = PL[c];
   Pm[4] = p_abs(PL[4], gas);
   bc_state(bt, Pm, ref, nv, t1, t2, gas.kappa, gas.R_gas, Pb);
-  R gx[5], gy[5], gz[5], fd[5];
-  if (parabolic) {
-#pragma unroll
-    for (int v = 0; v < 5; ++v) { gx[v] = gm[v * n2]; gy[v] = gm[(5 + v) * n2]; gz[v] = gm[(10 + v) * n2]; }
-  }
+  R fd[5];
   if (bc_riemann_type(bt)) {
     // Riemann solver between the inner state and the boundary state (both via PrimToCons)
     R Uc[5], Ub[5], Ps[6];
@@ -624,6 +620,38 @@ k_bc_face(const R* __restrict__ Pf, const R* __restrict__ Gf, const R* __restric
       for (int v = 0; v < 5; ++v) F[v] = F[v] + fd[v];
     }
   }
+}
+
+// k_bc_face: GetBoundaryFlux_GPU with the SurfElem factor of FillFlux (fillflux.f90:162-170), thread
+// per face node of the BC sides (a launch of its own, so that the boundary code does not weigh on the
+// registers of k_face)
+template <typename R>
+__global__ void __launch_bounds__(256)
+k_bc_face(const R* __restrict__ Pf, const R* __restrict__ Gf, const R* __restrict__ Fgeo, Gas<R> gas, Launch L,
+          int n2, R* __restrict__ Flux) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)L.nBCSides * n2) return;
+  const int side = (int)(t / n2), pq = (int)(t - (long long)side * n2);
+  const int bt = L.bctype[side];
+  const R* ref = static_cast<const R*>(L.bcref) + 6 * L.bcstate[side];
+  const R* pf = Pf + (size_t)side * 6 * n2 + pq;
+  const R* gm = Gf + (size_t)side * 15 * n2 + pq;
+  const R* fg = Fgeo + (size_t)side * 10 * n2 + pq;
+  R* out = Flux + (size_t)side * 5 * n2 + pq;
+  R PL[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) PL[c] = pf[c * n2];
+  const R nv[3] = {fg[0], fg[n2], fg[2 * n2]};
+  const R t1[3] = {fg[3 * n2], fg[4 * n2], fg[5 * n2]};
+  const R t2[3] = {fg[6 * n2], fg[7 * n2], fg[8 * n2]};
+  const R se = fg[9 * n2];
+  R gx[5], gy[5], gz[5];
+  if (L.parabolic) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) { gx[v] = gm[v * n2]; gy[v] = gm[(5 + v) * n2]; gz[v] = gm[(10 + v) * n2]; }
+  }
+  R F[5];
+  bc_face_flux(bt, PL, gx, gy, gz, nv, t1, t2, ref, gas, L.riemann, L.split, L.parabolic, F);
 #pragma unroll
   for (int v = 0; v < 5; ++v) out[v * n2] = F[v] * se;
 }
@@ -685,28 +713,16 @@ k_face(const R* __restrict__ Uf, const R* __restrict__ Pf, const R* __restrict__
 // (surfint.t90:352-586) + VAX_GPU(-1) + ApplyJacobian, and in RK mode the fused
 // VAXPB_OUT_VAXPB_IN stage update (vector.f90:163-183).
 // =====================================================================================
-// Shared-memory position of node i + n(j + nk) in the staging of k_volume.  N=7: the i and j bits
-// are XOR-swizzled with bits of j and k so that the x-, y- and z-line threads of phase B and the
-// node threads hit 32 distinct FP32 banks (two wavefronts per FP64 access); the plain layout gave
-// 8-way (FP32) and 16-way (FP64) conflicts on the x-lines.  An involution that permutes each block
-// of 32 consecutive nodes.
-template <int NP>
-__device__ __forceinline__ int vsw(int node) {
-  if constexpr (NP == 8) {
-    const int kk = (node >> 6) & 3;
-    return node ^ ((((node >> 5) & 1) << 2) | kk | (kk << 3));
-  } else {
-    return node;
-  }
-}
-
 // staging slots per node of k_volume (see there); shared by the kernel and its launch code.  FP32 (mixed
 // form) at N <= 7 also stages the metric terms of the split-form phase (9 slots after its node data),
 // which FP64 reads through L1 so that two blocks fit an SM
 template <int NP, typename R>
 __host__ __device__ constexpr bool vol_metrics_staged(int split) { return sizeof(R) == 4 && split >= 0 && NP <= 8; }
 template <int NP, typename R>
-__host__ __device__ constexpr int vol_stage_slots(int split, int parab) {
+__host__ __device__ constexpr int vol_stage_slots(int split, int parab, int lines = 0) {
+  // lines: the split-form volume term comes precomputed (k_split_lines); the staging holds phase A's
+  // viscous fluxes and phase C's surface sums only
+  if (lines) return parab ? 12 : 5;
   const int base = split < 0 ? 15 : (parab ? 12 : (split == DG_SPLIT_PI ? 6 : 9));
   const int met = vol_metrics_staged<NP, R>(split) ? (split == DG_SPLIT_PI ? 6 : 9) + 9 : 0;
   return base > met ? base : met;
@@ -745,17 +761,19 @@ struct RKArgsT {
 };
 using RKArgs = RKArgsT<double>;
 
-// S: type of the state arrays U, Ut, Ut_tmp (double; Dual<1> for the tangent-linear operator)
-template <int NP, typename R, int SPLIT, int PARAB, typename S = double>
+// S: type of the state arrays U, Ut, Ut_tmp (double; Dual<1> for the tangent-linear operator).
+// LINES = 1 (split form): phase B adds the split volume term Vs computed by k_split_lines instead of
+// evaluating the pair fluxes here.
+template <int NP, typename R, int SPLIT, int PARAB, typename S = double, int LINES = 0>
 __global__ void __launch_bounds__(EPBof<NP>::v * NP * NP * NP)
 k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restrict__ Gvol,
          const R* __restrict__ Met, const R* __restrict__ Flux, const int* __restrict__ E2S, DevBasis<R> basis,
-         Gas<R> gas, Launch L, RKArgsT<S> rk, int rkmode) {
+         Gas<R> gas, Launch L, RKArgsT<S> rk, int rkmode, const R* __restrict__ Vs = nullptr) {
   constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, EPB = EPBof<NP>::v, N = NP - 1;
   // staging slots per node: the flux-form fluxes of phase A (15; split form: the 12 non-zero viscous
   // ones), then the node data of phase B (PI: rho, aux, u, v, w, p; other split forms also m1..m3);
   // the metrics of phase B are read from global memory (L1), so that at N=7 two blocks fit an SM
-  constexpr int NA = vol_stage_slots<NP, R>(SPLIT, PARAB);
+  constexpr int NA = vol_stage_slots<NP, R>(SPLIT, PARAB, LINES);
   constexpr int S_RHO = 0, S_AUX = 1, S_U = 2, S_V = 3, S_W = 4, S_PM = 5, S_M1 = 6, S_M2 = 7, S_M3 = 8;
   constexpr bool MST = vol_metrics_staged<NP, R>(SPLIT);        // metric terms of phase B staged
   constexpr int S_MET = (SPLIT == DG_SPLIT_PI) ? 6 : 9;          // their slots: S_MET + 3*dir + c
@@ -765,7 +783,7 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
   R* A = reinterpret_cast<R*>(smem_raw);             // [EPB][NA][n3]
   R* AccD = A + (size_t)EPB * NA * n3;               // [EPB][NH][3][5][n3]  (split form only)
   load_basis(sb, basis);
-  if constexpr (SPLIT == DG_SPLIT_PI) {
+  if constexpr (SPLIT == DG_SPLIT_PI && !LINES) {
     // PI pair fluxes are evaluated as 8F (see phase B): fold the 1/8 into DVolSurf (exact scaling)
     __syncthreads();
     for (int t = threadIdx.x; t < NP * NP; t += blockDim.x) sb.DVS[t] = sb.DVS[t] * R(0.125);
@@ -853,10 +871,18 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
     }
   }
 
+  // ---- phase B (LINES): the split volume term of k_split_lines
+  if constexpr (SPLIT >= 0 && LINES) {
+    if (active) {
+      const R* vs = Vs + (size_t)e * 5 * n3 + node;
+#pragma unroll
+      for (int v = 0; v < 5; ++v) vacc[v] = vacc[v] + vs[v * n3];
+    }
+  }
   // ---- phase B: split-form flux differencing with pair symmetry, one thread per 1D line.
   // Node a keeps its sum in registers over its pairs (a,b>a); node b's share goes to the line
   // owner's per-direction shared accumulator, so no two threads ever write the same entry.
-  if constexpr (SPLIT >= 0) {
+  if constexpr (SPLIT >= 0 && !LINES) {
     __syncthreads();  // phase A reads of the staging area are complete
     if (active) {
       const S* Un = U + ((size_t)e * n3 + node) * 5;

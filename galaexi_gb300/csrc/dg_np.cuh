@@ -27,8 +27,9 @@ constexpr int NP = GX_NP;
 constexpr int EPB = gx::EPBof<NP>::v;
 constexpr int NT = EPB * NP * NP * NP;  // threads per element block
 
-template <typename R, int SPL, int PAR> constexpr size_t volume_smem() {
-  return sizeof(R) * (size_t)EPB * (gx::vol_stage_slots<NP, R>(SPL, PAR) + (SPL >= 0 ? 15 * gx::vol_line_threads<NP, R>() : 0)) *
+template <typename R, int SPL, int PAR, int LINES = 0> constexpr size_t volume_smem() {
+  return sizeof(R) * (size_t)EPB *
+         (gx::vol_stage_slots<NP, R>(SPL, PAR, LINES) + (SPL >= 0 && !LINES ? 15 * gx::vol_line_threads<NP, R>() : 0)) *
          NP * NP * NP;
 }
 template <typename R> constexpr size_t lift_smem() {
@@ -43,21 +44,27 @@ int smem_limit() {
   return lim;
 }
 
-template <typename R, int SPL, int PAR>
+template <typename R, int SPL, int PAR, int LINES = 0>
 bool vol_fits() {
-  return volume_smem<R, SPL, PAR>() + sizeof(gx::SBasis<NP, R>) <= (size_t)smem_limit();
+  return volume_smem<R, SPL, PAR, LINES>() + sizeof(gx::SBasis<NP, R>) <= (size_t)smem_limit();
 }
 
-template <typename R, int SPL, int PAR, typename S = double>
+template <typename R, int SPL, int PAR, typename S = double, int LINES = 0>
 int cfg_vol() {
-  if (!vol_fits<R, SPL, PAR>()) return DG_OK;  // variant not runnable on this device; rejected at launch
-  GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_volume<NP, R, SPL, PAR, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)volume_smem<R, SPL, PAR>()),
+  if (!vol_fits<R, SPL, PAR, LINES>()) return DG_OK;  // variant not runnable on this device; rejected at launch
+  GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_volume<NP, R, SPL, PAR, S, LINES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)volume_smem<R, SPL, PAR, LINES>()),
               "k_volume shared-memory attribute");
   // the largest shared-memory carve-out, so that two blocks share an SM where their staging fits
-  GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_volume<NP, R, SPL, PAR, S>, cudaFuncAttributePreferredSharedMemoryCarveout,
+  GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_volume<NP, R, SPL, PAR, S, LINES>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                    100),
               "k_volume carve-out attribute");
+  return DG_OK;
+}
+// the line-per-thread split form of the mixed form (k_split_lines + k_volume<..., LINES = 1>)
+template <typename R, int SPL>
+int cfg_lines() {
+  if constexpr (gx::UseLines<NP, R, SPL>::v) return cfg_vol<R, SPL, 0, double, 1>() | cfg_vol<R, SPL, 1, double, 1>();
   return DG_OK;
 }
 
@@ -76,6 +83,7 @@ int configure() {
   if constexpr (NP >= 3) {
     rc |= cfg_vol<R, 0, 0>() | cfg_vol<R, 0, 1>() | cfg_vol<R, 1, 0>() | cfg_vol<R, 1, 1>() | cfg_vol<R, 2, 0>() |
           cfg_vol<R, 2, 1>() | cfg_vol<R, 3, 0>() | cfg_vol<R, 3, 1>() | cfg_vol<R, 4, 0>() | cfg_vol<R, 4, 1>();
+    rc |= cfg_lines<R, 0>() | cfg_lines<R, 3>() | cfg_lines<R, 4>();
   }
   return rc ? DG_ERR_CUDA : DG_OK;
 }
@@ -83,6 +91,28 @@ int configure() {
 template <typename R, int SPL, typename S = double>
 int vol(dg_ctx* ctx, PrecData<R>& P, const S* U, gx::RKArgsT<S> rk, int rkmode, const gx::Gas<R>& gas,
         cudaStream_t st) {
+  if constexpr (SPL >= 0 && gx::UseLines<NP, R, SPL>::v && std::is_same<S, double>::value) {
+    // mixed form: the split volume term by k_split_lines, then k_volume with that term precomputed
+    if (!P.Vs.p) {
+      gxh::set_error("split volume term buffer missing");
+      return DG_ERR_ALLOC;
+    }
+    gx::LineDVS<NP> dvs;
+    const double scale = SPL == DG_SPLIT_PI ? 0.125 : 1.0;
+    for (int t = 0; t < NP * NP; ++t) dvs.d[t] = (float)ctx->B.DVS[t] * (float)scale;
+    const gx::DevBasis<R> b = gxc::dev_basis(P, NP);
+    const gx::Launch L = gxc::make_launch(ctx);
+    gx::k_split_lines<NP, SPL><<<ctx->nElems, 3 * NP * NP, 0, st>>>(P.Pvol.p, P.Met.p, dvs, gas, ctx->nElems, P.Vs.p);
+    ctx->launches++;
+    const int grid = (ctx->nElems + EPB - 1) / EPB;
+    if (ctx->cfg.parabolic)
+      gx::k_volume<NP, R, SPL, 1, S, 1><<<grid, NT, volume_smem<R, SPL, 1, 1>(), st>>>(
+          U, P.Pvol.p, P.Gvol.p, P.Met.p, P.Flux.p, ctx->E2S.p, b, gas, L, rk, rkmode, P.Vs.p);
+    else
+      gx::k_volume<NP, R, SPL, 0, S, 1><<<grid, NT, volume_smem<R, SPL, 0, 1>(), st>>>(
+          U, P.Pvol.p, P.Gvol.p, P.Met.p, P.Flux.p, ctx->E2S.p, b, gas, L, rk, rkmode, P.Vs.p);
+    return DG_OK;
+  }
   if (ctx->cfg.parabolic ? !vol_fits<R, SPL, 1>() : !vol_fits<R, SPL, 0>()) {
     gxh::set_error("this N / precision / form needs more shared memory per block than the device offers");
     return DG_ERR_UNSUPPORTED;
@@ -277,25 +307,42 @@ int adj(dg_ctx* ctx, const double* U, gx::CotSrc cs, int mode, double* Uout, dou
   AL.lambda = c.mu0 * AL.lamc;
   AL.inv_mu = c.mu0 > 0. ? 1. / c.mu0 : 0.;
   AL.kappa = c.kappa; AL.sR = 1. / c.R;
+  AL.nBCSides = ctx->nBCSides; AL.bctype = ctx->bctype.p; AL.bcstate = ctx->bcstate.p; AL.bcref = ctx->bcref_d.p;
   const gx::DevBasis<double> b = gxc::dev_basis(ctx->d, NP);
   const long long nf = (long long)ctx->nSides * NP * NP;
-  const int fgrid = (int)((nf + 127) / 128);
+  const long long nbf = (long long)ctx->nBCSides * NP * NP;  // face nodes of the BC sides (listed first)
+  const int fgrid = (int)((nf - nbf + 127) / 128);
+  const int bgrid = (int)((nbf + 127) / 128);
   const int vgrid = (ctx->nElems + EPB - 1) / EPB;
-  if (gx::riemann_vjp_supported_host(c.riemann, c.split_dg))
+  if (fgrid == 0) {
+    // no connected sides: nothing for ka_face
+  } else if (gx::riemann_vjp_supported_host(c.riemann, c.split_dg))
     gx::ka_face<NP, true><<<fgrid, 128, 0, st>>>(cs, ctx->d.Met.p, ctx->d.Uf.p, ctx->d.Pf.p, ctx->d.Gf.p, ctx->d.Fgeo.p,
                                                  ctx->S2E.p, b, gas, AL, ctx->UfB.p, ctx->GfB.p, ctx->part.p);
   else
     gx::ka_face<NP, false><<<fgrid, 128, 0, st>>>(cs, ctx->d.Met.p, ctx->d.Uf.p, ctx->d.Pf.p, ctx->d.Gf.p, ctx->d.Fgeo.p,
                                                   ctx->S2E.p, b, gas, AL, ctx->UfB.p, ctx->GfB.p, ctx->part.p);
+  if (bgrid > 0) {
+    gx::ka_bc_face<NP><<<bgrid, 128, 0, st>>>(cs, ctx->d.Met.p, ctx->d.Uf.p, ctx->d.Gf.p, ctx->d.Fgeo.p, ctx->S2E.p, b,
+                                              gas, AL, ctx->UfB.p, ctx->GfB.p, ctx->part.p + fgrid + vgrid);
+    ctx->launches++;
+  }
   switch (c.split_dg) {
     case DG_SPLIT_NONE: adj_vol<-1>(ctx, U, cs, AL, ctx->part.p + fgrid, st); break;
     case DG_SPLIT_KG: if constexpr (NP >= 3) adj_vol<3>(ctx, U, cs, AL, ctx->part.p + fgrid, st); break;
     default: if constexpr (NP >= 3) adj_vol<4>(ctx, U, cs, AL, ctx->part.p + fgrid, st); break;
   }
-  gx::k_adj_sum<<<1, 256, 0, st>>>(ctx->part.p, fgrid + vgrid, acc);
+  gx::k_adj_sum<<<1, 256, 0, st>>>(ctx->part.p, fgrid + vgrid + bgrid, acc);
   if (c.parabolic) {
-    gx::ka_jump<<<(int)((nf + 255) / 256), 256, 0, st>>>(ctx->d.Uf.p, ctx->JB.p, AL, NP * NP, ctx->UfB.p);
-    ctx->launches++;
+    if (nf > nbf) {
+      gx::ka_jump<<<(int)((nf - nbf + 255) / 256), 256, 0, st>>>(ctx->d.Uf.p, ctx->JB.p, AL, NP * NP, ctx->UfB.p);
+      ctx->launches++;
+    }
+    if (nbf > 0) {
+      gx::ka_bc_jump<<<(int)((nbf + 255) / 256), 256, 0, st>>>(ctx->d.Uf.p, ctx->JB.p, ctx->d.Fgeo.p, gas, AL, NP * NP,
+                                                              ctx->UfB.p);
+      ctx->launches++;
+    }
   }
   const long long nn = (long long)ctx->nElems * NP * NP * NP;
   gx::ka_final<NP><<<(int)((nn + 255) / 256), 256, 0, st>>>(ctx->UBv.p, ctx->UfB.p, ctx->E2S.p, b, AL, mode, Uout,

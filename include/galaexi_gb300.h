@@ -228,9 +228,10 @@ int dg_kinetic_energy(dg_ctx* ctx, const double* d_U, double* J, double* d_dJdU,
 
 /* ---- tangent-linear and adjoint operators (FP64 form; no counterpart in the reference) ---------
  * Supported: Gauss or Gauss-Lobatto nodes, weak form or split form PI / KG, every Riemann solver,
- * Euler or Navier-Stokes, periodic meshes, no solution filter; the adjoint with BR1 lifting in
- * strong form.  The tangent-linear operator also takes BR1 in weak or conservative form, BR2, and
- * meshes with boundary sides.  Others return DG_ERR_UNSUPPORTED.
+ * Euler or Navier-Stokes, periodic meshes and meshes with boundary sides (every BC type of
+ * dg_set_boundaries), no solution filter; the adjoint with BR1 lifting in strong form.  The
+ * tangent-linear operator also takes BR1 in weak or conservative form and BR2.  Others return
+ * DG_ERR_UNSUPPORTED.
  *
  * dg_rhs_jvp: Ut = R(U) (if d_Ut is not null) and Utdot = dR/dU . Udot + dR/dmu . mu_dot, the exact
  * linearisation of the operator (forward-mode dual numbers through the same kernels).

@@ -268,15 +268,72 @@ def test_gpu_reproduces_cavity_regression():
     assert err <= CAVITY_ATOL, err
 
 
+# the adjoint's forms (BR1 in strong form, non-conservative or conservative; Euler)
+ADJOINT_CONFIGS = [c for c in CONFIGS if "weaklift" not in c[0] and "br2" not in c[0]]
+
+
+def _adjoint_state(m, seed):
+    rng = np.random.default_rng(seed)
+    U0 = flow_state(m, seed)
+    # node noise: keeps the Lax-Friedrichs / Roe wave-speed maxima away from ties, where the operator
+    # has one-sided derivatives only
+    return U0 * (1.0 + 1e-3 * rng.standard_normal(U0.shape)), rng
+
+
 @pytest.mark.gpu
-def test_bc_meshes_rejected_by_adjoint():
+@pytest.mark.parametrize("cname,ckw,nt", ADJOINT_CONFIGS, ids=[c[0] for c in ADJOINT_CONFIGS])
+@pytest.mark.parametrize("mname,path,bcs,N", MESHES, ids=[m[0] for m in MESHES])
+def test_bc_adjoint_dot_product(cname, ckw, nt, mname, path, bcs, N):
+    """The discrete adjoint on meshes with boundary sides (the boundary flux and the lifting ghost
+    state transposed through their local Jacobians) against the tangent-linear operator:
+    <ybar, J v> = <J^T ybar, v> + mubar mu_dot per RHS evaluation, to round-off."""
+    torch = pytest.importorskip("torch")
+    cfg = gx.config(N=N, R=RGAS, kappa=KAPPA, **ckw)
+    m = gx.Mesh.from_hopr(path, N, nt)
+    bnd = m.boundaries(FLOW_REFSTATES, bcs)
+    U0, rng = _adjoint_state(m, zlib.crc32((cname + mname + "adj").encode()))
+    U = torch.from_numpy(U0).cuda()
+    v = torch.from_numpy(rng.standard_normal(U0.shape)).cuda()
+    ybar = torch.from_numpy(rng.standard_normal(U0.shape)).cuda()
+    mu_dot = 0.7 if cfg.parabolic else 0.0
+    op = gx.DG(cfg, m, boundaries=bnd)
+    _, Jv = op.rhs_jvp(U, v, mu_dot)
+    Ub, mub = op.rhs_vjp(U, ybar)
+    op.close()
+    lhs = float((ybar * Jv).sum())
+    rhs = float((Ub * v).sum()) + mub * mu_dot
+    scale = float(ybar.norm() * Jv.norm())
+    assert abs(lhs - rhs) <= 1e-13 * scale, (cname, mname, lhs, rhs, scale)
+
+
+@pytest.mark.gpu
+def test_bc_adjoint_window_dot_product_cavity():
+    """The adjoint of 10 LSERK steps of the cavity regression's operator (isothermal walls, a
+    Dirichlet lid) from a perturbed moving state: <ybar, Udot(t_end)> of the tangent-linear steps
+    equals <Ubar(t0), v> + mubar mu_dot of the reverse sweep to 1e-10."""
     torch = pytest.importorskip("torch")
     m, bnd = cavity_case()
     op = gx.DG(cavity_config(), m, boundaries=bnd)
-    U = torch.from_numpy(cavity_initial(m)).cuda()
-    with pytest.raises(gx.DGError):
-        op.rhs_vjp(U, torch.zeros_like(U))
+    rng = np.random.default_rng(11)
+    U0 = cavity_initial(m)
+    U0[..., 1] = 0.1 * np.sin(m.Elem_xGP[..., 1] * np.pi)  # some x-momentum
+    U0[..., 4] += 0.5 * U0[..., 1] ** 2
+    U0 = torch.from_numpy(U0 * (1.0 + 1e-3 * rng.standard_normal(U0.shape))).cuda()
+    dt, err = op.CalcTimeStep(U0, 0.99, 0.4)
+    assert err == 0
+    nSteps, mu_dot = 10, 0.3
+    v = torch.from_numpy(rng.standard_normal(tuple(U0.shape))).cuda()
+    ybar = torch.from_numpy(rng.standard_normal(tuple(U0.shape))).cuda()
+    U, Ud, K = U0.clone(), v.clone(), torch.zeros_like(U0)
+    op.tlm_steps(dt, U, Ud, K, nSteps=nSteps, mu_dot=mu_dot)
+    Uf, plan = op.adjoint_forward(dt, nSteps, U0, budget_bytes=1 << 32)
+    assert float((Uf - U).abs().max()) <= 1e-13 * float(U.abs().max())
+    Ub = ybar.clone()
+    mub = op.adjoint_reverse(Ub)
     op.close()
+    lhs = float((ybar * Ud).sum())
+    rhs = float((Ub * v).sum()) + mub * mu_dot
+    assert abs(lhs - rhs) <= 1e-10 * abs(lhs), (lhs, rhs)
 
 
 @pytest.mark.gpu
