@@ -115,10 +115,6 @@ int alloc_prec(dg_ctx* ctx, gxc::PrecData<R>& P, const std::vector<double>& met,
   bool ok = P.Met.alloc(nE * 10 * n3) && P.Fgeo.alloc(nS * 10 * n2) && P.Pvol.alloc(nE * 7 * n3) &&
             P.Uf.alloc(2 * nS * 5 * n2) && P.Pf.alloc(2 * nS * 6 * n2) && P.Flux.alloc(nS * 5 * n2);
   if (ok && par) ok = P.Gvol.alloc(nE * 15 * n3) && P.Gf.alloc(2 * nS * 15 * n2);
-  // the mixed split form (SD, KG, PI) at N = 3..7 takes its split volume term from the line kernel
-  const int sp = ctx->cfg.split_dg;
-  if (ok && sizeof(R) == 4 && (sp == DG_SPLIT_SD || sp == DG_SPLIT_KG || sp == DG_SPLIT_PI) && ctx->n >= 4 && ctx->n <= 8)
-    ok = P.Vs.alloc(nE * 5 * n3);
   if (!ok) { set_error("cudaMalloc scratch"); return DG_ERR_ALLOC; }
   std::vector<R> hm(met.size()), hg(fgeo.size());
   for (size_t t = 0; t < met.size(); ++t) hm[t] = (R)met[t];

@@ -36,10 +36,9 @@ template <typename R>
 struct PrecData {
   DBuf<R> basis;  // D, DhatT, DVS (n^2 each), Lm, Lp, Lhm, Lhp (n each)
   DBuf<R> Met, Fgeo, Pvol, Gvol, Uf, Pf, Gf, Flux;
-  DBuf<R> Vs;     // [e][5][n^3] split-form volume term of the line kernel (mixed split form)
   void release() {
     basis.release(); Met.release(); Fgeo.release(); Pvol.release(); Gvol.release();
-    Uf.release(); Pf.release(); Gf.release(); Flux.release(); Vs.release();
+    Uf.release(); Pf.release(); Gf.release(); Flux.release();
   }
 };
 

@@ -22,7 +22,6 @@
 #pragma once
 #include "dg_physics.cuh"
 #include "dg_bc.cuh"
-#include "dg_lines.cuh"
 
 namespace gx {
 
@@ -719,10 +718,7 @@ k_face(const R* __restrict__ Uf, const R* __restrict__ Pf, const R* __restrict__
 template <int NP, typename R>
 __host__ __device__ constexpr bool vol_metrics_staged(int split) { return sizeof(R) == 4 && split >= 0 && NP <= 8; }
 template <int NP, typename R>
-__host__ __device__ constexpr int vol_stage_slots(int split, int parab, int lines = 0) {
-  // lines: the split-form volume term comes precomputed (k_split_lines); the staging holds phase A's
-  // viscous fluxes and phase C's surface sums only
-  if (lines) return parab ? 12 : 5;
+__host__ __device__ constexpr int vol_stage_slots(int split, int parab) {
   const int base = split < 0 ? 15 : (parab ? 12 : (split == DG_SPLIT_PI ? 6 : 9));
   const int met = vol_metrics_staged<NP, R>(split) ? (split == DG_SPLIT_PI ? 6 : 9) + 9 : 0;
   return base > met ? base : met;
@@ -761,19 +757,17 @@ struct RKArgsT {
 };
 using RKArgs = RKArgsT<double>;
 
-// S: type of the state arrays U, Ut, Ut_tmp (double; Dual<1> for the tangent-linear operator).
-// LINES = 1 (split form): phase B adds the split volume term Vs computed by k_split_lines instead of
-// evaluating the pair fluxes here.
-template <int NP, typename R, int SPLIT, int PARAB, typename S = double, int LINES = 0>
+// S: type of the state arrays U, Ut, Ut_tmp (double; Dual<1> for the tangent-linear operator)
+template <int NP, typename R, int SPLIT, int PARAB, typename S = double>
 __global__ void __launch_bounds__(EPBof<NP>::v * NP * NP * NP)
 k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restrict__ Gvol,
          const R* __restrict__ Met, const R* __restrict__ Flux, const int* __restrict__ E2S, DevBasis<R> basis,
-         Gas<R> gas, Launch L, RKArgsT<S> rk, int rkmode, const R* __restrict__ Vs = nullptr) {
+         Gas<R> gas, Launch L, RKArgsT<S> rk, int rkmode) {
   constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, EPB = EPBof<NP>::v, N = NP - 1;
   // staging slots per node: the flux-form fluxes of phase A (15; split form: the 12 non-zero viscous
   // ones), then the node data of phase B (PI: rho, aux, u, v, w, p; other split forms also m1..m3);
   // the metrics of phase B are read from global memory (L1), so that at N=7 two blocks fit an SM
-  constexpr int NA = vol_stage_slots<NP, R>(SPLIT, PARAB, LINES);
+  constexpr int NA = vol_stage_slots<NP, R>(SPLIT, PARAB);
   constexpr int S_RHO = 0, S_AUX = 1, S_U = 2, S_V = 3, S_W = 4, S_PM = 5, S_M1 = 6, S_M2 = 7, S_M3 = 8;
   constexpr bool MST = vol_metrics_staged<NP, R>(SPLIT);        // metric terms of phase B staged
   constexpr int S_MET = (SPLIT == DG_SPLIT_PI) ? 6 : 9;          // their slots: S_MET + 3*dir + c
@@ -783,7 +777,7 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
   R* A = reinterpret_cast<R*>(smem_raw);             // [EPB][NA][n3]
   R* AccD = A + (size_t)EPB * NA * n3;               // [EPB][NH][3][5][n3]  (split form only)
   load_basis(sb, basis);
-  if constexpr (SPLIT == DG_SPLIT_PI && !LINES) {
+  if constexpr (SPLIT == DG_SPLIT_PI) {
     // PI pair fluxes are evaluated as 8F (see phase B): fold the 1/8 into DVolSurf (exact scaling)
     __syncthreads();
     for (int t = threadIdx.x; t < NP * NP; t += blockDim.x) sb.DVS[t] = sb.DVS[t] * R(0.125);
@@ -871,18 +865,10 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
     }
   }
 
-  // ---- phase B (LINES): the split volume term of k_split_lines
-  if constexpr (SPLIT >= 0 && LINES) {
-    if (active) {
-      const R* vs = Vs + (size_t)e * 5 * n3 + node;
-#pragma unroll
-      for (int v = 0; v < 5; ++v) vacc[v] = vacc[v] + vs[v * n3];
-    }
-  }
   // ---- phase B: split-form flux differencing with pair symmetry, one thread per 1D line.
   // Node a keeps its sum in registers over its pairs (a,b>a); node b's share goes to the line
   // owner's per-direction shared accumulator, so no two threads ever write the same entry.
-  if constexpr (SPLIT >= 0 && !LINES) {
+  if constexpr (SPLIT >= 0) {
     __syncthreads();  // phase A reads of the staging area are complete
     if (active) {
       const S* Un = U + ((size_t)e * n3 + node) * 5;
@@ -1171,3 +1157,5 @@ static __global__ void k_check(const double* __restrict__ U, long long nNodes, d
 }
 
 }  // namespace gx
+
+#include "dg_lines.cuh"

@@ -1,17 +1,22 @@
-// Split-form volume integral of the mixed (FP32) form with one thread per 1D line of an element.
+// The volume kernel of the mixed (FP32) split form with one thread per 1D line of an element.
 //
 // VolInt_splitForm (src/dg/volint.f90:211-353, SplitVolumeFlux* of splitflux.f90:145-730) sums, for
-// every node i of a line, DVolSurf(l,i) * F#(U_i, U_l; (M_i + M_l)/2) over the line's nodes l.  In the
-// element-per-block kernel the line's nodes sit in shared memory and every pair costs ~20 shared-memory
-// accesses (the partner's node data, and the read-modify-write of its accumulators), which bounds the
+// every node i of a line, DVolSurf(l,i) * F#(U_i, U_l; (M_i + M_l)/2) over the line's nodes l; the
+// viscous part (VolInt_weakForm_Visc, volint.f90:238-240, with EvalTransformedDiffFlux3D,
+// flux.f90:619-697) adds D_hat^T(l,i) * f_visc(l) along the same lines.  In the element-per-block
+// kernel (k_volume) the line's nodes sit in shared memory and every pair costs ~20 shared-memory
+// accesses (the partner's node data and the read-modify-write of its accumulators), which bounds the
 // FP32 kernel.  Here a thread holds its whole line in registers: the node data (rho, u, v, w, the
 // momentum pressure, the form's auxiliary variable and the line direction's metric terms) and the five
-// accumulators of every node.  All n(n-1)/2 pairs run fully unrolled for the compile-time n with each
-// pair flux evaluated once and added to both nodes, and the DVolSurf coefficients are compile-time
-// indexed kernel parameters (constant-bank operands of the FMAs).  A block is one element's 3 n^2
-// lines; the three directions' sums of a node meet in shared memory (padded so that neither the
-// line-ordered writes nor the node-ordered reads conflict at N = 7) and the node's split volume term
-// is written to Vs[e][5][n^3], which k_volume adds to its viscous volume and surface terms.
+// accumulators of every node.  All n(n-1)/2 pairs run fully unrolled for the compile-time n, each pair
+// flux evaluated once and added to both nodes; then the line direction's contravariant viscous fluxes
+// of its nodes (from the lifted gradients) are contracted with D_hat^T.  DVolSurf and D_hat^T are
+// compile-time indexed kernel parameters (constant-bank operands of the FMAs).  A block is one
+// element's 3 n^2 lines; the three directions' sums of a node meet in shared memory (padded so that
+// neither the line-ordered writes nor the node-ordered reads conflict at N = 7), and the block's
+// threads then finish node by node: the Gauss-Lobatto surface integral of the face fluxes
+// (SurfIntCons, surfint.t90:352-586), -1, the Jacobian and the output or LSERK-W2 stage update
+// (vector.f90:163-183) in FP64.
 // Registers: ~9 n + 5 n values per thread, so the kernel is instantiated for n <= 8 and the forms
 // whose pair flux needs no momenta (SD, KG, PI).
 #pragma once
@@ -19,8 +24,14 @@
 
 namespace gx {
 
-// DVolSurf(l,i) at d[l + NP*i], pre-scaled for the form (PI: 1/8, see the pair flux below)
-template <int NP> struct LineDVS { float d[NP * NP]; };
+// 1D operators of the line kernel: DVolSurf(l,i) at dvs[l + NP*i] (pre-scaled by 1/8 for PI, see
+// below), D_hat^T(l,i) at dht[l + NP*i], and the Gauss-Lobatto surface weights L_hat_minus(0),
+// L_hat_plus(N)
+template <int NP> struct LineBasis {
+  float dvs[NP * NP];
+  float dht[NP * NP];
+  float lhm0, lhpN;
+};
 
 template <int NP> __host__ __device__ constexpr int line_pad(int dir) {
   // row strides of the three directions' result regions: with n = 8 these make the bank of
@@ -37,11 +48,13 @@ template <int NP, typename R, int SPLIT> struct UseLines {
   static constexpr bool v = sizeof(R) == 4 && NP >= 4 && NP <= 8 && LinesForm<SPLIT>::v;
 };
 
-template <int NP, int SPLIT>
+template <int NP, int SPLIT, int PARAB>
 __global__ void __launch_bounds__(3 * NP * NP, 2)
-k_split_lines(const float* __restrict__ Pvol, const float* __restrict__ Met, LineDVS<NP> dvs, Gas<float> gas,
-              int nElems, float* __restrict__ Vs) {
-  constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP;
+k_volume_lines(const double* __restrict__ U, const float* __restrict__ Pvol, const float* __restrict__ Gvol,
+               const float* __restrict__ Met, const float* __restrict__ Flux, const int* __restrict__ E2S,
+               LineBasis<NP> lb, Gas<float> gas, int nElems, int nSides, double* __restrict__ Ut,
+               double* __restrict__ Uio, double* __restrict__ Ut_tmp, double mRKA, double b_dt, int rkmode) {
+  constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, N = NP - 1;
   constexpr int P0 = line_pad<NP>(0), P1 = line_pad<NP>(1), P2 = line_pad<NP>(2);
   constexpr int OFF1 = 5 * n * P0, OFF2 = OFF1 + 5 * n * P1;
   __shared__ float red[line_red_words<NP>()];
@@ -55,61 +68,98 @@ k_split_lines(const float* __restrict__ Pvol, const float* __restrict__ Met, Lin
   else { base = li; stride = n2; }
   const float* P = Pvol + (size_t)e * 7 * n3;
   const float* M = Met + ((size_t)e * 10 + 3 * dir) * n3;
-  // the line's node data
-  float rho[n], u[n], v[n], w[n], pm[n], aux[n], m0[n], m1[n], m2[n];
-#pragma unroll
-  for (int l = 0; l < n; ++l) {
-    const int node = base + l * stride;
-    rho[l] = P[node];
-    u[l] = P[n3 + node];
-    v[l] = P[2 * n3 + node];
-    w[l] = P[3 * n3 + node];
-    const float pmom = P[4 * n3 + node];  // momentum pressure (p' = p - p_ref in the mixed form)
-    const float srho = P[6 * n3 + node];
-    m0[l] = M[node];
-    m1[l] = M[n3 + node];
-    m2[l] = M[2 * n3 + node];
-    const float pabs = p_abs(pmom, gas);
-    const float E = pabs * gas.sKappaM1 + 0.5f * rho[l] * (u[l] * u[l] + v[l] * v[l] + w[l] * w[l]);
-    aux[l] = pair_aux<SPLIT, float>(rho[l], u[l], v[l], w[l], E, pabs, srho);
-    pm[l] = (SPLIT == DG_SPLIT_PI) ? 4.f * pmom : pmom;  // PI: 4p (exact scaling, see below)
-  }
   float acc[n][5];
+  float m0[n], m1[n], m2[n];
+  {
+    // the line's node data
+    float rho[n], u[n], v[n], w[n], pm[n], aux[n];
 #pragma unroll
-  for (int l = 0; l < n; ++l)
+    for (int l = 0; l < n; ++l) {
+      const int node = base + l * stride;
+      rho[l] = P[node];
+      u[l] = P[n3 + node];
+      v[l] = P[2 * n3 + node];
+      w[l] = P[3 * n3 + node];
+      const float pmom = P[4 * n3 + node];  // momentum pressure (p' = p - p_ref in the mixed form)
+      const float srho = P[6 * n3 + node];
+      m0[l] = M[node];
+      m1[l] = M[n3 + node];
+      m2[l] = M[2 * n3 + node];
+      const float pabs = p_abs(pmom, gas);
+      const float E = pabs * gas.sKappaM1 + 0.5f * rho[l] * (u[l] * u[l] + v[l] * v[l] + w[l] * w[l]);
+      aux[l] = pair_aux<SPLIT, float>(rho[l], u[l], v[l], w[l], E, pabs, srho);
+      pm[l] = (SPLIT == DG_SPLIT_PI) ? 4.f * pmom : pmom;  // PI: 4p (exact scaling, see below)
+    }
 #pragma unroll
-    for (int c = 0; c < 5; ++c) acc[l][c] = 0.f;
+    for (int l = 0; l < n; ++l)
 #pragma unroll
-  for (int a = 0; a < n - 1; ++a) {
+      for (int c = 0; c < 5; ++c) acc[l][c] = 0.f;
+    // split form: every pair of the line once, added to both of its nodes
 #pragma unroll
-    for (int b = a + 1; b < n; ++b) {
-      const float Ms0 = m0[a] + m0[b], Ms1 = m1[a] + m1[b], Ms2 = m2[a] + m2[b];
-      float F[5];
-      if constexpr (SPLIT == DG_SPLIT_PI) {
-        // 8 x the PI flux, the density row at 4 x (doubled at the end); DVolSurf carries the 1/8
-        const float rs = rho[a] + rho[b], us = u[a] + u[b], vs = v[a] + v[b], ws = w[a] + w[b];
-        const float ps4 = pm[a] + pm[b];
-        const float Vsum = Ms0 * us + Ms1 * vs + Ms2 * ws;
-        const float q8 = rs * Vsum;
-        F[0] = q8;
-        F[1] = q8 * us + ps4 * Ms0;
-        F[2] = q8 * vs + ps4 * Ms1;
-        F[3] = q8 * ws + ps4 * Ms2;
-        F[4] = q8 * (aux[a] + aux[b]);
-      } else {
-        PairNode<float> A, B;
-        A.rho = rho[a]; A.u = u[a]; A.v = v[a]; A.w = w[a]; A.pm = pm[a]; A.aux = aux[a];
-        B.rho = rho[b]; B.u = u[b]; B.v = v[b]; B.w = w[b]; B.pm = pm[b]; B.aux = aux[b];
-        A.m1 = A.m2 = A.m3 = B.m1 = B.m2 = B.m3 = 0.f;
-        split_pair_flux<SPLIT, float>(A, B, Ms0, Ms1, Ms2, 2.f * gas.pref, F);
-      }
-      const float dba = dvs.d[b + n * a], dab = dvs.d[a + n * b];  // DVolSurf(l=b,i=a), DVolSurf(l=a,i=b)
+    for (int a = 0; a < n - 1; ++a) {
 #pragma unroll
-      for (int c = 0; c < 5; ++c) {
-        acc[a][c] = acc[a][c] + dba * F[c];
-        acc[b][c] = acc[b][c] + dab * F[c];
+      for (int b = a + 1; b < n; ++b) {
+        const float Ms0 = m0[a] + m0[b], Ms1 = m1[a] + m1[b], Ms2 = m2[a] + m2[b];
+        float F[5];
+        if constexpr (SPLIT == DG_SPLIT_PI) {
+          // 8 x the PI flux, the density row at 4 x (doubled at the end); DVolSurf carries the 1/8
+          const float rs = rho[a] + rho[b], us = u[a] + u[b], vs = v[a] + v[b], ws = w[a] + w[b];
+          const float ps4 = pm[a] + pm[b];
+          const float Vsum = Ms0 * us + Ms1 * vs + Ms2 * ws;
+          const float q8 = rs * Vsum;
+          F[0] = q8;
+          F[1] = q8 * us + ps4 * Ms0;
+          F[2] = q8 * vs + ps4 * Ms1;
+          F[3] = q8 * ws + ps4 * Ms2;
+          F[4] = q8 * (aux[a] + aux[b]);
+        } else {
+          PairNode<float> A, B;
+          A.rho = rho[a]; A.u = u[a]; A.v = v[a]; A.w = w[a]; A.pm = pm[a]; A.aux = aux[a];
+          B.rho = rho[b]; B.u = u[b]; B.v = v[b]; B.w = w[b]; B.pm = pm[b]; B.aux = aux[b];
+          A.m1 = A.m2 = A.m3 = B.m1 = B.m2 = B.m3 = 0.f;
+          split_pair_flux<SPLIT, float>(A, B, Ms0, Ms1, Ms2, 2.f * gas.pref, F);
+        }
+        const float dba = lb.dvs[b + n * a], dab = lb.dvs[a + n * b];  // DVolSurf(l=b,i=a), DVolSurf(l=a,i=b)
+#pragma unroll
+        for (int c = 0; c < 5; ++c) {
+          acc[a][c] = acc[a][c] + dba * F[c];
+          acc[b][c] = acc[b][c] + dab * F[c];
+        }
       }
     }
+    if constexpr (SPLIT == DG_SPLIT_PI) {
+#pragma unroll
+      for (int l = 0; l < n; ++l) acc[l][0] = 2.f * acc[l][0];
+    }
+  }
+  if constexpr (PARAB) {
+    // viscous part: the line direction's contravariant viscous fluxes of the line's nodes
+    // (EvalTransformedDiffFlux3D with the direction's metric terms), contracted with D_hat^T
+    const float* G = Gvol + (size_t)e * 15 * n3;
+    float fv[n][4];
+#pragma unroll
+    for (int l = 0; l < n; ++l) {
+      const int node = base + l * stride;
+      float gx[5], gy[5], gz[5];
+      gx[0] = gy[0] = gz[0] = 0.f;  // no flux reads the density gradient
+#pragma unroll
+      for (int c = 1; c < 5; ++c) { gx[c] = G[c * n3 + node]; gy[c] = G[(5 + c) * n3 + node]; gz[c] = G[(10 + c) * n3 + node]; }
+      const float vel[3] = {P[n3 + node], P[2 * n3 + node], P[3 * n3 + node]};
+      float tau[6], tq[3];
+      visc_stress(gx, gy, gz, vel, gas.mu, gas.lambda, tau, tq);
+      fv[l][0] = -m0[l] * tau[0] - m1[l] * tau[3] - m2[l] * tau[4];
+      fv[l][1] = -m0[l] * tau[3] - m1[l] * tau[1] - m2[l] * tau[5];
+      fv[l][2] = -m0[l] * tau[4] - m1[l] * tau[5] - m2[l] * tau[2];
+      fv[l][3] = -m0[l] * tq[0] - m1[l] * tq[1] - m2[l] * tq[2];
+    }
+#pragma unroll
+    for (int i = 0; i < n; ++i)
+#pragma unroll
+      for (int l = 0; l < n; ++l) {
+        const float c = lb.dht[l + n * i];
+#pragma unroll
+        for (int v = 1; v < 5; ++v) acc[i][v] = acc[i][v] + c * fv[l][v - 1];
+      }
   }
   // the three directions' sums of every node meet in shared memory
   float* R0 = red + (dir == 0 ? 0 : (dir == 1 ? OFF1 : OFF2));
@@ -117,16 +167,64 @@ k_split_lines(const float* __restrict__ Pvol, const float* __restrict__ Met, Lin
 #pragma unroll
   for (int l = 0; l < n; ++l)
 #pragma unroll
-    for (int c = 0; c < 5; ++c)
-      R0[(c * n + l) * Pd + li] = (SPLIT == DG_SPLIT_PI && c == 0) ? 2.f * acc[l][c] : acc[l][c];
+    for (int c = 0; c < 5; ++c) R0[(c * n + l) * Pd + li] = acc[l][c];
   __syncthreads();
-  float* out = Vs + (size_t)e * 5 * n3;
-  for (int t = tid; t < 5 * n3; t += blockDim.x) {
-    const int c = t / n3, node = t - c * n3;
+  // node by node: volume sum + Gauss-Lobatto surface integral, -1, Jacobian, output / RK stage
+  const int* e2s = E2S + (size_t)e * 12;
+  for (int node = tid; node < n3; node += blockDim.x) {
     const int i = node % n, j = (node / n) % n, k = node / n2;
-    out[t] = red[(c * n + i) * P0 + j + n * k] + red[OFF1 + (c * n + j) * P1 + i + n * k] +
-             red[OFF2 + (c * n + k) * P2 + i + n * j];
+    float val[5], ut[5];
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      val[c] = red[(c * n + i) * P0 + j + n * k] + red[OFF1 + (c * n + j) * P1 + i + n * k] +
+               red[OFF2 + (c * n + k) * P2 + i + n * j];
+      ut[c] = 0.f;
+    }
+    // the faces this node lies on: (local side, face coordinates a, b)
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+      int ls, a, b;
+      bool on;
+      switch (f) {
+        case 0: ls = L_XI_MINUS; on = i == 0; a = j; b = k; break;
+        case 1: ls = L_XI_PLUS; on = i == N; a = j; b = k; break;
+        case 2: ls = L_ETA_MINUS; on = j == 0; a = i; b = k; break;
+        case 3: ls = L_ETA_PLUS; on = j == N; a = i; b = k; break;
+        case 4: ls = L_ZETA_MINUS; on = k == 0; a = i; b = j; break;
+        default: ls = L_ZETA_PLUS; on = k == N; a = i; b = j; break;
+      }
+      if (!on) continue;
+      const int side = e2s[(ls - 1) * 2 + 0], flip = e2s[(ls - 1) * 2 + 1];
+      int p, q;
+      s2v2_inv(N, a, b, flip, ls, p, q);
+      const float* fx = Flux + (size_t)side * 5 * n2 + p + n * q;
+      const float Lhat = is_minus(ls) ? lb.lhm0 : lb.lhpN;
+      if (flip == 0) {
+#pragma unroll
+        for (int c = 0; c < 5; ++c) ut[c] = ut[c] + fx[c * n2] * Lhat;
+      } else {
+#pragma unroll
+        for (int c = 0; c < 5; ++c) ut[c] = ut[c] - fx[c * n2] * Lhat;
+      }
+    }
+    const float sj = Met[((size_t)e * 10 + 9) * n3 + node];
+    const size_t g = ((size_t)e * n3 + node) * 5;
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      float x = val[c] + ut[c];
+      x = x * -1.f;
+      x = x * sj;
+      if (rkmode == 0) {
+        Ut[g + c] = (double)x;
+      } else {
+        const double utmp = Ut_tmp[g + c] * mRKA + (double)x;
+        Ut_tmp[g + c] = utmp;
+        Uio[g + c] = Uio[g + c] + utmp * b_dt;
+      }
+    }
   }
+  (void)nSides;
+  (void)U;
 }
 
 }  // namespace gx

@@ -27,9 +27,8 @@ constexpr int NP = GX_NP;
 constexpr int EPB = gx::EPBof<NP>::v;
 constexpr int NT = EPB * NP * NP * NP;  // threads per element block
 
-template <typename R, int SPL, int PAR, int LINES = 0> constexpr size_t volume_smem() {
-  return sizeof(R) * (size_t)EPB *
-         (gx::vol_stage_slots<NP, R>(SPL, PAR, LINES) + (SPL >= 0 && !LINES ? 15 * gx::vol_line_threads<NP, R>() : 0)) *
+template <typename R, int SPL, int PAR> constexpr size_t volume_smem() {
+  return sizeof(R) * (size_t)EPB * (gx::vol_stage_slots<NP, R>(SPL, PAR) + (SPL >= 0 ? 15 * gx::vol_line_threads<NP, R>() : 0)) *
          NP * NP * NP;
 }
 template <typename R> constexpr size_t lift_smem() {
@@ -44,27 +43,32 @@ int smem_limit() {
   return lim;
 }
 
-template <typename R, int SPL, int PAR, int LINES = 0>
+template <typename R, int SPL, int PAR>
 bool vol_fits() {
-  return volume_smem<R, SPL, PAR, LINES>() + sizeof(gx::SBasis<NP, R>) <= (size_t)smem_limit();
+  return volume_smem<R, SPL, PAR>() + sizeof(gx::SBasis<NP, R>) <= (size_t)smem_limit();
 }
 
-template <typename R, int SPL, int PAR, typename S = double, int LINES = 0>
+template <typename R, int SPL, int PAR, typename S = double>
 int cfg_vol() {
-  if (!vol_fits<R, SPL, PAR, LINES>()) return DG_OK;  // variant not runnable on this device; rejected at launch
-  GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_volume<NP, R, SPL, PAR, S, LINES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)volume_smem<R, SPL, PAR, LINES>()),
+  if (!vol_fits<R, SPL, PAR>()) return DG_OK;  // variant not runnable on this device; rejected at launch
+  GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_volume<NP, R, SPL, PAR, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)volume_smem<R, SPL, PAR>()),
               "k_volume shared-memory attribute");
   // the largest shared-memory carve-out, so that two blocks share an SM where their staging fits
-  GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_volume<NP, R, SPL, PAR, S, LINES>, cudaFuncAttributePreferredSharedMemoryCarveout,
+  GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_volume<NP, R, SPL, PAR, S>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                    100),
               "k_volume carve-out attribute");
   return DG_OK;
 }
-// the line-per-thread split form of the mixed form (k_split_lines + k_volume<..., LINES = 1>)
+// the line-per-thread volume kernel of the mixed split form
 template <typename R, int SPL>
 int cfg_lines() {
-  if constexpr (gx::UseLines<NP, R, SPL>::v) return cfg_vol<R, SPL, 0, double, 1>() | cfg_vol<R, SPL, 1, double, 1>();
+  if constexpr (gx::UseLines<NP, R, SPL>::v) {
+    GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_volume_lines<NP, SPL, 0>, cudaFuncAttributePreferredSharedMemoryCarveout, 100),
+                "k_volume_lines carve-out attribute");
+    GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_volume_lines<NP, SPL, 1>, cudaFuncAttributePreferredSharedMemoryCarveout, 100),
+                "k_volume_lines carve-out attribute");
+  }
   return DG_OK;
 }
 
@@ -92,25 +96,23 @@ template <typename R, int SPL, typename S = double>
 int vol(dg_ctx* ctx, PrecData<R>& P, const S* U, gx::RKArgsT<S> rk, int rkmode, const gx::Gas<R>& gas,
         cudaStream_t st) {
   if constexpr (SPL >= 0 && gx::UseLines<NP, R, SPL>::v && std::is_same<S, double>::value) {
-    // mixed form: the split volume term by k_split_lines, then k_volume with that term precomputed
-    if (!P.Vs.p) {
-      gxh::set_error("split volume term buffer missing");
-      return DG_ERR_ALLOC;
+    // mixed split form: one thread per 1D line (k_volume_lines)
+    gx::LineBasis<NP> lb;
+    const float scale = SPL == DG_SPLIT_PI ? 0.125f : 1.f;  // PI: the 1/8 of the pair flux (exact scaling)
+    for (int t = 0; t < NP * NP; ++t) {
+      lb.dvs[t] = (float)ctx->B.DVS[t] * scale;
+      lb.dht[t] = (float)ctx->B.DhatT[t];
     }
-    gx::LineDVS<NP> dvs;
-    const double scale = SPL == DG_SPLIT_PI ? 0.125 : 1.0;
-    for (int t = 0; t < NP * NP; ++t) dvs.d[t] = (float)ctx->B.DVS[t] * (float)scale;
-    const gx::DevBasis<R> b = gxc::dev_basis(P, NP);
-    const gx::Launch L = gxc::make_launch(ctx);
-    gx::k_split_lines<NP, SPL><<<ctx->nElems, 3 * NP * NP, 0, st>>>(P.Pvol.p, P.Met.p, dvs, gas, ctx->nElems, P.Vs.p);
-    ctx->launches++;
-    const int grid = (ctx->nElems + EPB - 1) / EPB;
+    lb.lhm0 = (float)ctx->B.Lhm[0];
+    lb.lhpN = (float)ctx->B.Lhp[NP - 1];
     if (ctx->cfg.parabolic)
-      gx::k_volume<NP, R, SPL, 1, S, 1><<<grid, NT, volume_smem<R, SPL, 1, 1>(), st>>>(
-          U, P.Pvol.p, P.Gvol.p, P.Met.p, P.Flux.p, ctx->E2S.p, b, gas, L, rk, rkmode, P.Vs.p);
+      gx::k_volume_lines<NP, SPL, 1><<<ctx->nElems, 3 * NP * NP, 0, st>>>(
+          U, P.Pvol.p, P.Gvol.p, P.Met.p, P.Flux.p, ctx->E2S.p, lb, gas, ctx->nElems, ctx->nSides, rk.Ut, rk.U,
+          rk.Ut_tmp, rk.mRKA, rk.b_dt, rkmode);
     else
-      gx::k_volume<NP, R, SPL, 0, S, 1><<<grid, NT, volume_smem<R, SPL, 0, 1>(), st>>>(
-          U, P.Pvol.p, P.Gvol.p, P.Met.p, P.Flux.p, ctx->E2S.p, b, gas, L, rk, rkmode, P.Vs.p);
+      gx::k_volume_lines<NP, SPL, 0><<<ctx->nElems, 3 * NP * NP, 0, st>>>(
+          U, P.Pvol.p, P.Gvol.p, P.Met.p, P.Flux.p, ctx->E2S.p, lb, gas, ctx->nElems, ctx->nSides, rk.Ut, rk.U,
+          rk.Ut_tmp, rk.mRKA, rk.b_dt, rkmode);
     return DG_OK;
   }
   if (ctx->cfg.parabolic ? !vol_fits<R, SPL, 1>() : !vol_fits<R, SPL, 0>()) {
