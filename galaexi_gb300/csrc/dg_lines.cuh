@@ -228,3 +228,144 @@ k_volume_lines(const double* __restrict__ U, const float* __restrict__ Pvol, con
 }
 
 }  // namespace gx
+
+namespace gx {
+
+// The BR1 lifting of the mixed form (Lifting_BR1, lifting_br1.t90:47-167, strong non-conservative
+// form, Gauss-Lobatto nodes) with one thread per 1D line for the volume part.  The line threads
+// differentiate u, v, w and T along their line (D(i,l) as compile-time indexed kernel parameters);
+// the three directions' derivatives of a node meet in shared memory; the block's threads then finish
+// node by node: the metric transform with the Jacobian (Lifting_VolInt_Nonconservative,
+// lifting_volint.t90:262-328), the surface part of the faces the node lies on (0.5 SurfElem
+// (P_slave - P_master) n L_hat sJ, lifting_fillflux.t90:39-103, 212-256, surfint.t90:591-725), and the
+// gradients and their face traces (ProlongToFaceLifting: on Gauss-Lobatto nodes the node's own value).
+// The density gradient, which no flux reads, is not formed.
+template <int NP> struct LiftBasis {
+  float D[NP * NP];  // D(i,l) at D[i + NP*l]
+  float lhm0, lhpN;
+};
+template <int NP> __host__ __device__ constexpr int lift_red_words() {
+  return 4 * NP * (line_pad<NP>(0) + line_pad<NP>(1) + line_pad<NP>(2));
+}
+template <int NP, typename R> struct UseLiftLines {
+  static constexpr bool v = sizeof(R) == 4 && NP >= 4 && NP <= 8;
+};
+
+template <int NP>
+__global__ void __launch_bounds__(3 * NP * NP, 4)
+k_lift_lines(const float* __restrict__ Pvol, const float* __restrict__ Met, const float* __restrict__ Pf,
+             const float* __restrict__ Fgeo, const int* __restrict__ E2S, LiftBasis<NP> lb, int nElems, int nSides,
+             float* __restrict__ Gvol, float* __restrict__ Gf) {
+  constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, N = NP - 1;
+  constexpr int P0 = line_pad<NP>(0), P1 = line_pad<NP>(1), P2 = line_pad<NP>(2);
+  constexpr int OFF1 = 4 * n * P0, OFF2 = OFF1 + 4 * n * P1;
+  __shared__ float red[lift_red_words<NP>()];
+  const int e = blockIdx.x;
+  if (e >= nElems) return;
+  const int tid = threadIdx.x;
+  {
+    const int dir = tid / n2, li = tid - dir * n2;
+    int base, stride;
+    if (dir == 0) { base = n * li; stride = 1; }
+    else if (dir == 1) { base = (li % n) + n2 * (li / n); stride = n; }
+    else { base = li; stride = n2; }
+    const float* P = Pvol + (size_t)e * 7 * n3;
+    const int slot[4] = {1, 2, 3, 5};  // u, v, w, T
+    float x[4][n];
+#pragma unroll
+    for (int l = 0; l < n; ++l)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) x[c][l] = P[slot[c] * n3 + base + l * stride];
+    float* R0 = red + (dir == 0 ? 0 : (dir == 1 ? OFF1 : OFF2));
+    const int Pd = dir == 0 ? P0 : (dir == 1 ? P1 : P2);
+#pragma unroll
+    for (int i = 0; i < n; ++i)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        float s = 0.f;
+#pragma unroll
+        for (int l = 0; l < n; ++l) s = s + lb.D[i + n * l] * x[c][l];
+        R0[(c * n + i) * Pd + li] = s;
+      }
+  }
+  __syncthreads();
+  const int* e2s = E2S + (size_t)e * 12;
+  const int liftc[4] = {1, 2, 3, 5};
+  for (int node = tid; node < n3; node += blockDim.x) {
+    const int i = node % n, j = (node / n) % n, k = node / n2;
+    const float* M = Met + (size_t)e * 10 * n3 + node;
+    const float sj = M[9 * n3];
+    const float mf[3] = {sj * M[0], sj * M[n3], sj * M[2 * n3]}, mg[3] = {sj * M[3 * n3], sj * M[4 * n3], sj * M[5 * n3]},
+                mh[3] = {sj * M[6 * n3], sj * M[7 * n3], sj * M[8 * n3]};
+    float g[3][4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const float gxi = red[(c * n + i) * P0 + j + n * k];
+      const float geta = red[OFF1 + (c * n + j) * P1 + i + n * k];
+      const float gzeta = red[OFF2 + (c * n + k) * P2 + i + n * j];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) g[d][c] = mf[d] * gxi + mg[d] * geta + mh[d] * gzeta;
+    }
+    // surface part of the faces the node lies on, one normal direction after the other
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+      int ls, a, b;
+      bool on;
+      switch (f) {
+        case 0: ls = L_XI_MINUS; on = i == 0; a = j; b = k; break;
+        case 1: ls = L_XI_PLUS; on = i == N; a = j; b = k; break;
+        case 2: ls = L_ETA_MINUS; on = j == 0; a = i; b = k; break;
+        case 3: ls = L_ETA_PLUS; on = j == N; a = i; b = k; break;
+        case 4: ls = L_ZETA_MINUS; on = k == 0; a = i; b = j; break;
+        default: ls = L_ZETA_PLUS; on = k == N; a = i; b = j; break;
+      }
+      if (!on) continue;
+      const int side = e2s[(ls - 1) * 2 + 0], flip = e2s[(ls - 1) * 2 + 1];
+      int p, q;
+      s2v2_inv(N, a, b, flip, ls, p, q);
+      const int pq = p + n * q;
+      const float* pm = Pf + (size_t)side * 6 * n2 + pq;
+      const float* ps = Pf + ((size_t)nSides + side) * 6 * n2 + pq;
+      const float* fg = Fgeo + (size_t)side * 10 * n2 + pq;
+      const float Lhat = is_minus(ls) ? lb.lhm0 : lb.lhpN;
+      const float wgt = Lhat * 0.5f * fg[9 * n2] * sj;
+      const float nvv[3] = {wgt * fg[0], wgt * fg[n2], wgt * fg[2 * n2]};
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const float fl = -pm[liftc[c] * n2] + ps[liftc[c] * n2];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) g[d][c] = g[d][c] + fl * nvv[d];
+      }
+    }
+    float* G = Gvol + (size_t)e * 15 * n3 + node;
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) G[(d * 5 + 1 + c) * n3] = g[d][c];
+    // face traces: on Gauss-Lobatto nodes the node's own gradient
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+      int ls, a, b;
+      bool on;
+      switch (f) {
+        case 0: ls = L_XI_MINUS; on = i == 0; a = j; b = k; break;
+        case 1: ls = L_XI_PLUS; on = i == N; a = j; b = k; break;
+        case 2: ls = L_ETA_MINUS; on = j == 0; a = i; b = k; break;
+        case 3: ls = L_ETA_PLUS; on = j == N; a = i; b = k; break;
+        case 4: ls = L_ZETA_MINUS; on = k == 0; a = i; b = j; break;
+        default: ls = L_ZETA_PLUS; on = k == N; a = i; b = j; break;
+      }
+      if (!on) continue;
+      const int side = e2s[(ls - 1) * 2 + 0], flip = e2s[(ls - 1) * 2 + 1];
+      int p, q;
+      s2v2_inv(N, a, b, flip, ls, p, q);
+      float* gf = Gf + (((size_t)(flip == 0 ? 0 : 1) * nSides + side) * 15) * n2 + p + n * q;
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) gf[(d * 5 + 1 + c) * n2] = g[d][c];
+    }
+  }
+}
+
+}  // namespace gx

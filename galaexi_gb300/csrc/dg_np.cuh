@@ -150,8 +150,22 @@ void rhs_front(dg_ctx* ctx, PrecData<R>& P, const S* U, const gx::Gas<R>& gas, c
   }
   if (ev) cudaEventRecord(ev[1], st);
   if (ctx->cfg.parabolic) {
-    gx::k_lift<NP, R, V0><<<grid, NT, lift_smem<R>(), st>>>(P.Pvol.p, P.Met.p, P.Pf.p, P.Fgeo.p, ctx->E2S.p, b, L,
-                                                            P.Gvol.p, P.Gf.p);
+    bool lines = false;
+    if constexpr (gx::UseLiftLines<NP, R>::v && V0 == 1 && std::is_same<S, double>::value) {
+      // mixed form, Gauss-Lobatto BR1 in strong non-conservative form: one thread per 1D line
+      if (!L.gauss && !L.br2 && L.lift_mode == 0) {
+        gx::LiftBasis<NP> lb;
+        for (int t = 0; t < NP * NP; ++t) lb.D[t] = (float)ctx->B.D[t];
+        lb.lhm0 = (float)ctx->B.Lhm[0];
+        lb.lhpN = (float)ctx->B.Lhp[NP - 1];
+        gx::k_lift_lines<NP><<<ctx->nElems, 3 * NP * NP, 0, st>>>(P.Pvol.p, P.Met.p, P.Pf.p, P.Fgeo.p, ctx->E2S.p, lb,
+                                                                  ctx->nElems, ctx->nSides, P.Gvol.p, P.Gf.p);
+        lines = true;
+      }
+    }
+    if (!lines)
+      gx::k_lift<NP, R, V0><<<grid, NT, lift_smem<R>(), st>>>(P.Pvol.p, P.Met.p, P.Pf.p, P.Fgeo.p, ctx->E2S.p, b, L,
+                                                              P.Gvol.p, P.Gf.p);
     ctx->launches++;
   }
   if (ev) cudaEventRecord(ev[2], st);
