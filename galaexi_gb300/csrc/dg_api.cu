@@ -436,7 +436,8 @@ int dg_ctx_create(const dg_config* cfg, dg_ctx** out) {
   int rc = upload_basis(ctx, ctx->d);
   if (rc == DG_OK && cfg->precision == DG_PRECISION_MIXED) rc = upload_basis(ctx, ctx->f);
   if (rc == DG_OK) rc = (cfg->precision == DG_PRECISION_FP64) ? T->configure_d() : T->configure_f();
-  if (rc == DG_OK && !(ctx->red.alloc(2) && ctx->bad.alloc(1))) { set_error("cudaMalloc"); rc = DG_ERR_ALLOC; }
+  if (rc == DG_OK && !(ctx->red.alloc(2) && ctx->bad.alloc(1) && ctx->kerr.alloc(1))) { set_error("cudaMalloc"); rc = DG_ERR_ALLOC; }
+  if (rc == DG_OK && cudaMemset(ctx->kerr.p, 0, sizeof(int)) != cudaSuccess) { set_error("clear error flag"); rc = DG_ERR_CUDA; }
   if (rc == DG_OK && !fmat.empty()) {
     if (!ctx->filt.alloc(fmat.size())) { set_error("cudaMalloc filter"); rc = DG_ERR_ALLOC; }
     else if (cudaMemcpy(ctx->filt.p, fmat.data(), fmat.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
@@ -460,6 +461,7 @@ int dg_ctx_destroy(dg_ctx* ctx) {
   ctx->E2S.release();
   ctx->red.release();
   ctx->bad.release();
+  ctx->kerr.release();
   ctx->S2E.release(); ctx->wq.release();
   ctx->bctype.release(); ctx->bcstate.release(); ctx->bcref_d.release(); ctx->bcref_f.release(); ctx->bcref_t.release();
   ctx->t.release(); ctx->Ud.release(); ctx->Utd.release();
@@ -697,6 +699,17 @@ int dg_lserk_step(dg_ctx* ctx, double t, double dt, double* d_U, double* d_Ut_tm
   return dg_lserk_steps(ctx, t, dt, 1, d_U, d_Ut_tmp, stream);
 }
 
+// the error flag of the kernels' bounded waits (read after the stream has been synchronised)
+static int kernel_wait_status(dg_ctx* ctx, cudaStream_t st) {
+  int f = 0;
+  CUDA_TRY(cudaMemcpyAsync(&f, ctx->kerr.p, sizeof(int), cudaMemcpyDeviceToHost, st), "read error flag");
+  CUDA_TRY(cudaStreamSynchronize(st), "sync error flag");
+  if (!f) return DG_OK;
+  CUDA_TRY(cudaMemsetAsync(ctx->kerr.p, 0, sizeof(int), st), "clear error flag");
+  set_error("a kernel's wait for its bulk copies into shared memory ran out; results since the last check are invalid");
+  return DG_ERR_TIMEOUT;
+}
+
 int dg_calc_timestep(dg_ctx* ctx, const double* d_U, double cfl_scale, double dfl_scale, double* dt_out, void* stream) {
   if (int rc = check_ctx(ctx, true)) return rc;
   if (!d_U || !dt_out) { set_error("dg_calc_timestep: null argument"); return DG_ERR_ARG; }
@@ -716,6 +729,7 @@ int dg_calc_timestep(dg_ctx* ctx, const double* d_U, double cfl_scale, double df
   CUDA_TRY(cudaMemcpyAsync(&bad, ctx->bad.p, sizeof(bad), cudaMemcpyDeviceToHost, st), "read flag");
   CUDA_TRY(cudaStreamSynchronize(st), "sync dt");
   *dt_out = h[0] < h[1] ? h[0] : h[1];
+  if (int rc = kernel_wait_status(ctx, st)) return rc;
   if (bad) { set_error("state holds NaN/Inf or non-positive density/pressure"); return DG_ERR_NAN; }
   return DG_OK;
 }
@@ -735,6 +749,7 @@ int dg_check_state(dg_ctx* ctx, const double* d_U, long long* bad_count, void* s
   CUDA_TRY(cudaMemcpyAsync(&bad, ctx->bad.p, sizeof(bad), cudaMemcpyDeviceToHost, st), "read flag");
   CUDA_TRY(cudaStreamSynchronize(st), "sync check");
   *bad_count = (long long)bad;
+  if (int rc = kernel_wait_status(ctx, st)) return rc;
   return bad ? DG_ERR_NAN : DG_OK;
 }
 

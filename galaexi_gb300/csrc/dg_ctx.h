@@ -110,6 +110,7 @@ struct dg_ctx {
   gxc::DBuf<int> E2S;      // [e][6][2]: 0-based side, flip
   gxc::DBuf<double> red;   // dt reduction result (2)
   gxc::DBuf<unsigned long long> bad;
+  gxc::DBuf<int> kerr;     // set by a kernel whose bounded wait ran out (read by the synchronising calls)
   long long launches = 0;
   gxc::DBuf<int> S2E;      // [side][5]: master elem, master local side, slave elem, slave local side, flip (0-based)
   gxc::DBuf<double> wq;    // 1D quadrature weights (n)

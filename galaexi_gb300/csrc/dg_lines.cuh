@@ -1,35 +1,55 @@
-// The volume kernel of the mixed (FP32) split form with one thread per 1D line of an element.
+// Kernels of the mixed (FP32) form with one thread per 1D line of an element.
 //
-// VolInt_splitForm (src/dg/volint.f90:211-353, SplitVolumeFlux* of splitflux.f90:145-730) sums, for
-// every node i of a line, DVolSurf(l,i) * F#(U_i, U_l; (M_i + M_l)/2) over the line's nodes l; the
-// viscous part (VolInt_weakForm_Visc, volint.f90:238-240, with EvalTransformedDiffFlux3D,
-// flux.f90:619-697) adds D_hat^T(l,i) * f_visc(l) along the same lines.  In the element-per-block
-// kernel (k_volume) the line's nodes sit in shared memory and every pair costs ~20 shared-memory
-// accesses (the partner's node data and the read-modify-write of its accumulators), which bounds the
-// FP32 kernel.  Here a thread holds its whole line in registers: the node data (rho, u, v, w, the
-// momentum pressure, the form's auxiliary variable and the line direction's metric terms) and the five
-// accumulators of every node.  All n(n-1)/2 pairs run fully unrolled for the compile-time n, each pair
-// flux evaluated once and added to both nodes; then the line direction's contravariant viscous fluxes
-// of its nodes (from the lifted gradients) are contracted with D_hat^T.  DVolSurf and D_hat^T are
-// compile-time indexed kernel parameters (constant-bank operands of the FMAs).  A block is one
-// element's 3 n^2 lines; the three directions' sums of a node meet in shared memory (padded so that
-// neither the line-ordered writes nor the node-ordered reads conflict at N = 7), and the block's
-// threads then finish node by node: the Gauss-Lobatto surface integral of the face fluxes
+// k_volume_lines: the volume kernel of the split form.  VolInt_splitForm (src/dg/volint.f90:211-353,
+// SplitVolumeFlux* of splitflux.f90:145-730) sums, for every node i of a line, DVolSurf(l,i) *
+// F#(U_i, U_l; (M_i + M_l)/2) over the line's nodes l; the viscous part (VolInt_weakForm_Visc,
+// volint.f90:238-240, with EvalTransformedDiffFlux3D, flux.f90:619-697) adds D_hat^T(l,i) * f_visc(l)
+// along the same lines.  In the element-per-block kernel (k_volume) the line's nodes sit in shared
+// memory and every pair costs ~20 shared-memory accesses (the partner's node data and the
+// read-modify-write of its accumulators), which bounds the FP32 kernel.  Here a thread holds its whole
+// line in registers: the node data (rho, u, v, w, the momentum pressure, the form's auxiliary variable
+// and the line direction's metric terms) and the five accumulators of every node.  All n(n-1)/2 pairs
+// run fully unrolled for the compile-time n, each pair flux evaluated once and added to both nodes;
+// then the line direction's contravariant viscous fluxes of its nodes (from the lifted gradients) are
+// contracted with D_hat^T.  DVolSurf and D_hat^T are compile-time indexed kernel parameters
+// (constant-bank operands of the FMAs).  The three directions' sums of a node meet in shared memory
+// (padded so that neither the line-ordered writes nor the node-ordered reads conflict at N = 7), and
+// the block's threads then finish node by node: the Gauss-Lobatto surface integral of the face fluxes
 // (SurfIntCons, surfint.t90:352-586), -1, the Jacobian and the output or LSERK-W2 stage update
 // (vector.f90:163-183) in FP64.
-// Registers: ~9 n + 5 n values per thread, so the kernel is instantiated for n <= 8 and the forms
-// whose pair flux needs no momenta (SD, KG, PI).
+//
+// k_lift_lines: the BR1 lifting (Lifting_BR1, lifting_br1.t90:47-167, strong non-conservative form,
+// Gauss-Lobatto nodes).  The line threads differentiate u, v, w and T along their line (D(i,l) as
+// kernel parameters); the node-by-node finish applies the metric terms and the Jacobian
+// (Lifting_VolInt_Nonconservative, lifting_volint.t90:262-328), adds the surface part of the faces the
+// node lies on (0.5 SurfElem (P_slave - P_master) n L_hat sJ, lifting_fillflux.t90:39-103, 212-256,
+// surfint.t90:591-725) and writes the gradients and their face traces (ProlongToFaceLifting: on
+// Gauss-Lobatto nodes the node's own value).  The density gradient, which no flux reads, is not formed.
+//
+// A block is one element's 3 n^2 lines.  Its input slabs (the element's primitives, metric terms,
+// lifted gradients and FP64 state / RK register: each one contiguous in memory) are copied into shared
+// memory by the tensor memory accelerator (cp.async.bulk, dg_tma.cuh) at the start of the block, all
+// at once, so that the few warps of a block wait once for their data instead of once per dependent
+// load; where a slab is not 16-byte aligned (N = 4, 6) the threads copy it.
+// Registers: ~9 n + 5 n values per thread, so the kernels are instantiated for n <= 8, the volume
+// kernel for the forms whose pair flux needs no momenta (SD, KG, PI).
 #pragma once
 #include "dg_physics.cuh"
+#include "dg_tma.cuh"
 
 namespace gx {
 
-// 1D operators of the line kernel: DVolSurf(l,i) at dvs[l + NP*i] (pre-scaled by 1/8 for PI, see
-// below), D_hat^T(l,i) at dht[l + NP*i], and the Gauss-Lobatto surface weights L_hat_minus(0),
+// 1D operators of the volume line kernel: DVolSurf(l,i) at dvs[l + NP*i] (pre-scaled by 1/8 for PI,
+// see below), D_hat^T(l,i) at dht[l + NP*i], and the Gauss-Lobatto surface weights L_hat_minus(0),
 // L_hat_plus(N)
 template <int NP> struct LineBasis {
   float dvs[NP * NP];
   float dht[NP * NP];
+  float lhm0, lhpN;
+};
+// 1D operators of the lifting line kernel: D(i,l) at D[i + NP*l]
+template <int NP> struct LiftBasis {
+  float D[NP * NP];
   float lhm0, lhpN;
 };
 
@@ -38,8 +58,8 @@ template <int NP> __host__ __device__ constexpr int line_pad(int dir) {
   // (row l, line) distinct for the 32 lines a warp writes and for the 32 nodes a warp reads
   return NP * NP + (dir == 0 ? 4 : (dir == 1 ? 8 : 0));
 }
-template <int NP> __host__ __device__ constexpr int line_red_words() {
-  return 5 * NP * (line_pad<NP>(0) + line_pad<NP>(1) + line_pad<NP>(2));
+template <int NP> __host__ __device__ constexpr int line_red_words(int vars) {
+  return vars * NP * (line_pad<NP>(0) + line_pad<NP>(1) + line_pad<NP>(2));
 }
 template <int SPLIT> struct LinesForm {
   static constexpr bool v = SPLIT == DG_SPLIT_PI || SPLIT == DG_SPLIT_KG || SPLIT == DG_SPLIT_SD;
@@ -47,27 +67,97 @@ template <int SPLIT> struct LinesForm {
 template <int NP, typename R, int SPLIT> struct UseLines {
   static constexpr bool v = sizeof(R) == 4 && NP >= 4 && NP <= 8 && LinesForm<SPLIT>::v;
 };
+template <int NP, typename R> struct UseLiftLines {
+  static constexpr bool v = sizeof(R) == 4 && NP >= 4 && NP <= 8;
+};
+
+__host__ __device__ constexpr size_t round16(size_t b) { return (b + 15) / 16 * 16; }
+
+// shared-memory layout of k_volume_lines (bytes): region A holds the lifted gradients, later the three
+// directions' sums; then the primitives, the metric terms, the FP64 state and RK register
+template <int NP> struct VolLinesSmem {
+  static constexpr size_t n3 = (size_t)NP * NP * NP;
+  static constexpr size_t A = round16(15 * n3 * 4 > line_red_words<NP>(5) * 4 ? 15 * n3 * 4 : line_red_words<NP>(5) * 4);
+  static constexpr size_t P = A, M = P + round16(7 * n3 * 4), U = M + round16(10 * n3 * 4), T = U + round16(5 * n3 * 8);
+  static constexpr size_t bytes = T + round16(5 * n3 * 8);
+};
+template <int NP> struct LiftLinesSmem {
+  static constexpr size_t n3 = (size_t)NP * NP * NP;
+  static constexpr size_t A = round16(line_red_words<NP>(4) * 4);
+  static constexpr size_t P = A, M = P + round16(7 * n3 * 4);
+  static constexpr size_t bytes = M + round16(10 * n3 * 4);
+};
+
+// copy `bytes` from src to dst in shared memory: the issuing thread queues a bulk copy where src, dst
+// and the size are 16-byte aligned (returns the bytes queued), else the block's threads copy words
+__device__ __forceinline__ unsigned stage_slab(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+  if (bulk_ok(src, dst, bytes)) {
+    if (threadIdx.x == 0) bulk_g2s(dst, src, bytes, bar);
+    return bytes;
+  }
+  const unsigned* s = static_cast<const unsigned*>(src);
+  unsigned* d = static_cast<unsigned*>(dst);
+  for (unsigned t = threadIdx.x; t < bytes / 4; t += blockDim.x) d[t] = s[t];
+  return 0;
+}
+
+// the faces a node (i,j,k) lies on, in normal-direction order: local side and face coordinates
+template <int NP>
+__device__ __forceinline__ bool node_face(int f, int i, int j, int k, int& ls, int& a, int& b) {
+  constexpr int N = NP - 1;
+  switch (f) {
+    case 0: ls = L_XI_MINUS; a = j; b = k; return i == 0;
+    case 1: ls = L_XI_PLUS; a = j; b = k; return i == N;
+    case 2: ls = L_ETA_MINUS; a = i; b = k; return j == 0;
+    case 3: ls = L_ETA_PLUS; a = i; b = k; return j == N;
+    case 4: ls = L_ZETA_MINUS; a = i; b = j; return k == 0;
+    default: ls = L_ZETA_PLUS; a = i; b = j; return k == N;
+  }
+}
 
 template <int NP, int SPLIT, int PARAB>
 __global__ void __launch_bounds__(3 * NP * NP, 2)
 k_volume_lines(const double* __restrict__ U, const float* __restrict__ Pvol, const float* __restrict__ Gvol,
                const float* __restrict__ Met, const float* __restrict__ Flux, const int* __restrict__ E2S,
-               LineBasis<NP> lb, Gas<float> gas, int nElems, int nSides, double* __restrict__ Ut,
-               double* __restrict__ Uio, double* __restrict__ Ut_tmp, double mRKA, double b_dt, int rkmode) {
+               LineBasis<NP> lb, Gas<float> gas, int nElems, double* __restrict__ Ut, double* __restrict__ Uio,
+               double* __restrict__ Ut_tmp, double mRKA, double b_dt, int rkmode, int* __restrict__ err) {
   constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, N = NP - 1;
   constexpr int P0 = line_pad<NP>(0), P1 = line_pad<NP>(1), P2 = line_pad<NP>(2);
   constexpr int OFF1 = 5 * n * P0, OFF2 = OFF1 + 5 * n * P1;
-  __shared__ float red[line_red_words<NP>()];
+  using L = VolLinesSmem<NP>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ uint64_t bar;
+  float* const red = reinterpret_cast<float*>(smem_raw);            // after the line phase
+  float* const Gs = reinterpret_cast<float*>(smem_raw);             // [15][n3] during the line phase
+  float* const Ps = reinterpret_cast<float*>(smem_raw + L::P);      // [7][n3]
+  float* const Ms = reinterpret_cast<float*>(smem_raw + L::M);      // [10][n3]
+  double* const Us = reinterpret_cast<double*>(smem_raw + L::U);    // [n3][5]
+  double* const Ts = reinterpret_cast<double*>(smem_raw + L::T);    // [n3][5]
   const int e = blockIdx.x;
   if (e >= nElems) return;
   const int tid = threadIdx.x;
+  // ---- the element's slabs into shared memory
+  if (tid == 0) mbar_init(&bar);
+  __syncthreads();
+  {
+    unsigned tx = 0;
+    tx += stage_slab(Ps, Pvol + (size_t)e * 7 * n3, 7 * n3 * 4, &bar);
+    tx += stage_slab(Ms, Met + (size_t)e * 10 * n3, 10 * n3 * 4, &bar);
+    if (PARAB) tx += stage_slab(Gs, Gvol + (size_t)e * 15 * n3, 15 * n3 * 4, &bar);
+    if (rkmode) {
+      tx += stage_slab(Us, Uio + (size_t)e * 5 * n3, 5 * n3 * 8, &bar);
+      tx += stage_slab(Ts, Ut_tmp + (size_t)e * 5 * n3, 5 * n3 * 8, &bar);
+    }
+    if (tid == 0) mbar_arrive_expect(&bar, tx);
+  }
+  __syncthreads();  // the threads' own copies
+  if (__syncthreads_or(!mbar_wait(&bar, 0, err))) return;  // the bulk copies did not complete in time
   const int dir = tid / n2, li = tid - dir * n2;
   int base, stride;
   if (dir == 0) { base = n * li; stride = 1; }
   else if (dir == 1) { base = (li % n) + n2 * (li / n); stride = n; }
   else { base = li; stride = n2; }
-  const float* P = Pvol + (size_t)e * 7 * n3;
-  const float* M = Met + ((size_t)e * 10 + 3 * dir) * n3;
+  const float* M = Ms + 3 * dir * n3;
   float acc[n][5];
   float m0[n], m1[n], m2[n];
   {
@@ -76,12 +166,12 @@ k_volume_lines(const double* __restrict__ U, const float* __restrict__ Pvol, con
 #pragma unroll
     for (int l = 0; l < n; ++l) {
       const int node = base + l * stride;
-      rho[l] = P[node];
-      u[l] = P[n3 + node];
-      v[l] = P[2 * n3 + node];
-      w[l] = P[3 * n3 + node];
-      const float pmom = P[4 * n3 + node];  // momentum pressure (p' = p - p_ref in the mixed form)
-      const float srho = P[6 * n3 + node];
+      rho[l] = Ps[node];
+      u[l] = Ps[n3 + node];
+      v[l] = Ps[2 * n3 + node];
+      w[l] = Ps[3 * n3 + node];
+      const float pmom = Ps[4 * n3 + node];  // momentum pressure (p' = p - p_ref in the mixed form)
+      const float srho = Ps[6 * n3 + node];
       m0[l] = M[node];
       m1[l] = M[n3 + node];
       m2[l] = M[2 * n3 + node];
@@ -135,7 +225,6 @@ k_volume_lines(const double* __restrict__ U, const float* __restrict__ Pvol, con
   if constexpr (PARAB) {
     // viscous part: the line direction's contravariant viscous fluxes of the line's nodes
     // (EvalTransformedDiffFlux3D with the direction's metric terms), contracted with D_hat^T
-    const float* G = Gvol + (size_t)e * 15 * n3;
     float fv[n][4];
 #pragma unroll
     for (int l = 0; l < n; ++l) {
@@ -143,8 +232,8 @@ k_volume_lines(const double* __restrict__ U, const float* __restrict__ Pvol, con
       float gx[5], gy[5], gz[5];
       gx[0] = gy[0] = gz[0] = 0.f;  // no flux reads the density gradient
 #pragma unroll
-      for (int c = 1; c < 5; ++c) { gx[c] = G[c * n3 + node]; gy[c] = G[(5 + c) * n3 + node]; gz[c] = G[(10 + c) * n3 + node]; }
-      const float vel[3] = {P[n3 + node], P[2 * n3 + node], P[3 * n3 + node]};
+      for (int c = 1; c < 5; ++c) { gx[c] = Gs[c * n3 + node]; gy[c] = Gs[(5 + c) * n3 + node]; gz[c] = Gs[(10 + c) * n3 + node]; }
+      const float vel[3] = {Ps[n3 + node], Ps[2 * n3 + node], Ps[3 * n3 + node]};
       float tau[6], tq[3];
       visc_stress(gx, gy, gz, vel, gas.mu, gas.lambda, tau, tq);
       fv[l][0] = -m0[l] * tau[0] - m1[l] * tau[3] - m2[l] * tau[4];
@@ -160,6 +249,7 @@ k_volume_lines(const double* __restrict__ U, const float* __restrict__ Pvol, con
 #pragma unroll
         for (int v = 1; v < 5; ++v) acc[i][v] = acc[i][v] + c * fv[l][v - 1];
       }
+    __syncthreads();  // every read of the gradients, which the sums overwrite
   }
   // the three directions' sums of every node meet in shared memory
   float* R0 = red + (dir == 0 ? 0 : (dir == 1 ? OFF1 : OFF2));
@@ -180,20 +270,10 @@ k_volume_lines(const double* __restrict__ U, const float* __restrict__ Pvol, con
                red[OFF2 + (c * n + k) * P2 + i + n * j];
       ut[c] = 0.f;
     }
-    // the faces this node lies on: (local side, face coordinates a, b)
 #pragma unroll
     for (int f = 0; f < 6; ++f) {
       int ls, a, b;
-      bool on;
-      switch (f) {
-        case 0: ls = L_XI_MINUS; on = i == 0; a = j; b = k; break;
-        case 1: ls = L_XI_PLUS; on = i == N; a = j; b = k; break;
-        case 2: ls = L_ETA_MINUS; on = j == 0; a = i; b = k; break;
-        case 3: ls = L_ETA_PLUS; on = j == N; a = i; b = k; break;
-        case 4: ls = L_ZETA_MINUS; on = k == 0; a = i; b = j; break;
-        default: ls = L_ZETA_PLUS; on = k == N; a = i; b = j; break;
-      }
-      if (!on) continue;
+      if (!node_face<NP>(f, i, j, k, ls, a, b)) continue;
       const int side = e2s[(ls - 1) * 2 + 0], flip = e2s[(ls - 1) * 2 + 1];
       int p, q;
       s2v2_inv(N, a, b, flip, ls, p, q);
@@ -207,7 +287,7 @@ k_volume_lines(const double* __restrict__ U, const float* __restrict__ Pvol, con
         for (int c = 0; c < 5; ++c) ut[c] = ut[c] - fx[c * n2] * Lhat;
       }
     }
-    const float sj = Met[((size_t)e * 10 + 9) * n3 + node];
+    const float sj = Ms[9 * n3 + node];
     const size_t g = ((size_t)e * n3 + node) * 5;
 #pragma unroll
     for (int c = 0; c < 5; ++c) {
@@ -217,65 +297,54 @@ k_volume_lines(const double* __restrict__ U, const float* __restrict__ Pvol, con
       if (rkmode == 0) {
         Ut[g + c] = (double)x;
       } else {
-        const double utmp = Ut_tmp[g + c] * mRKA + (double)x;
+        const double utmp = Ts[node * 5 + c] * mRKA + (double)x;
         Ut_tmp[g + c] = utmp;
-        Uio[g + c] = Uio[g + c] + utmp * b_dt;
+        Uio[g + c] = Us[node * 5 + c] + utmp * b_dt;
       }
     }
   }
-  (void)nSides;
   (void)U;
 }
-
-}  // namespace gx
-
-namespace gx {
-
-// The BR1 lifting of the mixed form (Lifting_BR1, lifting_br1.t90:47-167, strong non-conservative
-// form, Gauss-Lobatto nodes) with one thread per 1D line for the volume part.  The line threads
-// differentiate u, v, w and T along their line (D(i,l) as compile-time indexed kernel parameters);
-// the three directions' derivatives of a node meet in shared memory; the block's threads then finish
-// node by node: the metric transform with the Jacobian (Lifting_VolInt_Nonconservative,
-// lifting_volint.t90:262-328), the surface part of the faces the node lies on (0.5 SurfElem
-// (P_slave - P_master) n L_hat sJ, lifting_fillflux.t90:39-103, 212-256, surfint.t90:591-725), and the
-// gradients and their face traces (ProlongToFaceLifting: on Gauss-Lobatto nodes the node's own value).
-// The density gradient, which no flux reads, is not formed.
-template <int NP> struct LiftBasis {
-  float D[NP * NP];  // D(i,l) at D[i + NP*l]
-  float lhm0, lhpN;
-};
-template <int NP> __host__ __device__ constexpr int lift_red_words() {
-  return 4 * NP * (line_pad<NP>(0) + line_pad<NP>(1) + line_pad<NP>(2));
-}
-template <int NP, typename R> struct UseLiftLines {
-  static constexpr bool v = sizeof(R) == 4 && NP >= 4 && NP <= 8;
-};
 
 template <int NP>
 __global__ void __launch_bounds__(3 * NP * NP, 4)
 k_lift_lines(const float* __restrict__ Pvol, const float* __restrict__ Met, const float* __restrict__ Pf,
              const float* __restrict__ Fgeo, const int* __restrict__ E2S, LiftBasis<NP> lb, int nElems, int nSides,
-             float* __restrict__ Gvol, float* __restrict__ Gf) {
+             float* __restrict__ Gvol, float* __restrict__ Gf, int* __restrict__ err) {
   constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, N = NP - 1;
   constexpr int P0 = line_pad<NP>(0), P1 = line_pad<NP>(1), P2 = line_pad<NP>(2);
   constexpr int OFF1 = 4 * n * P0, OFF2 = OFF1 + 4 * n * P1;
-  __shared__ float red[lift_red_words<NP>()];
+  using L = LiftLinesSmem<NP>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ uint64_t bar;
+  float* const red = reinterpret_cast<float*>(smem_raw);
+  float* const Ps = reinterpret_cast<float*>(smem_raw + L::P);  // [7][n3]
+  float* const Ms = reinterpret_cast<float*>(smem_raw + L::M);  // [10][n3]
   const int e = blockIdx.x;
   if (e >= nElems) return;
   const int tid = threadIdx.x;
+  if (tid == 0) mbar_init(&bar);
+  __syncthreads();
+  {
+    unsigned tx = 0;
+    tx += stage_slab(Ps, Pvol + (size_t)e * 7 * n3, 7 * n3 * 4, &bar);
+    tx += stage_slab(Ms, Met + (size_t)e * 10 * n3, 10 * n3 * 4, &bar);
+    if (tid == 0) mbar_arrive_expect(&bar, tx);
+  }
+  __syncthreads();
+  if (__syncthreads_or(!mbar_wait(&bar, 0, err))) return;  // the bulk copies did not complete in time
   {
     const int dir = tid / n2, li = tid - dir * n2;
     int base, stride;
     if (dir == 0) { base = n * li; stride = 1; }
     else if (dir == 1) { base = (li % n) + n2 * (li / n); stride = n; }
     else { base = li; stride = n2; }
-    const float* P = Pvol + (size_t)e * 7 * n3;
     const int slot[4] = {1, 2, 3, 5};  // u, v, w, T
     float x[4][n];
 #pragma unroll
     for (int l = 0; l < n; ++l)
 #pragma unroll
-      for (int c = 0; c < 4; ++c) x[c][l] = P[slot[c] * n3 + base + l * stride];
+      for (int c = 0; c < 4; ++c) x[c][l] = Ps[slot[c] * n3 + base + l * stride];
     float* R0 = red + (dir == 0 ? 0 : (dir == 1 ? OFF1 : OFF2));
     const int Pd = dir == 0 ? P0 : (dir == 1 ? P1 : P2);
 #pragma unroll
@@ -293,7 +362,7 @@ k_lift_lines(const float* __restrict__ Pvol, const float* __restrict__ Met, cons
   const int liftc[4] = {1, 2, 3, 5};
   for (int node = tid; node < n3; node += blockDim.x) {
     const int i = node % n, j = (node / n) % n, k = node / n2;
-    const float* M = Met + (size_t)e * 10 * n3 + node;
+    const float* M = Ms + node;
     const float sj = M[9 * n3];
     const float mf[3] = {sj * M[0], sj * M[n3], sj * M[2 * n3]}, mg[3] = {sj * M[3 * n3], sj * M[4 * n3], sj * M[5 * n3]},
                 mh[3] = {sj * M[6 * n3], sj * M[7 * n3], sj * M[8 * n3]};
@@ -310,16 +379,7 @@ k_lift_lines(const float* __restrict__ Pvol, const float* __restrict__ Met, cons
 #pragma unroll
     for (int f = 0; f < 6; ++f) {
       int ls, a, b;
-      bool on;
-      switch (f) {
-        case 0: ls = L_XI_MINUS; on = i == 0; a = j; b = k; break;
-        case 1: ls = L_XI_PLUS; on = i == N; a = j; b = k; break;
-        case 2: ls = L_ETA_MINUS; on = j == 0; a = i; b = k; break;
-        case 3: ls = L_ETA_PLUS; on = j == N; a = i; b = k; break;
-        case 4: ls = L_ZETA_MINUS; on = k == 0; a = i; b = j; break;
-        default: ls = L_ZETA_PLUS; on = k == N; a = i; b = j; break;
-      }
-      if (!on) continue;
+      if (!node_face<NP>(f, i, j, k, ls, a, b)) continue;
       const int side = e2s[(ls - 1) * 2 + 0], flip = e2s[(ls - 1) * 2 + 1];
       int p, q;
       s2v2_inv(N, a, b, flip, ls, p, q);
@@ -346,16 +406,7 @@ k_lift_lines(const float* __restrict__ Pvol, const float* __restrict__ Met, cons
 #pragma unroll
     for (int f = 0; f < 6; ++f) {
       int ls, a, b;
-      bool on;
-      switch (f) {
-        case 0: ls = L_XI_MINUS; on = i == 0; a = j; b = k; break;
-        case 1: ls = L_XI_PLUS; on = i == N; a = j; b = k; break;
-        case 2: ls = L_ETA_MINUS; on = j == 0; a = i; b = k; break;
-        case 3: ls = L_ETA_PLUS; on = j == N; a = i; b = k; break;
-        case 4: ls = L_ZETA_MINUS; on = k == 0; a = i; b = j; break;
-        default: ls = L_ZETA_PLUS; on = k == N; a = i; b = j; break;
-      }
-      if (!on) continue;
+      if (!node_face<NP>(f, i, j, k, ls, a, b)) continue;
       const int side = e2s[(ls - 1) * 2 + 0], flip = e2s[(ls - 1) * 2 + 1];
       int p, q;
       s2v2_inv(N, a, b, flip, ls, p, q);

@@ -64,10 +64,26 @@ int cfg_vol() {
 template <typename R, int SPL>
 int cfg_lines() {
   if constexpr (gx::UseLines<NP, R, SPL>::v) {
+    const int b = (int)gx::VolLinesSmem<NP>::bytes;
+    GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_volume_lines<NP, SPL, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, b),
+                "k_volume_lines shared-memory attribute");
+    GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_volume_lines<NP, SPL, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, b),
+                "k_volume_lines shared-memory attribute");
     GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_volume_lines<NP, SPL, 0>, cudaFuncAttributePreferredSharedMemoryCarveout, 100),
                 "k_volume_lines carve-out attribute");
     GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_volume_lines<NP, SPL, 1>, cudaFuncAttributePreferredSharedMemoryCarveout, 100),
                 "k_volume_lines carve-out attribute");
+  }
+  return DG_OK;
+}
+template <typename R>
+int cfg_lift_lines() {
+  if constexpr (gx::UseLiftLines<NP, R>::v) {
+    GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_lift_lines<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)gx::LiftLinesSmem<NP>::bytes),
+                "k_lift_lines shared-memory attribute");
+    GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_lift_lines<NP>, cudaFuncAttributePreferredSharedMemoryCarveout, 100),
+                "k_lift_lines carve-out attribute");
   }
   return DG_OK;
 }
@@ -83,7 +99,7 @@ int configure() {
               "k_lift carve-out attribute");
   GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_lift<NP, R, 1>, cudaFuncAttributePreferredSharedMemoryCarveout, 100),
               "k_lift carve-out attribute");
-  int rc = cfg_vol<R, -1, 0>() | cfg_vol<R, -1, 1>();
+  int rc = cfg_vol<R, -1, 0>() | cfg_vol<R, -1, 1>() | cfg_lift_lines<R>();
   if constexpr (NP >= 3) {
     rc |= cfg_vol<R, 0, 0>() | cfg_vol<R, 0, 1>() | cfg_vol<R, 1, 0>() | cfg_vol<R, 1, 1>() | cfg_vol<R, 2, 0>() |
           cfg_vol<R, 2, 1>() | cfg_vol<R, 3, 0>() | cfg_vol<R, 3, 1>() | cfg_vol<R, 4, 0>() | cfg_vol<R, 4, 1>();
@@ -105,14 +121,15 @@ int vol(dg_ctx* ctx, PrecData<R>& P, const S* U, gx::RKArgsT<S> rk, int rkmode, 
     }
     lb.lhm0 = (float)ctx->B.Lhm[0];
     lb.lhpN = (float)ctx->B.Lhp[NP - 1];
+    const size_t sm = gx::VolLinesSmem<NP>::bytes;
     if (ctx->cfg.parabolic)
-      gx::k_volume_lines<NP, SPL, 1><<<ctx->nElems, 3 * NP * NP, 0, st>>>(
-          U, P.Pvol.p, P.Gvol.p, P.Met.p, P.Flux.p, ctx->E2S.p, lb, gas, ctx->nElems, ctx->nSides, rk.Ut, rk.U,
-          rk.Ut_tmp, rk.mRKA, rk.b_dt, rkmode);
+      gx::k_volume_lines<NP, SPL, 1><<<ctx->nElems, 3 * NP * NP, sm, st>>>(
+          U, P.Pvol.p, P.Gvol.p, P.Met.p, P.Flux.p, ctx->E2S.p, lb, gas, ctx->nElems, rk.Ut, rk.U, rk.Ut_tmp, rk.mRKA,
+          rk.b_dt, rkmode, ctx->kerr.p);
     else
-      gx::k_volume_lines<NP, SPL, 0><<<ctx->nElems, 3 * NP * NP, 0, st>>>(
-          U, P.Pvol.p, P.Gvol.p, P.Met.p, P.Flux.p, ctx->E2S.p, lb, gas, ctx->nElems, ctx->nSides, rk.Ut, rk.U,
-          rk.Ut_tmp, rk.mRKA, rk.b_dt, rkmode);
+      gx::k_volume_lines<NP, SPL, 0><<<ctx->nElems, 3 * NP * NP, sm, st>>>(
+          U, P.Pvol.p, P.Gvol.p, P.Met.p, P.Flux.p, ctx->E2S.p, lb, gas, ctx->nElems, rk.Ut, rk.U, rk.Ut_tmp, rk.mRKA,
+          rk.b_dt, rkmode, ctx->kerr.p);
     return DG_OK;
   }
   if (ctx->cfg.parabolic ? !vol_fits<R, SPL, 1>() : !vol_fits<R, SPL, 0>()) {
@@ -158,8 +175,8 @@ void rhs_front(dg_ctx* ctx, PrecData<R>& P, const S* U, const gx::Gas<R>& gas, c
         for (int t = 0; t < NP * NP; ++t) lb.D[t] = (float)ctx->B.D[t];
         lb.lhm0 = (float)ctx->B.Lhm[0];
         lb.lhpN = (float)ctx->B.Lhp[NP - 1];
-        gx::k_lift_lines<NP><<<ctx->nElems, 3 * NP * NP, 0, st>>>(P.Pvol.p, P.Met.p, P.Pf.p, P.Fgeo.p, ctx->E2S.p, lb,
-                                                                  ctx->nElems, ctx->nSides, P.Gvol.p, P.Gf.p);
+        gx::k_lift_lines<NP><<<ctx->nElems, 3 * NP * NP, gx::LiftLinesSmem<NP>::bytes, st>>>(
+            P.Pvol.p, P.Met.p, P.Pf.p, P.Fgeo.p, ctx->E2S.p, lb, ctx->nElems, ctx->nSides, P.Gvol.p, P.Gf.p, ctx->kerr.p);
         lines = true;
       }
     }
