@@ -174,11 +174,14 @@ def _gpu_rows(cfg, mesh, U0):
 
 # Agreement of the GPU run with the oracle's run over the whole regression (t = 0..13, 5,527 steps).
 # Round-off differences of the two evaluation orders grow in the turbulent phase; they reach the
-# time step (dt follows the state), so the times drift apart by ~5e-10 relative by t = 13.  Bounds:
-GPU_VS_ORACLE_EARLY = 1e-10   # every column and the time, t <= 4
-GPU_VS_ORACLE_TIME = 1e-8     # time, whole run (relative)
-GPU_VS_ORACLE_KE = 1e-7       # kinetic energy (incompressible and compressible), whole run
-GPU_VS_ORACLE_ALL = 1e-5      # every column, whole run
+# time step (dt follows the state), so the times drift apart too.  Measured: time 3.6e-15 up to t = 4
+# and 4.7e-10 at t = 13; every column 1.3e-10 up to t = 4; over the whole run kinetic energy 9.5e-10,
+# maximum vorticity 2.0e-7, DR_p 1.4e-8, the other columns <= 1.2e-8.  Bounds:
+GPU_VS_ORACLE_EARLY_TIME = 1e-12  # time, t <= 4 (relative to tEnd)
+GPU_VS_ORACLE_EARLY = 1e-9        # every column, t <= 4
+GPU_VS_ORACLE_TIME = 1e-8         # time, whole run (relative to tEnd)
+GPU_VS_ORACLE_KE = 1e-8           # kinetic energy (incompressible and compressible), whole run
+GPU_VS_ORACLE_ALL = 1e-5          # every column, whole run
 
 
 @pytest.mark.gpu
@@ -194,7 +197,7 @@ def test_tgv_run_gpu_matches_oracle_run():
     early = t_orc <= 4.0
     print("GPU vs oracle: time %.3e (t <= 4: %.3e); columns t <= 4 %.3e; whole run per column %s" % (
         t_err.max(), t_err[early].max(), err[early].max(), {COLUMNS[c]: float(err[:, c].max()) for c in range(15)}))
-    assert t_err[early].max() <= GPU_VS_ORACLE_EARLY, t_err[early].max()
+    assert t_err[early].max() <= GPU_VS_ORACLE_EARLY_TIME, t_err[early].max()
     assert t_err.max() <= GPU_VS_ORACLE_TIME, t_err.max()
     assert err[early].max() <= GPU_VS_ORACLE_EARLY, err[early].max()
     assert err[:, 2:4].max() <= GPU_VS_ORACLE_KE, err[:, 2:4].max()
