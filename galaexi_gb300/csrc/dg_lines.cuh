@@ -73,32 +73,76 @@ template <int NP, typename R> struct UseLiftLines {
 
 __host__ __device__ constexpr size_t round16(size_t b) { return (b + 15) / 16 * 16; }
 
-// shared-memory layout of k_volume_lines (bytes): region A holds the lifted gradients, later the three
-// directions' sums; then the primitives, the metric terms, the FP64 state and RK register
+// shared-memory layout of k_volume_lines, one buffer (bytes): region A holds the lifted gradients
+// (the 12 slots of u, v, w, T; the density gradient is not read), later the three directions' sums;
+// then the primitives rho, u, v, w, p, 1/rho (6 slots), the metric terms and sJ (10 slots), the FP64
+// state and RK register.  A slot is NP planes of NP^2 floats; at NP = 8 the planes are padded by 8
+// words, so that the lines across planes (zeta) and within a plane (eta) read distinct banks.  The
+// kernel holds two buffers.
 template <int NP> struct VolLinesSmem {
+  static constexpr int PADW = NP == 8 ? 8 : 0;
+  static constexpr int PS = NP * NP + PADW;  // plane stride (words)
+  static constexpr int SS = NP * PS;         // slot stride (words)
   static constexpr size_t n3 = (size_t)NP * NP * NP;
-  static constexpr size_t A = round16(15 * n3 * 4 > line_red_words<NP>(5) * 4 ? 15 * n3 * 4 : line_red_words<NP>(5) * 4);
-  static constexpr size_t P = A, M = P + round16(7 * n3 * 4), U = M + round16(10 * n3 * 4), T = U + round16(5 * n3 * 8);
-  static constexpr size_t bytes = T + round16(5 * n3 * 8);
+  static constexpr size_t A = round16(12 * SS * 4 > line_red_words<NP>(5) * 4 ? 12 * SS * 4 : line_red_words<NP>(5) * 4);
+  static constexpr size_t P = A, M = P + round16(6 * SS * 4), U = M + round16(10 * SS * 4), T = U + round16(5 * n3 * 8);
+  static constexpr size_t buffer = T + round16(5 * n3 * 8);
+  static constexpr size_t bytes = 2 * buffer;
 };
-template <int NP> struct LiftLinesSmem {
-  static constexpr size_t n3 = (size_t)NP * NP * NP;
-  static constexpr size_t A = round16(line_red_words<NP>(4) * 4);
-  static constexpr size_t P = A, M = P + round16(7 * n3 * 4);
-  static constexpr size_t bytes = M + round16(10 * n3 * 4);
-};
+// padded shared-memory word of a node
+template <int NP> __device__ __forceinline__ int pidx(int node) {
+  return node + (node / (NP * NP)) * VolLinesSmem<NP>::PADW;
+}
 
-// copy `bytes` from src to dst in shared memory: the issuing thread queues a bulk copy where src, dst
-// and the size are 16-byte aligned (returns the bytes queued), else the block's threads copy words
-__device__ __forceinline__ unsigned stage_slab(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
-  if (bulk_ok(src, dst, bytes)) {
-    if (threadIdx.x == 0) bulk_g2s(dst, src, bytes, bar);
-    return bytes;
+// copy nslots slots of n^3 floats from src into padded shared-memory slots from dst on: with bulk
+// copies (one per plane where the planes are padded, else one for the run), issued by the block's
+// threads in turn, or by the threads' loads where `bulk` is false
+template <int NP>
+__device__ __forceinline__ void stage_slots(float* dst, const float* src, int nslots, bool bulk, uint64_t* bar) {
+  using L = VolLinesSmem<NP>;
+  constexpr int n2 = NP * NP, n3 = NP * NP * NP;
+  if (bulk) {
+    if constexpr (L::PADW > 0) {
+      for (int t = threadIdx.x; t < nslots * NP; t += blockDim.x) {
+        const int s = t / NP, p = t - s * NP;
+        bulk_g2s(dst + s * L::SS + p * L::PS, src + (size_t)s * n3 + p * n2, n2 * 4, bar);
+      }
+    } else {
+      if (threadIdx.x == 0) bulk_g2s(dst, src, nslots * n3 * 4, bar);
+    }
+  } else {
+    for (int t = threadIdx.x; t < nslots * n3; t += blockDim.x) {
+      const int s = t / n3, node = t - s * n3;
+      dst[s * L::SS + pidx<NP>(node)] = src[t];
+    }
   }
-  const unsigned* s = static_cast<const unsigned*>(src);
-  unsigned* d = static_cast<unsigned*>(dst);
-  for (unsigned t = threadIdx.x; t < bytes / 4; t += blockDim.x) d[t] = s[t];
-  return 0;
+}
+__device__ __forceinline__ void stage_bytes(void* dst, const void* src, unsigned bytes, bool bulk, uint64_t* bar) {
+  if (bulk) {
+    if (threadIdx.x == 0) bulk_g2s(dst, src, bytes, bar);
+  } else {
+    const unsigned* s = static_cast<const unsigned*>(src);
+    unsigned* d = static_cast<unsigned*>(dst);
+    for (unsigned t = threadIdx.x; t < bytes / 4; t += blockDim.x) d[t] = s[t];
+  }
+}
+
+// a line of one slot into registers: padded word base + l * step; the xi lines of NP = 4, 8 are
+// 16-byte aligned rows, read as float4
+template <int NP>
+__device__ __forceinline__ void line_load(const float* s, int dir, int pbase, int step, float (&x)[NP]) {
+  if constexpr (NP % 4 == 0) {
+    if (dir == 0) {
+#pragma unroll
+      for (int q = 0; q < NP / 4; ++q) {
+        const float4 t = *reinterpret_cast<const float4*>(s + pbase + 4 * q);
+        x[4 * q] = t.x; x[4 * q + 1] = t.y; x[4 * q + 2] = t.z; x[4 * q + 3] = t.w;
+      }
+      return;
+    }
+  }
+#pragma unroll
+  for (int l = 0; l < NP; ++l) x[l] = s[pbase + l * step];
 }
 
 // the faces a node (i,j,k) lies on, in normal-direction order: local side and face coordinates
@@ -115,236 +159,258 @@ __device__ __forceinline__ bool node_face(int f, int i, int j, int k, int& ls, i
   }
 }
 
+// Persistent: block b computes elements b, b + gridDim.x, ...  The slabs of the block's next element
+// are copied into one of two shared-memory buffers while it computes the current one from the other.
 template <int NP, int SPLIT, int PARAB>
-__global__ void __launch_bounds__(3 * NP * NP, 2)
-k_volume_lines(const double* __restrict__ U, const float* __restrict__ Pvol, const float* __restrict__ Gvol,
-               const float* __restrict__ Met, const float* __restrict__ Flux, const int* __restrict__ E2S,
-               LineBasis<NP> lb, Gas<float> gas, int nElems, double* __restrict__ Ut, double* __restrict__ Uio,
-               double* __restrict__ Ut_tmp, double mRKA, double b_dt, int rkmode, int* __restrict__ err) {
+__global__ void __launch_bounds__(3 * NP * NP, 1)
+k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, const float* __restrict__ Met,
+               const float* __restrict__ Flux, const int* __restrict__ E2S, LineBasis<NP> lb, Gas<float> gas,
+               int nElems, double* __restrict__ Ut, double* __restrict__ Uio, double* __restrict__ Ut_tmp, double mRKA,
+               double b_dt, int rkmode, int* __restrict__ err) {
   constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, N = NP - 1;
   constexpr int P0 = line_pad<NP>(0), P1 = line_pad<NP>(1), P2 = line_pad<NP>(2);
   constexpr int OFF1 = 5 * n * P0, OFF2 = OFF1 + 5 * n * P1;
   using L = VolLinesSmem<NP>;
+  constexpr int SS = L::SS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ uint64_t bar;
-  float* const red = reinterpret_cast<float*>(smem_raw);            // after the line phase
-  float* const Gs = reinterpret_cast<float*>(smem_raw);             // [15][n3] during the line phase
-  float* const Ps = reinterpret_cast<float*>(smem_raw + L::P);      // [7][n3]
-  float* const Ms = reinterpret_cast<float*>(smem_raw + L::M);      // [10][n3]
-  double* const Us = reinterpret_cast<double*>(smem_raw + L::U);    // [n3][5]
-  double* const Ts = reinterpret_cast<double*>(smem_raw + L::T);    // [n3][5]
-  const int e = blockIdx.x;
-  if (e >= nElems) return;
+  __shared__ uint64_t bar[2];
   const int tid = threadIdx.x;
-  // ---- the element's slabs into shared memory
-  if (tid == 0) mbar_init(&bar);
+  if ((int)blockIdx.x >= nElems) return;
+  // bulk copies where every slab starts 16-byte aligned (the float slots and the FP64 slabs of an
+  // element are multiples of 16 bytes for even n); else the threads copy
+  const bool fbulk = (n3 % 4 == 0) && bulk_ok(Pvol, Met, 16) && bulk_ok(Gvol, Gvol, 16);
+  const bool dbulk = (n3 % 2 == 0) && bulk_ok(Uio, Ut_tmp, 16);
+  const unsigned txb = (fbulk ? (unsigned)((6 + 10 + (PARAB ? 12 : 0)) * n3 * 4) : 0u) +
+                       (dbulk && rkmode ? (unsigned)(2 * 5 * n3 * 8) : 0u);
+  if (tid == 0) { mbar_init(&bar[0]); mbar_init(&bar[1]); }
   __syncthreads();
-  {
-    unsigned tx = 0;
-    tx += stage_slab(Ps, Pvol + (size_t)e * 7 * n3, 7 * n3 * 4, &bar);
-    tx += stage_slab(Ms, Met + (size_t)e * 10 * n3, 10 * n3 * 4, &bar);
-    if (PARAB) tx += stage_slab(Gs, Gvol + (size_t)e * 15 * n3, 15 * n3 * 4, &bar);
-    if (rkmode) {
-      tx += stage_slab(Us, Uio + (size_t)e * 5 * n3, 5 * n3 * 8, &bar);
-      tx += stage_slab(Ts, Ut_tmp + (size_t)e * 5 * n3, 5 * n3 * 8, &bar);
-    }
-    if (tid == 0) mbar_arrive_expect(&bar, tx);
-  }
-  __syncthreads();  // the threads' own copies
-  if (__syncthreads_or(!mbar_wait(&bar, 0, err))) return;  // the bulk copies did not complete in time
-  const int dir = tid / n2, li = tid - dir * n2;
-  int base, stride;
-  if (dir == 0) { base = n * li; stride = 1; }
-  else if (dir == 1) { base = (li % n) + n2 * (li / n); stride = n; }
-  else { base = li; stride = n2; }
-  const float* M = Ms + 3 * dir * n3;
-  float acc[n][5];
-  float m0[n], m1[n], m2[n];
-  {
-    // the line's node data
-    float rho[n], u[n], v[n], w[n], pm[n], aux[n];
+  // queue the slabs of element e into buffer b; the barrier is armed with the byte count first
+  auto issue = [&](int e, int b) {
+    unsigned char* B = smem_raw + (size_t)b * L::buffer;
+    if (tid == 0) mbar_arrive_expect(&bar[b], txb);
+    float* Pd = reinterpret_cast<float*>(B + L::P);
+    const float* Pg = Pvol + (size_t)e * 7 * n3;
+    stage_slots<NP>(Pd, Pg, 5, fbulk, &bar[b]);                    // rho, u, v, w, p
+    stage_slots<NP>(Pd + 5 * SS, Pg + 6 * n3, 1, fbulk, &bar[b]);  // 1/rho
+    stage_slots<NP>(reinterpret_cast<float*>(B + L::M), Met + (size_t)e * 10 * n3, 10, fbulk, &bar[b]);
+    if (PARAB) {
+      const float* Gg = Gvol + (size_t)e * 15 * n3;
 #pragma unroll
-    for (int l = 0; l < n; ++l) {
-      const int node = base + l * stride;
-      rho[l] = Ps[node];
-      u[l] = Ps[n3 + node];
-      v[l] = Ps[2 * n3 + node];
-      w[l] = Ps[3 * n3 + node];
-      const float pmom = Ps[4 * n3 + node];  // momentum pressure (p' = p - p_ref in the mixed form)
-      const float srho = Ps[6 * n3 + node];
-      m0[l] = M[node];
-      m1[l] = M[n3 + node];
-      m2[l] = M[2 * n3 + node];
-      const float pabs = p_abs(pmom, gas);
-      const float E = pabs * gas.sKappaM1 + 0.5f * rho[l] * (u[l] * u[l] + v[l] * v[l] + w[l] * w[l]);
-      aux[l] = pair_aux<SPLIT, float>(rho[l], u[l], v[l], w[l], E, pabs, srho);
-      pm[l] = (SPLIT == DG_SPLIT_PI) ? 4.f * pmom : pmom;  // PI: 4p (exact scaling, see below)
+      for (int d = 0; d < 3; ++d)  // the gradients of u, v, w, T in x, y, z
+        stage_slots<NP>(reinterpret_cast<float*>(B) + 4 * d * SS, Gg + (5 * d + 1) * n3, 4, fbulk, &bar[b]);
     }
+    if (rkmode) {
+      stage_bytes(B + L::U, Uio + (size_t)e * 5 * n3, 5 * n3 * 8, dbulk, &bar[b]);
+      stage_bytes(B + L::T, Ut_tmp + (size_t)e * 5 * n3, 5 * n3 * 8, dbulk, &bar[b]);
+    }
+  };
+  issue(blockIdx.x, 0);
+  int k = 0;
+  for (int e = blockIdx.x; e < nElems; e += gridDim.x, ++k) {
+    const int cb = k & 1;
+    const int en = e + gridDim.x;
+    if (en < nElems) issue(en, cb ^ 1);  // the other buffer was released at the end of the last element
+    __syncthreads();                     // the threads' own copies
+    if (__syncthreads_or(!mbar_wait(&bar[cb], (k >> 1) & 1, err))) {
+      // the copies did not complete in time: wait (bounded) for those into the other buffer, and leave
+      if (en < nElems) mbar_wait(&bar[cb ^ 1], ((k + 1) >> 1) & 1, nullptr);
+      return;
+    }
+    unsigned char* B = smem_raw + (size_t)cb * L::buffer;
+    float* const red = reinterpret_cast<float*>(B);             // the directions' sums, after the line phase
+    const float* const Gs = reinterpret_cast<const float*>(B);  // [12] gradient slots during the line phase
+    const float* const Ps = reinterpret_cast<const float*>(B + L::P);
+    const float* const Ms = reinterpret_cast<const float*>(B + L::M);
+    const double* const Us = reinterpret_cast<const double*>(B + L::U);  // [n3][5]
+    const double* const Ts = reinterpret_cast<const double*>(B + L::T);
+    const int dir = tid / n2, li = tid - dir * n2;
+    int base, step;
+    if (dir == 0) { base = n * li; step = 1; }
+    else if (dir == 1) { base = (li % n) + n2 * (li / n); step = n; }
+    else { base = li; step = L::PS; }
+    const int pb = pidx<NP>(base);
+    const float* M = Ms + 3 * dir * SS;
+    float acc[n][5];
+    float m0[n], m1[n], m2[n], u[n], v[n], w[n];
+    line_load<NP>(Ps + SS, dir, pb, step, u);
+    line_load<NP>(Ps + 2 * SS, dir, pb, step, v);
+    line_load<NP>(Ps + 3 * SS, dir, pb, step, w);
+    line_load<NP>(M, dir, pb, step, m0);
+    line_load<NP>(M + SS, dir, pb, step, m1);
+    line_load<NP>(M + 2 * SS, dir, pb, step, m2);
+    {
+      // the line's node data
+      float rho[n], pm[n], aux[n], srho[n];
+      line_load<NP>(Ps, dir, pb, step, rho);
+      line_load<NP>(Ps + 4 * SS, dir, pb, step, pm);  // momentum pressure (p' = p - p_ref in the mixed form)
+      line_load<NP>(Ps + 5 * SS, dir, pb, step, srho);
+#pragma unroll
+      for (int l = 0; l < n; ++l) {
+        const float pmom = pm[l];
+        const float pabs = p_abs(pmom, gas);
+        const float E = pabs * gas.sKappaM1 + 0.5f * rho[l] * (u[l] * u[l] + v[l] * v[l] + w[l] * w[l]);
+        aux[l] = pair_aux<SPLIT, float>(rho[l], u[l], v[l], w[l], E, pabs, srho[l]);
+        pm[l] = (SPLIT == DG_SPLIT_PI) ? 4.f * pmom : pmom;  // PI: 4p (exact scaling, see below)
+      }
+#pragma unroll
+      for (int l = 0; l < n; ++l)
+#pragma unroll
+        for (int c = 0; c < 5; ++c) acc[l][c] = 0.f;
+      // split form: every pair of the line once, added to both of its nodes
+#pragma unroll
+      for (int a = 0; a < n - 1; ++a) {
+#pragma unroll
+        for (int b = a + 1; b < n; ++b) {
+          const float Ms0 = m0[a] + m0[b], Ms1 = m1[a] + m1[b], Ms2 = m2[a] + m2[b];
+          float F[5];
+          if constexpr (SPLIT == DG_SPLIT_PI) {
+            // 8 x the PI flux, the density row at 4 x (doubled at the end); DVolSurf carries the 1/8
+            const float rs = rho[a] + rho[b], us = u[a] + u[b], vs = v[a] + v[b], ws = w[a] + w[b];
+            const float ps4 = pm[a] + pm[b];
+            const float Vsum = Ms0 * us + Ms1 * vs + Ms2 * ws;
+            const float q8 = rs * Vsum;
+            F[0] = q8;
+            F[1] = q8 * us + ps4 * Ms0;
+            F[2] = q8 * vs + ps4 * Ms1;
+            F[3] = q8 * ws + ps4 * Ms2;
+            F[4] = q8 * (aux[a] + aux[b]);
+          } else {
+            PairNode<float> A, Bn;
+            A.rho = rho[a]; A.u = u[a]; A.v = v[a]; A.w = w[a]; A.pm = pm[a]; A.aux = aux[a];
+            Bn.rho = rho[b]; Bn.u = u[b]; Bn.v = v[b]; Bn.w = w[b]; Bn.pm = pm[b]; Bn.aux = aux[b];
+            A.m1 = A.m2 = A.m3 = Bn.m1 = Bn.m2 = Bn.m3 = 0.f;
+            split_pair_flux<SPLIT, float>(A, Bn, Ms0, Ms1, Ms2, 2.f * gas.pref, F);
+          }
+          const float dba = lb.dvs[b + n * a], dab = lb.dvs[a + n * b];  // DVolSurf(l=b,i=a), DVolSurf(l=a,i=b)
+#pragma unroll
+          for (int c = 0; c < 5; ++c) {
+            acc[a][c] = acc[a][c] + dba * F[c];
+            acc[b][c] = acc[b][c] + dab * F[c];
+          }
+        }
+      }
+      if constexpr (SPLIT == DG_SPLIT_PI) {
+#pragma unroll
+        for (int l = 0; l < n; ++l) acc[l][0] = 2.f * acc[l][0];
+      }
+    }
+    if constexpr (PARAB) {
+      // viscous part: the line direction's contravariant viscous fluxes of the line's nodes
+      // (EvalTransformedDiffFlux3D with the direction's metric terms), contracted with D_hat^T
+      float fv[n][4];
+      {
+        float g[12][n];  // d(u, v, w, T)/dx, then /dy, /dz
+#pragma unroll
+        for (int s = 0; s < 12; ++s) line_load<NP>(Gs + s * SS, dir, pb, step, g[s]);
+#pragma unroll
+        for (int l = 0; l < n; ++l) {
+          float gx[5], gy[5], gz[5];
+          gx[0] = gy[0] = gz[0] = 0.f;  // no flux reads the density gradient
+#pragma unroll
+          for (int c = 1; c < 5; ++c) { gx[c] = g[c - 1][l]; gy[c] = g[3 + c][l]; gz[c] = g[7 + c][l]; }
+          const float vel[3] = {u[l], v[l], w[l]};
+          float tau[6], tq[3];
+          visc_stress(gx, gy, gz, vel, gas.mu, gas.lambda, tau, tq);
+          fv[l][0] = -m0[l] * tau[0] - m1[l] * tau[3] - m2[l] * tau[4];
+          fv[l][1] = -m0[l] * tau[3] - m1[l] * tau[1] - m2[l] * tau[5];
+          fv[l][2] = -m0[l] * tau[4] - m1[l] * tau[5] - m2[l] * tau[2];
+          fv[l][3] = -m0[l] * tq[0] - m1[l] * tq[1] - m2[l] * tq[2];
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < n; ++i)
+#pragma unroll
+        for (int l = 0; l < n; ++l) {
+          const float c = lb.dht[l + n * i];
+#pragma unroll
+          for (int q = 1; q < 5; ++q) acc[i][q] = acc[i][q] + c * fv[l][q - 1];
+        }
+    }
+    __syncthreads();  // every read of the gradients, which the sums overwrite
+    // the three directions' sums of every node meet in shared memory
+    float* R0 = red + (dir == 0 ? 0 : (dir == 1 ? OFF1 : OFF2));
+    const int Pd = dir == 0 ? P0 : (dir == 1 ? P1 : P2);
 #pragma unroll
     for (int l = 0; l < n; ++l)
 #pragma unroll
-      for (int c = 0; c < 5; ++c) acc[l][c] = 0.f;
-    // split form: every pair of the line once, added to both of its nodes
+      for (int c = 0; c < 5; ++c) R0[(c * n + l) * Pd + li] = acc[l][c];
+    __syncthreads();
+    // node by node: volume sum + Gauss-Lobatto surface integral, -1, Jacobian, output / RK stage
+    const int* e2s = E2S + (size_t)e * 12;
+    for (int node = tid; node < n3; node += blockDim.x) {
+      const int i = node % n, j = (node / n) % n, kk = node / n2;
+      float val[5], ut[5];
 #pragma unroll
-    for (int a = 0; a < n - 1; ++a) {
+      for (int c = 0; c < 5; ++c) {
+        val[c] = red[(c * n + i) * P0 + j + n * kk] + red[OFF1 + (c * n + j) * P1 + i + n * kk] +
+                 red[OFF2 + (c * n + kk) * P2 + i + n * j];
+        ut[c] = 0.f;
+      }
 #pragma unroll
-      for (int b = a + 1; b < n; ++b) {
-        const float Ms0 = m0[a] + m0[b], Ms1 = m1[a] + m1[b], Ms2 = m2[a] + m2[b];
-        float F[5];
-        if constexpr (SPLIT == DG_SPLIT_PI) {
-          // 8 x the PI flux, the density row at 4 x (doubled at the end); DVolSurf carries the 1/8
-          const float rs = rho[a] + rho[b], us = u[a] + u[b], vs = v[a] + v[b], ws = w[a] + w[b];
-          const float ps4 = pm[a] + pm[b];
-          const float Vsum = Ms0 * us + Ms1 * vs + Ms2 * ws;
-          const float q8 = rs * Vsum;
-          F[0] = q8;
-          F[1] = q8 * us + ps4 * Ms0;
-          F[2] = q8 * vs + ps4 * Ms1;
-          F[3] = q8 * ws + ps4 * Ms2;
-          F[4] = q8 * (aux[a] + aux[b]);
+      for (int f = 0; f < 6; ++f) {
+        int ls, a, b;
+        if (!node_face<NP>(f, i, j, kk, ls, a, b)) continue;
+        const int side = e2s[(ls - 1) * 2 + 0], flip = e2s[(ls - 1) * 2 + 1];
+        int p, q;
+        s2v2_inv(N, a, b, flip, ls, p, q);
+        const float* fx = Flux + (size_t)side * 5 * n2 + p + n * q;
+        const float Lhat = is_minus(ls) ? lb.lhm0 : lb.lhpN;
+        if (flip == 0) {
+#pragma unroll
+          for (int c = 0; c < 5; ++c) ut[c] = ut[c] + fx[c * n2] * Lhat;
         } else {
-          PairNode<float> A, B;
-          A.rho = rho[a]; A.u = u[a]; A.v = v[a]; A.w = w[a]; A.pm = pm[a]; A.aux = aux[a];
-          B.rho = rho[b]; B.u = u[b]; B.v = v[b]; B.w = w[b]; B.pm = pm[b]; B.aux = aux[b];
-          A.m1 = A.m2 = A.m3 = B.m1 = B.m2 = B.m3 = 0.f;
-          split_pair_flux<SPLIT, float>(A, B, Ms0, Ms1, Ms2, 2.f * gas.pref, F);
-        }
-        const float dba = lb.dvs[b + n * a], dab = lb.dvs[a + n * b];  // DVolSurf(l=b,i=a), DVolSurf(l=a,i=b)
 #pragma unroll
-        for (int c = 0; c < 5; ++c) {
-          acc[a][c] = acc[a][c] + dba * F[c];
-          acc[b][c] = acc[b][c] + dab * F[c];
+          for (int c = 0; c < 5; ++c) ut[c] = ut[c] - fx[c * n2] * Lhat;
         }
       }
-    }
-    if constexpr (SPLIT == DG_SPLIT_PI) {
+      const float sj = Ms[9 * SS + pidx<NP>(node)];
+      const size_t g = ((size_t)e * n3 + node) * 5;
 #pragma unroll
-      for (int l = 0; l < n; ++l) acc[l][0] = 2.f * acc[l][0];
-    }
-  }
-  if constexpr (PARAB) {
-    // viscous part: the line direction's contravariant viscous fluxes of the line's nodes
-    // (EvalTransformedDiffFlux3D with the direction's metric terms), contracted with D_hat^T
-    float fv[n][4];
-#pragma unroll
-    for (int l = 0; l < n; ++l) {
-      const int node = base + l * stride;
-      float gx[5], gy[5], gz[5];
-      gx[0] = gy[0] = gz[0] = 0.f;  // no flux reads the density gradient
-#pragma unroll
-      for (int c = 1; c < 5; ++c) { gx[c] = Gs[c * n3 + node]; gy[c] = Gs[(5 + c) * n3 + node]; gz[c] = Gs[(10 + c) * n3 + node]; }
-      const float vel[3] = {Ps[n3 + node], Ps[2 * n3 + node], Ps[3 * n3 + node]};
-      float tau[6], tq[3];
-      visc_stress(gx, gy, gz, vel, gas.mu, gas.lambda, tau, tq);
-      fv[l][0] = -m0[l] * tau[0] - m1[l] * tau[3] - m2[l] * tau[4];
-      fv[l][1] = -m0[l] * tau[3] - m1[l] * tau[1] - m2[l] * tau[5];
-      fv[l][2] = -m0[l] * tau[4] - m1[l] * tau[5] - m2[l] * tau[2];
-      fv[l][3] = -m0[l] * tq[0] - m1[l] * tq[1] - m2[l] * tq[2];
-    }
-#pragma unroll
-    for (int i = 0; i < n; ++i)
-#pragma unroll
-      for (int l = 0; l < n; ++l) {
-        const float c = lb.dht[l + n * i];
-#pragma unroll
-        for (int v = 1; v < 5; ++v) acc[i][v] = acc[i][v] + c * fv[l][v - 1];
-      }
-    __syncthreads();  // every read of the gradients, which the sums overwrite
-  }
-  // the three directions' sums of every node meet in shared memory
-  float* R0 = red + (dir == 0 ? 0 : (dir == 1 ? OFF1 : OFF2));
-  const int Pd = dir == 0 ? P0 : (dir == 1 ? P1 : P2);
-#pragma unroll
-  for (int l = 0; l < n; ++l)
-#pragma unroll
-    for (int c = 0; c < 5; ++c) R0[(c * n + l) * Pd + li] = acc[l][c];
-  __syncthreads();
-  // node by node: volume sum + Gauss-Lobatto surface integral, -1, Jacobian, output / RK stage
-  const int* e2s = E2S + (size_t)e * 12;
-  for (int node = tid; node < n3; node += blockDim.x) {
-    const int i = node % n, j = (node / n) % n, k = node / n2;
-    float val[5], ut[5];
-#pragma unroll
-    for (int c = 0; c < 5; ++c) {
-      val[c] = red[(c * n + i) * P0 + j + n * k] + red[OFF1 + (c * n + j) * P1 + i + n * k] +
-               red[OFF2 + (c * n + k) * P2 + i + n * j];
-      ut[c] = 0.f;
-    }
-#pragma unroll
-    for (int f = 0; f < 6; ++f) {
-      int ls, a, b;
-      if (!node_face<NP>(f, i, j, k, ls, a, b)) continue;
-      const int side = e2s[(ls - 1) * 2 + 0], flip = e2s[(ls - 1) * 2 + 1];
-      int p, q;
-      s2v2_inv(N, a, b, flip, ls, p, q);
-      const float* fx = Flux + (size_t)side * 5 * n2 + p + n * q;
-      const float Lhat = is_minus(ls) ? lb.lhm0 : lb.lhpN;
-      if (flip == 0) {
-#pragma unroll
-        for (int c = 0; c < 5; ++c) ut[c] = ut[c] + fx[c * n2] * Lhat;
-      } else {
-#pragma unroll
-        for (int c = 0; c < 5; ++c) ut[c] = ut[c] - fx[c * n2] * Lhat;
+      for (int c = 0; c < 5; ++c) {
+        float x = val[c] + ut[c];
+        x = x * -1.f;
+        x = x * sj;
+        if (rkmode == 0) {
+          Ut[g + c] = (double)x;
+        } else {
+          const double utmp = Ts[node * 5 + c] * mRKA + (double)x;
+          Ut_tmp[g + c] = utmp;
+          Uio[g + c] = Us[node * 5 + c] + utmp * b_dt;
+        }
       }
     }
-    const float sj = Ms[9 * n3 + node];
-    const size_t g = ((size_t)e * n3 + node) * 5;
-#pragma unroll
-    for (int c = 0; c < 5; ++c) {
-      float x = val[c] + ut[c];
-      x = x * -1.f;
-      x = x * sj;
-      if (rkmode == 0) {
-        Ut[g + c] = (double)x;
-      } else {
-        const double utmp = Ts[node * 5 + c] * mRKA + (double)x;
-        Ut_tmp[g + c] = utmp;
-        Uio[g + c] = Us[node * 5 + c] + utmp * b_dt;
-      }
-    }
+    // this buffer is refilled by the bulk copies of the element after next: order this element's
+    // shared-memory accesses before them
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
   }
-  (void)U;
 }
 
 template <int NP>
 __global__ void __launch_bounds__(3 * NP * NP, 4)
 k_lift_lines(const float* __restrict__ Pvol, const float* __restrict__ Met, const float* __restrict__ Pf,
              const float* __restrict__ Fgeo, const int* __restrict__ E2S, LiftBasis<NP> lb, int nElems, int nSides,
-             float* __restrict__ Gvol, float* __restrict__ Gf, int* __restrict__ err) {
+             float* __restrict__ Gvol, float* __restrict__ Gf) {
   constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, N = NP - 1;
   constexpr int P0 = line_pad<NP>(0), P1 = line_pad<NP>(1), P2 = line_pad<NP>(2);
   constexpr int OFF1 = 4 * n * P0, OFF2 = OFF1 + 4 * n * P1;
-  using L = LiftLinesSmem<NP>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ uint64_t bar;
-  float* const red = reinterpret_cast<float*>(smem_raw);
-  float* const Ps = reinterpret_cast<float*>(smem_raw + L::P);  // [7][n3]
-  float* const Ms = reinterpret_cast<float*>(smem_raw + L::M);  // [10][n3]
+  __shared__ float red[line_red_words<NP>(4)];
   const int e = blockIdx.x;
   if (e >= nElems) return;
   const int tid = threadIdx.x;
-  if (tid == 0) mbar_init(&bar);
-  __syncthreads();
-  {
-    unsigned tx = 0;
-    tx += stage_slab(Ps, Pvol + (size_t)e * 7 * n3, 7 * n3 * 4, &bar);
-    tx += stage_slab(Ms, Met + (size_t)e * 10 * n3, 10 * n3 * 4, &bar);
-    if (tid == 0) mbar_arrive_expect(&bar, tx);
-  }
-  __syncthreads();
-  if (__syncthreads_or(!mbar_wait(&bar, 0, err))) return;  // the bulk copies did not complete in time
   {
     const int dir = tid / n2, li = tid - dir * n2;
     int base, stride;
     if (dir == 0) { base = n * li; stride = 1; }
     else if (dir == 1) { base = (li % n) + n2 * (li / n); stride = n; }
     else { base = li; stride = n2; }
+    const float* P = Pvol + (size_t)e * 7 * n3;
     const int slot[4] = {1, 2, 3, 5};  // u, v, w, T
     float x[4][n];
 #pragma unroll
     for (int l = 0; l < n; ++l)
 #pragma unroll
-      for (int c = 0; c < 4; ++c) x[c][l] = Ps[slot[c] * n3 + base + l * stride];
+      for (int c = 0; c < 4; ++c) x[c][l] = P[slot[c] * n3 + base + l * stride];
     float* R0 = red + (dir == 0 ? 0 : (dir == 1 ? OFF1 : OFF2));
     const int Pd = dir == 0 ? P0 : (dir == 1 ? P1 : P2);
 #pragma unroll
@@ -362,7 +428,7 @@ k_lift_lines(const float* __restrict__ Pvol, const float* __restrict__ Met, cons
   const int liftc[4] = {1, 2, 3, 5};
   for (int node = tid; node < n3; node += blockDim.x) {
     const int i = node % n, j = (node / n) % n, k = node / n2;
-    const float* M = Ms + node;
+    const float* M = Met + (size_t)e * 10 * n3 + node;
     const float sj = M[9 * n3];
     const float mf[3] = {sj * M[0], sj * M[n3], sj * M[2 * n3]}, mg[3] = {sj * M[3 * n3], sj * M[4 * n3], sj * M[5 * n3]},
                 mh[3] = {sj * M[6 * n3], sj * M[7 * n3], sj * M[8 * n3]};

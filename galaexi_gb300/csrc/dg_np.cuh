@@ -78,13 +78,9 @@ int cfg_lines() {
 }
 template <typename R>
 int cfg_lift_lines() {
-  if constexpr (gx::UseLiftLines<NP, R>::v) {
-    GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_lift_lines<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)gx::LiftLinesSmem<NP>::bytes),
-                "k_lift_lines shared-memory attribute");
+  if constexpr (gx::UseLiftLines<NP, R>::v)
     GX_CUDA_TRY(cudaFuncSetAttribute(gx::k_lift_lines<NP>, cudaFuncAttributePreferredSharedMemoryCarveout, 100),
                 "k_lift_lines carve-out attribute");
-  }
   return DG_OK;
 }
 
@@ -122,14 +118,23 @@ int vol(dg_ctx* ctx, PrecData<R>& P, const S* U, gx::RKArgsT<S> rk, int rkmode, 
     lb.lhm0 = (float)ctx->B.Lhm[0];
     lb.lhpN = (float)ctx->B.Lhp[NP - 1];
     const size_t sm = gx::VolLinesSmem<NP>::bytes;
-    if (ctx->cfg.parabolic)
-      gx::k_volume_lines<NP, SPL, 1><<<ctx->nElems, 3 * NP * NP, sm, st>>>(
-          U, P.Pvol.p, P.Gvol.p, P.Met.p, P.Flux.p, ctx->E2S.p, lb, gas, ctx->nElems, rk.Ut, rk.U, rk.Ut_tmp, rk.mRKA,
-          rk.b_dt, rkmode, ctx->kerr.p);
-    else
-      gx::k_volume_lines<NP, SPL, 0><<<ctx->nElems, 3 * NP * NP, sm, st>>>(
-          U, P.Pvol.p, P.Gvol.p, P.Met.p, P.Flux.p, ctx->E2S.p, lb, gas, ctx->nElems, rk.Ut, rk.U, rk.Ut_tmp, rk.mRKA,
-          rk.b_dt, rkmode, ctx->kerr.p);
+    auto kern = ctx->cfg.parabolic ? gx::k_volume_lines<NP, SPL, 1> : gx::k_volume_lines<NP, SPL, 0>;
+    if (ctx->lines_grid == 0) {
+      // persistent: every SM holds as many blocks as fit, each walks its share of the elements
+      int dev = 0, nsm = 0, occ = 0;
+      GX_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
+      GX_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
+      GX_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 3 * NP * NP, sm),
+                  "k_volume_lines occupancy");
+      if (occ < 1) {
+        gxh::set_error("k_volume_lines does not fit an SM");
+        return DG_ERR_UNSUPPORTED;
+      }
+      ctx->lines_grid = nsm * occ;
+    }
+    const int grid = ctx->nElems < ctx->lines_grid ? ctx->nElems : ctx->lines_grid;
+    kern<<<grid, 3 * NP * NP, sm, st>>>(P.Pvol.p, P.Gvol.p, P.Met.p, P.Flux.p, ctx->E2S.p, lb, gas, ctx->nElems, rk.Ut,
+                                        rk.U, rk.Ut_tmp, rk.mRKA, rk.b_dt, rkmode, ctx->kerr.p);
     return DG_OK;
   }
   if (ctx->cfg.parabolic ? !vol_fits<R, SPL, 1>() : !vol_fits<R, SPL, 0>()) {
@@ -175,8 +180,8 @@ void rhs_front(dg_ctx* ctx, PrecData<R>& P, const S* U, const gx::Gas<R>& gas, c
         for (int t = 0; t < NP * NP; ++t) lb.D[t] = (float)ctx->B.D[t];
         lb.lhm0 = (float)ctx->B.Lhm[0];
         lb.lhpN = (float)ctx->B.Lhp[NP - 1];
-        gx::k_lift_lines<NP><<<ctx->nElems, 3 * NP * NP, gx::LiftLinesSmem<NP>::bytes, st>>>(
-            P.Pvol.p, P.Met.p, P.Pf.p, P.Fgeo.p, ctx->E2S.p, lb, ctx->nElems, ctx->nSides, P.Gvol.p, P.Gf.p, ctx->kerr.p);
+        gx::k_lift_lines<NP><<<ctx->nElems, 3 * NP * NP, 0, st>>>(P.Pvol.p, P.Met.p, P.Pf.p, P.Fgeo.p, ctx->E2S.p, lb,
+                                                                  ctx->nElems, ctx->nSides, P.Gvol.p, P.Gf.p);
         lines = true;
       }
     }
