@@ -74,49 +74,20 @@ template <int NP, typename R> struct UseLiftLines {
 __host__ __device__ constexpr size_t round16(size_t b) { return (b + 15) / 16 * 16; }
 
 // shared-memory layout of k_volume_lines, one buffer (bytes): region A holds the lifted gradients
-// (the 12 slots of u, v, w, T; the density gradient is not read), later the three directions' sums;
-// then the primitives rho, u, v, w, p, 1/rho (6 slots), the metric terms and sJ (10 slots), the FP64
-// state and RK register.  A slot is NP planes of NP^2 floats; at NP = 8 the planes are padded by 8
-// words, so that the lines across planes (zeta) and within a plane (eta) read distinct banks.  The
-// kernel holds two buffers.
+// (12 slots: u, v, w, T in x, y, z; the density gradient is not read) and the primitives rho, u, v,
+// w, p, 1/rho (6 slots), later the three directions' sums; then the metric terms and sJ (10 slots).
+// A slot is n^3 floats in the node order of the state.  The kernel holds two buffers; at n = 8 they
+// take 112 KB, so that two blocks share an SM.
 template <int NP> struct VolLinesSmem {
-  static constexpr int PADW = NP == 8 ? 8 : 0;
-  static constexpr int PS = NP * NP + PADW;  // plane stride (words)
-  static constexpr int SS = NP * PS;         // slot stride (words)
-  static constexpr size_t n3 = (size_t)NP * NP * NP;
-  static constexpr size_t A = round16(12 * SS * 4 > line_red_words<NP>(5) * 4 ? 12 * SS * 4 : line_red_words<NP>(5) * 4);
-  static constexpr size_t P = A, M = P + round16(6 * SS * 4), U = M + round16(10 * SS * 4), T = U + round16(5 * n3 * 8);
-  static constexpr size_t buffer = T + round16(5 * n3 * 8);
+  static constexpr int SS = NP * NP * NP;  // slot stride (words)
+  static constexpr size_t A = round16(18 * SS * 4 > line_red_words<NP>(5) * 4 ? 18 * SS * 4 : line_red_words<NP>(5) * 4);
+  static constexpr size_t G = 0, P = 12 * SS * 4, M = A;
+  static constexpr size_t buffer = M + round16(10 * SS * 4);
   static constexpr size_t bytes = 2 * buffer;
 };
-// padded shared-memory word of a node
-template <int NP> __device__ __forceinline__ int pidx(int node) {
-  return node + (node / (NP * NP)) * VolLinesSmem<NP>::PADW;
-}
 
-// copy nslots slots of n^3 floats from src into padded shared-memory slots from dst on: with bulk
-// copies (one per plane where the planes are padded, else one for the run), issued by the block's
-// threads in turn, or by the threads' loads where `bulk` is false
-template <int NP>
-__device__ __forceinline__ void stage_slots(float* dst, const float* src, int nslots, bool bulk, uint64_t* bar) {
-  using L = VolLinesSmem<NP>;
-  constexpr int n2 = NP * NP, n3 = NP * NP * NP;
-  if (bulk) {
-    if constexpr (L::PADW > 0) {
-      for (int t = threadIdx.x; t < nslots * NP; t += blockDim.x) {
-        const int s = t / NP, p = t - s * NP;
-        bulk_g2s(dst + s * L::SS + p * L::PS, src + (size_t)s * n3 + p * n2, n2 * 4, bar);
-      }
-    } else {
-      if (threadIdx.x == 0) bulk_g2s(dst, src, nslots * n3 * 4, bar);
-    }
-  } else {
-    for (int t = threadIdx.x; t < nslots * n3; t += blockDim.x) {
-      const int s = t / n3, node = t - s * n3;
-      dst[s * L::SS + pidx<NP>(node)] = src[t];
-    }
-  }
-}
+// copy `bytes` from src to dst in shared memory: one bulk copy issued by thread 0 where `bulk`
+// (source, destination and size 16-byte aligned), else the block's threads copy words
 __device__ __forceinline__ void stage_bytes(void* dst, const void* src, unsigned bytes, bool bulk, uint64_t* bar) {
   if (bulk) {
     if (threadIdx.x == 0) bulk_g2s(dst, src, bytes, bar);
@@ -127,22 +98,30 @@ __device__ __forceinline__ void stage_bytes(void* dst, const void* src, unsigned
   }
 }
 
-// a line of one slot into registers: padded word base + l * step; the xi lines of NP = 4, 8 are
-// 16-byte aligned rows, read as float4
-template <int NP>
-__device__ __forceinline__ void line_load(const float* s, int dir, int pbase, int step, float (&x)[NP]) {
-  if constexpr (NP % 4 == 0) {
+// C consecutive nodes l0 .. l0+C-1 of a line of one slot: word base + l * step; on the xi lines
+// (step 1) of n = 4, 8 four nodes are one aligned float4
+template <int NP, int C>
+__device__ __forceinline__ void line_chunk(const float* s, int dir, int base, int step, int l0, float (&x)[C]) {
+  if constexpr (C == 4 && NP % 4 == 0) {
     if (dir == 0) {
-#pragma unroll
-      for (int q = 0; q < NP / 4; ++q) {
-        const float4 t = *reinterpret_cast<const float4*>(s + pbase + 4 * q);
-        x[4 * q] = t.x; x[4 * q + 1] = t.y; x[4 * q + 2] = t.z; x[4 * q + 3] = t.w;
-      }
+      const float4 t = *reinterpret_cast<const float4*>(s + base + l0);
+      x[0] = t.x; x[1] = t.y; x[2] = t.z; x[3] = t.w;
       return;
     }
   }
 #pragma unroll
-  for (int l = 0; l < NP; ++l) x[l] = s[pbase + l * step];
+  for (int c = 0; c < C; ++c) x[c] = s[base + (l0 + c) * step];
+}
+template <int NP>
+__device__ __forceinline__ void line_load(const float* s, int dir, int base, int step, float (&x)[NP]) {
+  constexpr int C = NP % 4 == 0 ? 4 : 1;
+#pragma unroll
+  for (int l0 = 0; l0 < NP; l0 += C) {
+    float t[C];
+    line_chunk<NP, C>(s, dir, base, step, l0, t);
+#pragma unroll
+    for (int c = 0; c < C; ++c) x[l0 + c] = t[c];
+  }
 }
 
 // the faces a node (i,j,k) lies on, in normal-direction order: local side and face coordinates
@@ -162,7 +141,7 @@ __device__ __forceinline__ bool node_face(int f, int i, int j, int k, int& ls, i
 // Persistent: block b computes elements b, b + gridDim.x, ...  The slabs of the block's next element
 // are copied into one of two shared-memory buffers while it computes the current one from the other.
 template <int NP, int SPLIT, int PARAB>
-__global__ void __launch_bounds__(3 * NP * NP, 1)
+__global__ void __launch_bounds__(3 * NP * NP, 2)
 k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, const float* __restrict__ Met,
                const float* __restrict__ Flux, const int* __restrict__ E2S, LineBasis<NP> lb, Gas<float> gas,
                int nElems, double* __restrict__ Ut, double* __restrict__ Uio, double* __restrict__ Ut_tmp, double mRKA,
@@ -170,38 +149,32 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
   constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, N = NP - 1;
   constexpr int P0 = line_pad<NP>(0), P1 = line_pad<NP>(1), P2 = line_pad<NP>(2);
   constexpr int OFF1 = 5 * n * P0, OFF2 = OFF1 + 5 * n * P1;
+  constexpr int SS = n3;
+  constexpr int C = NP % 4 == 0 ? 4 : 1;  // nodes per chunk of the viscous phase
   using L = VolLinesSmem<NP>;
-  constexpr int SS = L::SS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ uint64_t bar[2];
   const int tid = threadIdx.x;
   if ((int)blockIdx.x >= nElems) return;
-  // bulk copies where every slab starts 16-byte aligned (the float slots and the FP64 slabs of an
-  // element are multiples of 16 bytes for even n); else the threads copy
-  const bool fbulk = (n3 % 4 == 0) && bulk_ok(Pvol, Met, 16) && bulk_ok(Gvol, Gvol, 16);
-  const bool dbulk = (n3 % 2 == 0) && bulk_ok(Uio, Ut_tmp, 16);
-  const unsigned txb = (fbulk ? (unsigned)((6 + 10 + (PARAB ? 12 : 0)) * n3 * 4) : 0u) +
-                       (dbulk && rkmode ? (unsigned)(2 * 5 * n3 * 8) : 0u);
+  // bulk copies where the element's slabs start 16-byte aligned (n^3 a multiple of 4); else the
+  // threads copy
+  const bool bulk = (n3 % 4 == 0) && bulk_ok(Pvol, Met, 16) && bulk_ok(Gvol, Gvol, 16);
+  const unsigned txb = bulk ? (unsigned)((6 + 10 + (PARAB ? 12 : 0)) * n3 * 4) : 0u;
   if (tid == 0) { mbar_init(&bar[0]); mbar_init(&bar[1]); }
   __syncthreads();
   // queue the slabs of element e into buffer b; the barrier is armed with the byte count first
   auto issue = [&](int e, int b) {
     unsigned char* B = smem_raw + (size_t)b * L::buffer;
     if (tid == 0) mbar_arrive_expect(&bar[b], txb);
-    float* Pd = reinterpret_cast<float*>(B + L::P);
     const float* Pg = Pvol + (size_t)e * 7 * n3;
-    stage_slots<NP>(Pd, Pg, 5, fbulk, &bar[b]);                    // rho, u, v, w, p
-    stage_slots<NP>(Pd + 5 * SS, Pg + 6 * n3, 1, fbulk, &bar[b]);  // 1/rho
-    stage_slots<NP>(reinterpret_cast<float*>(B + L::M), Met + (size_t)e * 10 * n3, 10, fbulk, &bar[b]);
+    stage_bytes(B + L::P, Pg, 5 * n3 * 4, bulk, &bar[b]);                  // rho, u, v, w, p
+    stage_bytes(B + L::P + 5 * n3 * 4, Pg + 6 * n3, n3 * 4, bulk, &bar[b]);  // 1/rho
+    stage_bytes(B + L::M, Met + (size_t)e * 10 * n3, 10 * n3 * 4, bulk, &bar[b]);
     if (PARAB) {
       const float* Gg = Gvol + (size_t)e * 15 * n3;
 #pragma unroll
       for (int d = 0; d < 3; ++d)  // the gradients of u, v, w, T in x, y, z
-        stage_slots<NP>(reinterpret_cast<float*>(B) + 4 * d * SS, Gg + (5 * d + 1) * n3, 4, fbulk, &bar[b]);
-    }
-    if (rkmode) {
-      stage_bytes(B + L::U, Uio + (size_t)e * 5 * n3, 5 * n3 * 8, dbulk, &bar[b]);
-      stage_bytes(B + L::T, Ut_tmp + (size_t)e * 5 * n3, 5 * n3 * 8, dbulk, &bar[b]);
+        stage_bytes(B + L::G + 4 * d * n3 * 4, Gg + (5 * d + 1) * n3, 4 * n3 * 4, bulk, &bar[b]);
     }
   };
   issue(blockIdx.x, 0);
@@ -217,39 +190,36 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
       return;
     }
     unsigned char* B = smem_raw + (size_t)cb * L::buffer;
-    float* const red = reinterpret_cast<float*>(B);             // the directions' sums, after the line phase
-    const float* const Gs = reinterpret_cast<const float*>(B);  // [12] gradient slots during the line phase
+    float* const red = reinterpret_cast<float*>(B);  // the directions' sums, after the line phase
+    const float* const Gs = reinterpret_cast<const float*>(B + L::G);
     const float* const Ps = reinterpret_cast<const float*>(B + L::P);
     const float* const Ms = reinterpret_cast<const float*>(B + L::M);
-    const double* const Us = reinterpret_cast<const double*>(B + L::U);  // [n3][5]
-    const double* const Ts = reinterpret_cast<const double*>(B + L::T);
     const int dir = tid / n2, li = tid - dir * n2;
     int base, step;
     if (dir == 0) { base = n * li; step = 1; }
     else if (dir == 1) { base = (li % n) + n2 * (li / n); step = n; }
-    else { base = li; step = L::PS; }
-    const int pb = pidx<NP>(base);
+    else { base = li; step = n2; }
     const float* M = Ms + 3 * dir * SS;
     float acc[n][5];
     float m0[n], m1[n], m2[n], u[n], v[n], w[n];
-    line_load<NP>(Ps + SS, dir, pb, step, u);
-    line_load<NP>(Ps + 2 * SS, dir, pb, step, v);
-    line_load<NP>(Ps + 3 * SS, dir, pb, step, w);
-    line_load<NP>(M, dir, pb, step, m0);
-    line_load<NP>(M + SS, dir, pb, step, m1);
-    line_load<NP>(M + 2 * SS, dir, pb, step, m2);
+    line_load<NP>(Ps + SS, dir, base, step, u);
+    line_load<NP>(Ps + 2 * SS, dir, base, step, v);
+    line_load<NP>(Ps + 3 * SS, dir, base, step, w);
+    line_load<NP>(M, dir, base, step, m0);
+    line_load<NP>(M + SS, dir, base, step, m1);
+    line_load<NP>(M + 2 * SS, dir, base, step, m2);
     {
       // the line's node data
-      float rho[n], pm[n], aux[n], srho[n];
-      line_load<NP>(Ps, dir, pb, step, rho);
-      line_load<NP>(Ps + 4 * SS, dir, pb, step, pm);  // momentum pressure (p' = p - p_ref in the mixed form)
-      line_load<NP>(Ps + 5 * SS, dir, pb, step, srho);
+      float rho[n], pm[n], aux[n];
+      line_load<NP>(Ps, dir, base, step, rho);
+      line_load<NP>(Ps + 4 * SS, dir, base, step, pm);  // momentum pressure (p' = p - p_ref in the mixed form)
+      line_load<NP>(Ps + 5 * SS, dir, base, step, aux);  // 1/rho, replaced by the form's auxiliary variable
 #pragma unroll
       for (int l = 0; l < n; ++l) {
         const float pmom = pm[l];
         const float pabs = p_abs(pmom, gas);
         const float E = pabs * gas.sKappaM1 + 0.5f * rho[l] * (u[l] * u[l] + v[l] * v[l] + w[l] * w[l]);
-        aux[l] = pair_aux<SPLIT, float>(rho[l], u[l], v[l], w[l], E, pabs, srho[l]);
+        aux[l] = pair_aux<SPLIT, float>(rho[l], u[l], v[l], w[l], E, pabs, aux[l]);
         pm[l] = (SPLIT == DG_SPLIT_PI) ? 4.f * pmom : pmom;  // PI: 4p (exact scaling, see below)
       }
 #pragma unroll
@@ -295,38 +265,38 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
       }
     }
     if constexpr (PARAB) {
-      // viscous part: the line direction's contravariant viscous fluxes of the line's nodes
-      // (EvalTransformedDiffFlux3D with the direction's metric terms), contracted with D_hat^T
-      float fv[n][4];
-      {
-        float g[12][n];  // d(u, v, w, T)/dx, then /dy, /dz
+      // viscous part: the line direction's contravariant viscous flux of each node (EvalTransformedDiffFlux3D
+      // with the direction's metric terms), added to every node of the line with D_hat^T
 #pragma unroll
-        for (int s = 0; s < 12; ++s) line_load<NP>(Gs + s * SS, dir, pb, step, g[s]);
+      for (int l0 = 0; l0 < n; l0 += C) {
+        float g[12][C];  // d(u, v, w, T)/dx, then /dy, /dz of the chunk's nodes
 #pragma unroll
-        for (int l = 0; l < n; ++l) {
+        for (int s = 0; s < 12; ++s) line_chunk<NP, C>(Gs + s * SS, dir, base, step, l0, g[s]);
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+          const int l = l0 + c;
           float gx[5], gy[5], gz[5];
           gx[0] = gy[0] = gz[0] = 0.f;  // no flux reads the density gradient
 #pragma unroll
-          for (int c = 1; c < 5; ++c) { gx[c] = g[c - 1][l]; gy[c] = g[3 + c][l]; gz[c] = g[7 + c][l]; }
+          for (int q = 1; q < 5; ++q) { gx[q] = g[q - 1][c]; gy[q] = g[3 + q][c]; gz[q] = g[7 + q][c]; }
           const float vel[3] = {u[l], v[l], w[l]};
           float tau[6], tq[3];
           visc_stress(gx, gy, gz, vel, gas.mu, gas.lambda, tau, tq);
-          fv[l][0] = -m0[l] * tau[0] - m1[l] * tau[3] - m2[l] * tau[4];
-          fv[l][1] = -m0[l] * tau[3] - m1[l] * tau[1] - m2[l] * tau[5];
-          fv[l][2] = -m0[l] * tau[4] - m1[l] * tau[5] - m2[l] * tau[2];
-          fv[l][3] = -m0[l] * tq[0] - m1[l] * tq[1] - m2[l] * tq[2];
+          float fv[4];
+          fv[0] = -m0[l] * tau[0] - m1[l] * tau[3] - m2[l] * tau[4];
+          fv[1] = -m0[l] * tau[3] - m1[l] * tau[1] - m2[l] * tau[5];
+          fv[2] = -m0[l] * tau[4] - m1[l] * tau[5] - m2[l] * tau[2];
+          fv[3] = -m0[l] * tq[0] - m1[l] * tq[1] - m2[l] * tq[2];
+#pragma unroll
+          for (int i = 0; i < n; ++i) {
+            const float d = lb.dht[l + n * i];
+#pragma unroll
+            for (int q = 1; q < 5; ++q) acc[i][q] = acc[i][q] + d * fv[q - 1];
+          }
         }
       }
-#pragma unroll
-      for (int i = 0; i < n; ++i)
-#pragma unroll
-        for (int l = 0; l < n; ++l) {
-          const float c = lb.dht[l + n * i];
-#pragma unroll
-          for (int q = 1; q < 5; ++q) acc[i][q] = acc[i][q] + c * fv[l][q - 1];
-        }
     }
-    __syncthreads();  // every read of the gradients, which the sums overwrite
+    __syncthreads();  // every read of the gradients and primitives, which the sums overwrite
     // the three directions' sums of every node meet in shared memory
     float* R0 = red + (dir == 0 ? 0 : (dir == 1 ? OFF1 : OFF2));
     const int Pd = dir == 0 ? P0 : (dir == 1 ? P1 : P2);
@@ -339,6 +309,12 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
     const int* e2s = E2S + (size_t)e * 12;
     for (int node = tid; node < n3; node += blockDim.x) {
       const int i = node % n, j = (node / n) % n, kk = node / n2;
+      const size_t g = ((size_t)e * n3 + node) * 5;
+      double ur[5], tr[5];
+      if (rkmode) {
+#pragma unroll
+        for (int c = 0; c < 5; ++c) { ur[c] = Uio[g + c]; tr[c] = Ut_tmp[g + c]; }
+      }
       float val[5], ut[5];
 #pragma unroll
       for (int c = 0; c < 5; ++c) {
@@ -363,8 +339,7 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
           for (int c = 0; c < 5; ++c) ut[c] = ut[c] - fx[c * n2] * Lhat;
         }
       }
-      const float sj = Ms[9 * SS + pidx<NP>(node)];
-      const size_t g = ((size_t)e * n3 + node) * 5;
+      const float sj = Ms[9 * SS + node];
 #pragma unroll
       for (int c = 0; c < 5; ++c) {
         float x = val[c] + ut[c];
@@ -373,9 +348,9 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
         if (rkmode == 0) {
           Ut[g + c] = (double)x;
         } else {
-          const double utmp = Ts[node * 5 + c] * mRKA + (double)x;
+          const double utmp = tr[c] * mRKA + (double)x;
           Ut_tmp[g + c] = utmp;
-          Uio[g + c] = Us[node * 5 + c] + utmp * b_dt;
+          Uio[g + c] = ur[c] + utmp * b_dt;
         }
       }
     }
