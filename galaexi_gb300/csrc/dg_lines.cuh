@@ -75,14 +75,15 @@ __host__ __device__ constexpr size_t round16(size_t b) { return (b + 15) / 16 * 
 
 // shared-memory layout of k_volume_lines, one buffer (bytes): region A holds the lifted gradients
 // (12 slots: u, v, w, T in x, y, z; the density gradient is not read) and the primitives rho, u, v,
-// w, p, 1/rho (6 slots), later the three directions' sums; then the metric terms and sJ (10 slots).
-// A slot is n^3 floats in the node order of the state.  The kernel holds two buffers; at n = 8 they
+// w, p, 1/rho (6 slots), later the three directions' sums; then the metric terms and sJ (10 slots)
+// and the element's row of E2S.  A slot is n^3 floats in the node order of the state.  The kernel holds two buffers; at n = 8 they
 // take 112 KB, so that two blocks share an SM.
 template <int NP> struct VolLinesSmem {
   static constexpr int SS = NP * NP * NP;  // slot stride (words)
   static constexpr size_t A = round16(18 * SS * 4 > line_red_words<NP>(5) * 4 ? 18 * SS * 4 : line_red_words<NP>(5) * 4);
   static constexpr size_t G = 0, P = 12 * SS * 4, M = A;
-  static constexpr size_t buffer = M + round16(10 * SS * 4);
+  static constexpr size_t E = M + round16(10 * SS * 4);
+  static constexpr size_t buffer = E + 64;
   static constexpr size_t bytes = 2 * buffer;
 };
 
@@ -159,7 +160,12 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
   // bulk copies where the element's slabs start 16-byte aligned (n^3 a multiple of 4); else the
   // threads copy
   const bool bulk = (n3 % 4 == 0) && bulk_ok(Pvol, Met, 16) && bulk_ok(Gvol, Gvol, 16);
-  const unsigned txb = bulk ? (unsigned)((6 + 10 + (PARAB ? 12 : 0)) * n3 * 4) : 0u;
+  const bool ebulk = bulk_ok(E2S, E2S, 16);  // a row of E2S is 48 bytes
+  // the RK register and state of the next element, and the face fluxes of the current one, are
+  // pulled into L2 ahead of the node-by-node finish that reads them
+  const bool upre = rkmode && (n3 % 2 == 0) && bulk_ok(Uio, Ut_tmp, 16);
+  const bool fpre = (n2 % 4 == 0) && bulk_ok(Flux, Flux, 16);
+  const unsigned txb = (bulk ? (unsigned)((6 + 10 + (PARAB ? 12 : 0)) * n3 * 4) : 0u) + (ebulk ? 48u : 0u);
   if (tid == 0) { mbar_init(&bar[0]); mbar_init(&bar[1]); }
   __syncthreads();
   // queue the slabs of element e into buffer b; the barrier is armed with the byte count first
@@ -170,6 +176,11 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
     stage_bytes(B + L::P, Pg, 5 * n3 * 4, bulk, &bar[b]);                  // rho, u, v, w, p
     stage_bytes(B + L::P + 5 * n3 * 4, Pg + 6 * n3, n3 * 4, bulk, &bar[b]);  // 1/rho
     stage_bytes(B + L::M, Met + (size_t)e * 10 * n3, 10 * n3 * 4, bulk, &bar[b]);
+    stage_bytes(B + L::E, E2S + (size_t)e * 12, 48, ebulk, &bar[b]);
+    if (upre && tid == 32) {
+      bulk_prefetch_l2(Uio + (size_t)e * 5 * n3, 5 * n3 * 8);
+      bulk_prefetch_l2(Ut_tmp + (size_t)e * 5 * n3, 5 * n3 * 8);
+    }
     if (PARAB) {
       const float* Gg = Gvol + (size_t)e * 15 * n3;
 #pragma unroll
@@ -194,6 +205,8 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
     const float* const Gs = reinterpret_cast<const float*>(B + L::G);
     const float* const Ps = reinterpret_cast<const float*>(B + L::P);
     const float* const Ms = reinterpret_cast<const float*>(B + L::M);
+    const int* const es = reinterpret_cast<const int*>(B + L::E);  // E2S row: side, flip of the six local sides
+    if (fpre && tid >= 64 && tid < 70) bulk_prefetch_l2(Flux + (size_t)es[(tid - 64) * 2] * 5 * n2, 5 * n2 * 4);
     const int dir = tid / n2, li = tid - dir * n2;
     int base, step;
     if (dir == 0) { base = n * li; step = 1; }
@@ -304,53 +317,88 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
     for (int l = 0; l < n; ++l)
 #pragma unroll
       for (int c = 0; c < 5; ++c) R0[(c * n + l) * Pd + li] = acc[l][c];
-    __syncthreads();
-    // node by node: volume sum + Gauss-Lobatto surface integral, -1, Jacobian, output / RK stage
-    const int* e2s = E2S + (size_t)e * 12;
-    for (int node = tid; node < n3; node += blockDim.x) {
-      const int i = node % n, j = (node / n) % n, kk = node / n2;
-      const size_t g = ((size_t)e * n3 + node) * 5;
-      double ur[5], tr[5];
-      if (rkmode) {
+    // face fluxes of the node-by-node finish (pulled into L2 at the start of the element), loaded
+    // before the barrier, all at once: Gauss-Lobatto surface integral of the faces a node lies on
+    constexpr int NPT = (n3 + 3 * n2 - 1) / (3 * n2);  // nodes per thread
+    float ut[NPT][5];
 #pragma unroll
-        for (int c = 0; c < 5; ++c) { ur[c] = Uio[g + c]; tr[c] = Ut_tmp[g + c]; }
-      }
-      float val[5], ut[5];
+    for (int it = 0; it < NPT; ++it) {
+      const int node = tid + it * 3 * n2;
 #pragma unroll
-      for (int c = 0; c < 5; ++c) {
-        val[c] = red[(c * n + i) * P0 + j + n * kk] + red[OFF1 + (c * n + j) * P1 + i + n * kk] +
-                 red[OFF2 + (c * n + kk) * P2 + i + n * j];
-        ut[c] = 0.f;
-      }
+      for (int c = 0; c < 5; ++c) ut[it][c] = 0.f;
+      if (node < n3) {
+        const int i = node % n, j = (node / n) % n, kk = node / n2;
 #pragma unroll
-      for (int f = 0; f < 6; ++f) {
-        int ls, a, b;
-        if (!node_face<NP>(f, i, j, kk, ls, a, b)) continue;
-        const int side = e2s[(ls - 1) * 2 + 0], flip = e2s[(ls - 1) * 2 + 1];
-        int p, q;
-        s2v2_inv(N, a, b, flip, ls, p, q);
-        const float* fx = Flux + (size_t)side * 5 * n2 + p + n * q;
-        const float Lhat = is_minus(ls) ? lb.lhm0 : lb.lhpN;
-        if (flip == 0) {
+        for (int f = 0; f < 6; ++f) {
+          int ls, a, b;
+          if (!node_face<NP>(f, i, j, kk, ls, a, b)) continue;
+          const int side = es[(ls - 1) * 2 + 0], flip = es[(ls - 1) * 2 + 1];
+          int p, q;
+          s2v2_inv(N, a, b, flip, ls, p, q);
+          const float* fx = Flux + (size_t)side * 5 * n2 + p + n * q;
+          const float Lhat = is_minus(ls) ? lb.lhm0 : lb.lhpN;
+          if (flip == 0) {
 #pragma unroll
-          for (int c = 0; c < 5; ++c) ut[c] = ut[c] + fx[c * n2] * Lhat;
-        } else {
+            for (int c = 0; c < 5; ++c) ut[it][c] = ut[it][c] + fx[c * n2] * Lhat;
+          } else {
 #pragma unroll
-          for (int c = 0; c < 5; ++c) ut[c] = ut[c] - fx[c * n2] * Lhat;
+            for (int c = 0; c < 5; ++c) ut[it][c] = ut[it][c] - fx[c * n2] * Lhat;
+          }
         }
       }
-      const float sj = Ms[9 * SS + node];
+    }
+    __syncthreads();
+    // node by node: volume sum + surface integral, -1, Jacobian -> Ut in FP32, node-major [n3][5], in
+    // the metric slots 0-4 (read only by the line phase)
+    float* const Xs = reinterpret_cast<float*>(B + L::M);
 #pragma unroll
-      for (int c = 0; c < 5; ++c) {
-        float x = val[c] + ut[c];
-        x = x * -1.f;
-        x = x * sj;
-        if (rkmode == 0) {
-          Ut[g + c] = (double)x;
-        } else {
-          const double utmp = tr[c] * mRKA + (double)x;
-          Ut_tmp[g + c] = utmp;
-          Uio[g + c] = ur[c] + utmp * b_dt;
+    for (int it = 0; it < NPT; ++it) {
+      const int node = tid + it * 3 * n2;
+      if (node < n3) {
+        const int i = node % n, j = (node / n) % n, kk = node / n2;
+        const float sj = Ms[9 * SS + node];
+#pragma unroll
+        for (int c = 0; c < 5; ++c) {
+          const float vs = red[(c * n + i) * P0 + j + n * kk] + red[OFF1 + (c * n + j) * P1 + i + n * kk] +
+                           red[OFF2 + (c * n + kk) * P2 + i + n * j];
+          float x = vs + ut[it][c];
+          x = x * -1.f;
+          Xs[node * 5 + c] = x * sj;
+        }
+      }
+    }
+    __syncthreads();
+    // output / LSERK-W2 stage in FP64 (vector.f90:163-183), one value per thread in turn: the element's
+    // (5, n^3) record is contiguous, so the loads and stores coalesce; the loads of a thread's values
+    // are issued together (the state and RK register were pulled into L2 one element ahead)
+    {
+      constexpr int NV = 5 * n3, T3 = 3 * n2, NIT = (NV + T3 - 1) / T3;
+      const size_t g0 = (size_t)e * NV;
+      if (rkmode == 0) {
+#pragma unroll
+        for (int it = 0; it < NIT; ++it) {
+          const int t = tid + it * T3;
+          if (t < NV) Ut[g0 + t] = (double)Xs[t];
+        }
+      } else {
+        constexpr int BATCH = 7;
+#pragma unroll
+        for (int i0 = 0; i0 < NIT; i0 += BATCH) {
+          double tr[BATCH], ur[BATCH];
+#pragma unroll
+          for (int q = 0; q < BATCH; ++q) {
+            const int t = tid + (i0 + q) * T3;
+            if (i0 + q < NIT && t < NV) { tr[q] = Ut_tmp[g0 + t]; ur[q] = Uio[g0 + t]; }
+          }
+#pragma unroll
+          for (int q = 0; q < BATCH; ++q) {
+            const int t = tid + (i0 + q) * T3;
+            if (i0 + q < NIT && t < NV) {
+              const double utmp = tr[q] * mRKA + (double)Xs[t];
+              Ut_tmp[g0 + t] = utmp;
+              Uio[g0 + t] = ur[q] + utmp * b_dt;
+            }
+          }
         }
       }
     }

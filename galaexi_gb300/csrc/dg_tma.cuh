@@ -1,5 +1,6 @@
 // One-dimensional bulk copies global -> shared memory by the tensor memory accelerator
-// (cp.async.bulk), completing on an mbarrier in shared memory, and a bounded wait for them.
+// (cp.async.bulk), completing on an mbarrier in shared memory, and a bounded wait for them; bulk
+// prefetches global -> L2.
 //
 // A copy needs a 16-byte aligned source and destination and a size that is a multiple of 16 bytes;
 // bulk_ok() checks that.  One thread arms the barrier with the total byte count of its copies and
@@ -39,6 +40,11 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
                ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
                : "memory");
+}
+
+// start pulling `bytes` (16-byte aligned address and size) from global memory into L2; no completion
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
 }
 
 __device__ __forceinline__ bool mbar_test(uint64_t* bar, unsigned phase) {
