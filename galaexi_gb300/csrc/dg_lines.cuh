@@ -75,12 +75,12 @@ __host__ __device__ constexpr size_t round16(size_t b) { return (b + 15) / 16 * 
 
 // shared-memory layout of k_volume_lines, one buffer (bytes): region A holds the lifted gradients
 // (12 slots: u, v, w, T in x, y, z; the density gradient is not read) and the primitives rho, u, v,
-// w, p, 1/rho (6 slots), later the three directions' sums; then the metric terms and sJ (10 slots)
+// w, p (5 slots), later the three directions' sums; then the metric terms and sJ (10 slots)
 // and the element's row of E2S.  A slot is n^3 floats in the node order of the state.  The kernel holds two buffers; at n = 8 they
 // take 112 KB, so that two blocks share an SM.
 template <int NP> struct VolLinesSmem {
   static constexpr int SS = NP * NP * NP;  // slot stride (words)
-  static constexpr size_t A = round16(18 * SS * 4 > line_red_words<NP>(5) * 4 ? 18 * SS * 4 : line_red_words<NP>(5) * 4);
+  static constexpr size_t A = round16(17 * SS * 4 > line_red_words<NP>(5) * 4 ? 17 * SS * 4 : line_red_words<NP>(5) * 4);
   static constexpr size_t G = 0, P = 12 * SS * 4, M = A;
   static constexpr size_t E = M + round16(10 * SS * 4);
   static constexpr size_t buffer = E + 64;
@@ -165,7 +165,7 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
   // pulled into L2 ahead of the node-by-node finish that reads them
   const bool upre = rkmode && (n3 % 2 == 0) && bulk_ok(Uio, Ut_tmp, 16);
   const bool fpre = (n2 % 4 == 0) && bulk_ok(Flux, Flux, 16);
-  const unsigned txb = (bulk ? (unsigned)((6 + 10 + (PARAB ? 12 : 0)) * n3 * 4) : 0u) + (ebulk ? 48u : 0u);
+  const unsigned txb = (bulk ? (unsigned)((5 + 10 + (PARAB ? 12 : 0)) * n3 * 4) : 0u) + (ebulk ? 48u : 0u);
   if (tid == 0) { mbar_init(&bar[0]); mbar_init(&bar[1]); }
   __syncthreads();
   // queue the slabs of element e into buffer b; the barrier is armed with the byte count first
@@ -173,8 +173,7 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
     unsigned char* B = smem_raw + (size_t)b * L::buffer;
     if (tid == 0) mbar_arrive_expect(&bar[b], txb);
     const float* Pg = Pvol + (size_t)e * 7 * n3;
-    stage_bytes(B + L::P, Pg, 5 * n3 * 4, bulk, &bar[b]);                  // rho, u, v, w, p
-    stage_bytes(B + L::P + 5 * n3 * 4, Pg + 6 * n3, n3 * 4, bulk, &bar[b]);  // 1/rho
+    stage_bytes(B + L::P, Pg, 5 * n3 * 4, bulk, &bar[b]);  // rho, u, v, w, p
     stage_bytes(B + L::M, Met + (size_t)e * 10 * n3, 10 * n3 * 4, bulk, &bar[b]);
     stage_bytes(B + L::E, E2S + (size_t)e * 12, 48, ebulk, &bar[b]);
     if (upre && tid == 32) {
@@ -226,13 +225,13 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
       float rho[n], pm[n], aux[n];
       line_load<NP>(Ps, dir, base, step, rho);
       line_load<NP>(Ps + 4 * SS, dir, base, step, pm);  // momentum pressure (p' = p - p_ref in the mixed form)
-      line_load<NP>(Ps + 5 * SS, dir, base, step, aux);  // 1/rho, replaced by the form's auxiliary variable
 #pragma unroll
       for (int l = 0; l < n; ++l) {
         const float pmom = pm[l];
         const float pabs = p_abs(pmom, gas);
         const float E = pabs * gas.sKappaM1 + 0.5f * rho[l] * (u[l] * u[l] + v[l] * v[l] + w[l] * w[l]);
-        aux[l] = pair_aux<SPLIT, float>(rho[l], u[l], v[l], w[l], E, pabs, aux[l]);
+        const float srho = 1.f / rho[l];  // the same division as the stored 1/rho of the primitives
+        aux[l] = pair_aux<SPLIT, float>(rho[l], u[l], v[l], w[l], E, pabs, srho);
         pm[l] = (SPLIT == DG_SPLIT_PI) ? 4.f * pmom : pmom;  // PI: 4p (exact scaling, see below)
       }
 #pragma unroll
@@ -369,8 +368,8 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
     }
     __syncthreads();
     // output / LSERK-W2 stage in FP64 (vector.f90:163-183), one value per thread in turn: the element's
-    // (5, n^3) record is contiguous, so the loads and stores coalesce; the loads of a thread's values
-    // are issued together (the state and RK register were pulled into L2 one element ahead)
+    // (5, n^3) record is contiguous, so the loads and stores coalesce; all loads of a thread are issued
+    // before its first store (the state and RK register were pulled into L2 one element ahead)
     {
       constexpr int NV = 5 * n3, T3 = 3 * n2, NIT = (NV + T3 - 1) / T3;
       const size_t g0 = (size_t)e * NV;
@@ -381,23 +380,19 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
           if (t < NV) Ut[g0 + t] = (double)Xs[t];
         }
       } else {
-        constexpr int BATCH = 7;
+        double tr[NIT], ur[NIT];
 #pragma unroll
-        for (int i0 = 0; i0 < NIT; i0 += BATCH) {
-          double tr[BATCH], ur[BATCH];
+        for (int q = 0; q < NIT; ++q) {
+          const int t = tid + q * T3;
+          if (t < NV) { tr[q] = Ut_tmp[g0 + t]; ur[q] = Uio[g0 + t]; }
+        }
 #pragma unroll
-          for (int q = 0; q < BATCH; ++q) {
-            const int t = tid + (i0 + q) * T3;
-            if (i0 + q < NIT && t < NV) { tr[q] = Ut_tmp[g0 + t]; ur[q] = Uio[g0 + t]; }
-          }
-#pragma unroll
-          for (int q = 0; q < BATCH; ++q) {
-            const int t = tid + (i0 + q) * T3;
-            if (i0 + q < NIT && t < NV) {
-              const double utmp = tr[q] * mRKA + (double)Xs[t];
-              Ut_tmp[g0 + t] = utmp;
-              Uio[g0 + t] = ur[q] + utmp * b_dt;
-            }
+        for (int q = 0; q < NIT; ++q) {
+          const int t = tid + q * T3;
+          if (t < NV) {
+            const double utmp = tr[q] * mRKA + (double)Xs[t];
+            Ut_tmp[g0 + t] = utmp;
+            Uio[g0 + t] = ur[q] + utmp * b_dt;
           }
         }
       }
