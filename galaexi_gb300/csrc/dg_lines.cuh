@@ -201,11 +201,43 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
     }
     unsigned char* B = smem_raw + (size_t)cb * L::buffer;
     float* const red = reinterpret_cast<float*>(B);  // the directions' sums, after the line phase
-    const float* const Gs = reinterpret_cast<const float*>(B + L::G);
+    float* const Gs = reinterpret_cast<float*>(B + L::G);
     const float* const Ps = reinterpret_cast<const float*>(B + L::P);
     const float* const Ms = reinterpret_cast<const float*>(B + L::M);
     const int* const es = reinterpret_cast<const int*>(B + L::E);  // E2S row: side, flip of the six local sides
     if (fpre && tid >= 64 && tid < 70) bulk_prefetch_l2(Flux + (size_t)es[(tid - 64) * 2] * 5 * n2, 5 * n2 * 4);
+    constexpr int NPT = (n3 + 3 * n2 - 1) / (3 * n2);  // nodes per thread in the node-parallel phases
+    if constexpr (PARAB) {
+      // node by node: the viscous stress and heat flux from the lifted gradients, and from them the
+      // contravariant viscous flux of each direction d (EvalTransformedDiffFlux3D with the metric terms
+      // of d), written over the node's gradients: slot 4 d + (momentum x, y, z, energy)
+#pragma unroll
+      for (int it = 0; it < NPT; ++it) {
+        const int node = tid + it * 3 * n2;
+        if (node < n3) {
+          float gx[5], gy[5], gz[5];
+          gx[0] = gy[0] = gz[0] = 0.f;  // no flux reads the density gradient
+#pragma unroll
+          for (int q = 1; q < 5; ++q) {
+            gx[q] = Gs[(q - 1) * SS + node];
+            gy[q] = Gs[(3 + q) * SS + node];
+            gz[q] = Gs[(7 + q) * SS + node];
+          }
+          const float vel[3] = {Ps[SS + node], Ps[2 * SS + node], Ps[3 * SS + node]};
+          float tau[6], tq[3];
+          visc_stress(gx, gy, gz, vel, gas.mu, gas.lambda, tau, tq);
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            const float a0 = Ms[3 * d * SS + node], a1 = Ms[(3 * d + 1) * SS + node], a2 = Ms[(3 * d + 2) * SS + node];
+            Gs[4 * d * SS + node] = -a0 * tau[0] - a1 * tau[3] - a2 * tau[4];
+            Gs[(4 * d + 1) * SS + node] = -a0 * tau[3] - a1 * tau[1] - a2 * tau[5];
+            Gs[(4 * d + 2) * SS + node] = -a0 * tau[4] - a1 * tau[5] - a2 * tau[2];
+            Gs[(4 * d + 3) * SS + node] = -a0 * tq[0] - a1 * tq[1] - a2 * tq[2];
+          }
+        }
+      }
+      __syncthreads();
+    }
     const int dir = tid / n2, li = tid - dir * n2;
     int base, step;
     if (dir == 0) { base = n * li; step = 1; }
@@ -277,33 +309,21 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
       }
     }
     if constexpr (PARAB) {
-      // viscous part: the line direction's contravariant viscous flux of each node (EvalTransformedDiffFlux3D
-      // with the direction's metric terms), added to every node of the line with D_hat^T
+      // viscous part: the line direction's contravariant viscous fluxes of the line's nodes, added to
+      // every node of the line with D_hat^T
 #pragma unroll
       for (int l0 = 0; l0 < n; l0 += C) {
-        float g[12][C];  // d(u, v, w, T)/dx, then /dy, /dz of the chunk's nodes
+        float f[4][C];
 #pragma unroll
-        for (int s = 0; s < 12; ++s) line_chunk<NP, C>(Gs + s * SS, dir, base, step, l0, g[s]);
+        for (int q = 0; q < 4; ++q) line_chunk<NP, C>(Gs + (4 * dir + q) * SS, dir, base, step, l0, f[q]);
 #pragma unroll
         for (int c = 0; c < C; ++c) {
           const int l = l0 + c;
-          float gx[5], gy[5], gz[5];
-          gx[0] = gy[0] = gz[0] = 0.f;  // no flux reads the density gradient
-#pragma unroll
-          for (int q = 1; q < 5; ++q) { gx[q] = g[q - 1][c]; gy[q] = g[3 + q][c]; gz[q] = g[7 + q][c]; }
-          const float vel[3] = {u[l], v[l], w[l]};
-          float tau[6], tq[3];
-          visc_stress(gx, gy, gz, vel, gas.mu, gas.lambda, tau, tq);
-          float fv[4];
-          fv[0] = -m0[l] * tau[0] - m1[l] * tau[3] - m2[l] * tau[4];
-          fv[1] = -m0[l] * tau[3] - m1[l] * tau[1] - m2[l] * tau[5];
-          fv[2] = -m0[l] * tau[4] - m1[l] * tau[5] - m2[l] * tau[2];
-          fv[3] = -m0[l] * tq[0] - m1[l] * tq[1] - m2[l] * tq[2];
 #pragma unroll
           for (int i = 0; i < n; ++i) {
             const float d = lb.dht[l + n * i];
 #pragma unroll
-            for (int q = 1; q < 5; ++q) acc[i][q] = acc[i][q] + d * fv[q - 1];
+            for (int q = 1; q < 5; ++q) acc[i][q] = acc[i][q] + d * f[q - 1][c];
           }
         }
       }
@@ -318,7 +338,6 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
       for (int c = 0; c < 5; ++c) R0[(c * n + l) * Pd + li] = acc[l][c];
     // face fluxes of the node-by-node finish (pulled into L2 at the start of the element), loaded
     // before the barrier, all at once: Gauss-Lobatto surface integral of the faces a node lies on
-    constexpr int NPT = (n3 + 3 * n2 - 1) / (3 * n2);  // nodes per thread
     float ut[NPT][5];
 #pragma unroll
     for (int it = 0; it < NPT; ++it) {
