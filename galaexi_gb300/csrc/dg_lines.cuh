@@ -75,12 +75,12 @@ __host__ __device__ constexpr size_t round16(size_t b) { return (b + 15) / 16 * 
 
 // shared-memory layout of k_volume_lines, one buffer (bytes): region A holds the lifted gradients
 // (12 slots: u, v, w, T in x, y, z; the density gradient is not read) and the primitives rho, u, v,
-// w, p (5 slots), later the three directions' sums; then the metric terms and sJ (10 slots)
+// w, p, 1/rho (6 slots), later the three directions' sums; then the metric terms and sJ (10 slots)
 // and the element's row of E2S.  A slot is n^3 floats in the node order of the state.  The kernel holds two buffers; at n = 8 they
 // take 112 KB, so that two blocks share an SM.
 template <int NP> struct VolLinesSmem {
   static constexpr int SS = NP * NP * NP;  // slot stride (words)
-  static constexpr size_t A = round16(17 * SS * 4 > line_red_words<NP>(5) * 4 ? 17 * SS * 4 : line_red_words<NP>(5) * 4);
+  static constexpr size_t A = round16(18 * SS * 4 > line_red_words<NP>(5) * 4 ? 18 * SS * 4 : line_red_words<NP>(5) * 4);
   static constexpr size_t G = 0, P = 12 * SS * 4, M = A;
   static constexpr size_t E = M + round16(10 * SS * 4);
   static constexpr size_t buffer = E + 64;
@@ -165,7 +165,7 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
   // pulled into L2 ahead of the node-by-node finish that reads them
   const bool upre = rkmode && (n3 % 2 == 0) && bulk_ok(Uio, Ut_tmp, 16);
   const bool fpre = (n2 % 4 == 0) && bulk_ok(Flux, Flux, 16);
-  const unsigned txb = (bulk ? (unsigned)((5 + 10 + (PARAB ? 12 : 0)) * n3 * 4) : 0u) + (ebulk ? 48u : 0u);
+  const unsigned txb = (bulk ? (unsigned)((6 + 10 + (PARAB ? 12 : 0)) * n3 * 4) : 0u) + (ebulk ? 48u : 0u);
   if (tid == 0) { mbar_init(&bar[0]); mbar_init(&bar[1]); }
   __syncthreads();
   // queue the slabs of element e into buffer b; the barrier is armed with the byte count first
@@ -173,7 +173,8 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
     unsigned char* B = smem_raw + (size_t)b * L::buffer;
     if (tid == 0) mbar_arrive_expect(&bar[b], txb);
     const float* Pg = Pvol + (size_t)e * 7 * n3;
-    stage_bytes(B + L::P, Pg, 5 * n3 * 4, bulk, &bar[b]);  // rho, u, v, w, p
+    stage_bytes(B + L::P, Pg, 5 * n3 * 4, bulk, &bar[b]);                  // rho, u, v, w, p
+    stage_bytes(B + L::P + 5 * n3 * 4, Pg + 6 * n3, n3 * 4, bulk, &bar[b]);  // 1/rho
     stage_bytes(B + L::M, Met + (size_t)e * 10 * n3, 10 * n3 * 4, bulk, &bar[b]);
     stage_bytes(B + L::E, E2S + (size_t)e * 12, 48, ebulk, &bar[b]);
     if (upre && tid == 32) {
@@ -201,43 +202,11 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
     }
     unsigned char* B = smem_raw + (size_t)cb * L::buffer;
     float* const red = reinterpret_cast<float*>(B);  // the directions' sums, after the line phase
-    float* const Gs = reinterpret_cast<float*>(B + L::G);
+    const float* const Gs = reinterpret_cast<const float*>(B + L::G);
     const float* const Ps = reinterpret_cast<const float*>(B + L::P);
     const float* const Ms = reinterpret_cast<const float*>(B + L::M);
     const int* const es = reinterpret_cast<const int*>(B + L::E);  // E2S row: side, flip of the six local sides
     if (fpre && tid >= 64 && tid < 70) bulk_prefetch_l2(Flux + (size_t)es[(tid - 64) * 2] * 5 * n2, 5 * n2 * 4);
-    constexpr int NPT = (n3 + 3 * n2 - 1) / (3 * n2);  // nodes per thread in the node-parallel phases
-    if constexpr (PARAB) {
-      // node by node: the viscous stress and heat flux from the lifted gradients, and from them the
-      // contravariant viscous flux of each direction d (EvalTransformedDiffFlux3D with the metric terms
-      // of d), written over the node's gradients: slot 4 d + (momentum x, y, z, energy)
-#pragma unroll
-      for (int it = 0; it < NPT; ++it) {
-        const int node = tid + it * 3 * n2;
-        if (node < n3) {
-          float gx[5], gy[5], gz[5];
-          gx[0] = gy[0] = gz[0] = 0.f;  // no flux reads the density gradient
-#pragma unroll
-          for (int q = 1; q < 5; ++q) {
-            gx[q] = Gs[(q - 1) * SS + node];
-            gy[q] = Gs[(3 + q) * SS + node];
-            gz[q] = Gs[(7 + q) * SS + node];
-          }
-          const float vel[3] = {Ps[SS + node], Ps[2 * SS + node], Ps[3 * SS + node]};
-          float tau[6], tq[3];
-          visc_stress(gx, gy, gz, vel, gas.mu, gas.lambda, tau, tq);
-#pragma unroll
-          for (int d = 0; d < 3; ++d) {
-            const float a0 = Ms[3 * d * SS + node], a1 = Ms[(3 * d + 1) * SS + node], a2 = Ms[(3 * d + 2) * SS + node];
-            Gs[4 * d * SS + node] = -a0 * tau[0] - a1 * tau[3] - a2 * tau[4];
-            Gs[(4 * d + 1) * SS + node] = -a0 * tau[3] - a1 * tau[1] - a2 * tau[5];
-            Gs[(4 * d + 2) * SS + node] = -a0 * tau[4] - a1 * tau[5] - a2 * tau[2];
-            Gs[(4 * d + 3) * SS + node] = -a0 * tq[0] - a1 * tq[1] - a2 * tq[2];
-          }
-        }
-      }
-      __syncthreads();
-    }
     const int dir = tid / n2, li = tid - dir * n2;
     int base, step;
     if (dir == 0) { base = n * li; step = 1; }
@@ -257,13 +226,13 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
       float rho[n], pm[n], aux[n];
       line_load<NP>(Ps, dir, base, step, rho);
       line_load<NP>(Ps + 4 * SS, dir, base, step, pm);  // momentum pressure (p' = p - p_ref in the mixed form)
+      line_load<NP>(Ps + 5 * SS, dir, base, step, aux);  // 1/rho, replaced by the form's auxiliary variable
 #pragma unroll
       for (int l = 0; l < n; ++l) {
         const float pmom = pm[l];
         const float pabs = p_abs(pmom, gas);
         const float E = pabs * gas.sKappaM1 + 0.5f * rho[l] * (u[l] * u[l] + v[l] * v[l] + w[l] * w[l]);
-        const float srho = 1.f / rho[l];  // the same division as the stored 1/rho of the primitives
-        aux[l] = pair_aux<SPLIT, float>(rho[l], u[l], v[l], w[l], E, pabs, srho);
+        aux[l] = pair_aux<SPLIT, float>(rho[l], u[l], v[l], w[l], E, pabs, aux[l]);
         pm[l] = (SPLIT == DG_SPLIT_PI) ? 4.f * pmom : pmom;  // PI: 4p (exact scaling, see below)
       }
 #pragma unroll
@@ -309,21 +278,33 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
       }
     }
     if constexpr (PARAB) {
-      // viscous part: the line direction's contravariant viscous fluxes of the line's nodes, added to
-      // every node of the line with D_hat^T
+      // viscous part: the line direction's contravariant viscous flux of each node (EvalTransformedDiffFlux3D
+      // with the direction's metric terms), added to every node of the line with D_hat^T
 #pragma unroll
       for (int l0 = 0; l0 < n; l0 += C) {
-        float f[4][C];
+        float g[12][C];  // d(u, v, w, T)/dx, then /dy, /dz of the chunk's nodes
 #pragma unroll
-        for (int q = 0; q < 4; ++q) line_chunk<NP, C>(Gs + (4 * dir + q) * SS, dir, base, step, l0, f[q]);
+        for (int s = 0; s < 12; ++s) line_chunk<NP, C>(Gs + s * SS, dir, base, step, l0, g[s]);
 #pragma unroll
         for (int c = 0; c < C; ++c) {
           const int l = l0 + c;
+          float gx[5], gy[5], gz[5];
+          gx[0] = gy[0] = gz[0] = 0.f;  // no flux reads the density gradient
+#pragma unroll
+          for (int q = 1; q < 5; ++q) { gx[q] = g[q - 1][c]; gy[q] = g[3 + q][c]; gz[q] = g[7 + q][c]; }
+          const float vel[3] = {u[l], v[l], w[l]};
+          float tau[6], tq[3];
+          visc_stress(gx, gy, gz, vel, gas.mu, gas.lambda, tau, tq);
+          float fv[4];
+          fv[0] = -m0[l] * tau[0] - m1[l] * tau[3] - m2[l] * tau[4];
+          fv[1] = -m0[l] * tau[3] - m1[l] * tau[1] - m2[l] * tau[5];
+          fv[2] = -m0[l] * tau[4] - m1[l] * tau[5] - m2[l] * tau[2];
+          fv[3] = -m0[l] * tq[0] - m1[l] * tq[1] - m2[l] * tq[2];
 #pragma unroll
           for (int i = 0; i < n; ++i) {
             const float d = lb.dht[l + n * i];
 #pragma unroll
-            for (int q = 1; q < 5; ++q) acc[i][q] = acc[i][q] + d * f[q - 1][c];
+            for (int q = 1; q < 5; ++q) acc[i][q] = acc[i][q] + d * fv[q - 1];
           }
         }
       }
@@ -338,6 +319,7 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
       for (int c = 0; c < 5; ++c) R0[(c * n + l) * Pd + li] = acc[l][c];
     // face fluxes of the node-by-node finish (pulled into L2 at the start of the element), loaded
     // before the barrier, all at once: Gauss-Lobatto surface integral of the faces a node lies on
+    constexpr int NPT = (n3 + 3 * n2 - 1) / (3 * n2);  // nodes per thread
     float ut[NPT][5];
 #pragma unroll
     for (int it = 0; it < NPT; ++it) {
@@ -387,8 +369,8 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
     }
     __syncthreads();
     // output / LSERK-W2 stage in FP64 (vector.f90:163-183), one value per thread in turn: the element's
-    // (5, n^3) record is contiguous, so the loads and stores coalesce; all loads of a thread are issued
-    // before its first store (the state and RK register were pulled into L2 one element ahead)
+    // (5, n^3) record is contiguous, so the loads and stores coalesce; the loads of a thread's values
+    // are issued together (the state and RK register were pulled into L2 one element ahead)
     {
       constexpr int NV = 5 * n3, T3 = 3 * n2, NIT = (NV + T3 - 1) / T3;
       const size_t g0 = (size_t)e * NV;
@@ -399,19 +381,23 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
           if (t < NV) Ut[g0 + t] = (double)Xs[t];
         }
       } else {
-        double tr[NIT], ur[NIT];
+        constexpr int BATCH = 7;
 #pragma unroll
-        for (int q = 0; q < NIT; ++q) {
-          const int t = tid + q * T3;
-          if (t < NV) { tr[q] = Ut_tmp[g0 + t]; ur[q] = Uio[g0 + t]; }
-        }
+        for (int i0 = 0; i0 < NIT; i0 += BATCH) {
+          double tr[BATCH], ur[BATCH];
 #pragma unroll
-        for (int q = 0; q < NIT; ++q) {
-          const int t = tid + q * T3;
-          if (t < NV) {
-            const double utmp = tr[q] * mRKA + (double)Xs[t];
-            Ut_tmp[g0 + t] = utmp;
-            Uio[g0 + t] = ur[q] + utmp * b_dt;
+          for (int q = 0; q < BATCH; ++q) {
+            const int t = tid + (i0 + q) * T3;
+            if (i0 + q < NIT && t < NV) { tr[q] = Ut_tmp[g0 + t]; ur[q] = Uio[g0 + t]; }
+          }
+#pragma unroll
+          for (int q = 0; q < BATCH; ++q) {
+            const int t = tid + (i0 + q) * T3;
+            if (i0 + q < NIT && t < NV) {
+              const double utmp = tr[q] * mRKA + (double)Xs[t];
+              Ut_tmp[g0 + t] = utmp;
+              Uio[g0 + t] = ur[q] + utmp * b_dt;
+            }
           }
         }
       }
