@@ -37,16 +37,22 @@ ALG_FLOPS_N7 = {"prolong": 14.0, "lift": 30 * 8 + 75 + 270 / 8 + 15, "face": 120
                 "volume": 135 * 7 + 115 + 30 * 8 + 60 / 8 + 30}
 ALG_BYTES_N7 = 510.0  # compulsory HBM bytes per DOF-stage of a fully fused implementation (FP64)
 # DRAM traffic and executed FP64 instructions are not measurable inside this process; they come from
-# one ncu capture of the same kernels on the 16^3 case of this workload (2 097 152 DOF; traffic grows
-# with the number of elements, so it is scaled per DOF), taken with the source tree of this file.
-#   FP64 k_volume: dram__bytes_read.sum + dram__bytes_write.sum per DOF of one launch, and the executed
-#   FP64 thread-instructions (DFMA + DADD + DMUL) per DOF
-KVOL_DRAM_BYTES_PER_DOF = (670.293248e6 + 143.461888e6) / 2097152
-KVOL_FP64_INSTR_PER_DOF = 519.0
-KVOL_CAPTURE = "ncu --set full, one k_volume launch, tgv_n7_16cube, 2026-12-03"
-#   mixed form: the four kernels of one stage (k_prolong, k_lift, k_face, k_volume), bytes per DOF
-MIXED_STAGE_DRAM_BYTES_PER_DOF = (84e6 + 72e6 + 165e6 + 129e6 + 145e6 + 9e6 + 419e6 + 127e6) / 2097152
-MIXED_TRAFFIC_SOURCE = "ncu dram__bytes_read+write of the four mixed-form kernels of one stage, tgv_n7_16cube, 2026-12-03"
+# ncu captures of the same kernels on the 16^3 case of this workload (2 097 152 DOF; traffic grows
+# with the number of elements, so it is scaled per DOF), one kernel and one launch per capture:
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum --clock-control none
+#       -k regex:<kernel> -s 3 -c 1 python bench.py [--precision mixed] --workload tgv_n7_16cube_split_pi_roe_br1
+#       --steps 2 --warmup 1 --no-e2e --no-cpu-baseline --no-profile --no-extras
+#   and for k_volume (FP64) the executed DFMA + DADD + DMUL thread-instructions
+#   (sm__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum).
+CAPTURE = "ncu, one kernel and one launch per capture, tgv_n7_16cube, 2026-12-04 19:11 UTC, commit 05fa055"
+_DOF16 = 2097152
+DRAM_BYTES_PER_DOF = {  # read + write per launch
+    "fp64": {"prolong": (84145920 + 196942336) / _DOF16, "lift": (329342464 + 302912256) / _DOF16,
+             "face": (289529856 + 24906496) / _DOF16, "volume": (671186432 + 143390720) / _DOF16},
+    "mixed": {"prolong": (84113664 + 73380608) / _DOF16, "lift": (156297472 + 126710272) / _DOF16,
+              "face": (144754432 + 9628416) / _DOF16, "volume": (426945536 + 124306432) / _DOF16},
+}
+KVOL_FP64_INSTR_PER_DOF = (642252800 + 248512512 + 195297280) / _DOF16
 FP64_ISSUE_PER_CYCLE = 304  # sm__sass_thread_inst_executed_op_dfma_pred_on.sum.peak_sustained (152 SMs x 2)
 TGV_R = 71.42857
 CFL = 0.8  # CFLscale / DFLscale of the reference's TGV regression (regressioncheck/checks/tgv/split/parameter.ini)
@@ -307,7 +313,7 @@ def run_ours(args, world, rank, local):
     # ---- per-kernel timing (CUDA events on the launching stream) for the roofline
     roofline = None
     if not args.no_profile:
-        roofline = profile_roofline(args, op, U, dt, stream, nDOF)
+        roofline = profile_roofline(args, op, U, dt, stream, nDOF, sm_mhz=clk.summary().get("sm_mhz"))
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args.workload)
@@ -412,7 +418,9 @@ def mixed_roofline(op, U0, dt, stream, nDOF):
     return {"bound": "hbm", "unit": "GB/s", "alg_bytes_per_dof_stage": ALG_BYTES_N7_MIXED, "achieved": gbs,
             "peak": hbm_peak, "frac": gbs / hbm_peak if hbm_peak else None,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)",
-            "traffic_per_dof_stage": MIXED_STAGE_DRAM_BYTES_PER_DOF, "traffic_source": MIXED_TRAFFIC_SOURCE,
+            "traffic_per_dof_stage": sum(DRAM_BYTES_PER_DOF["mixed"].values()),
+            "traffic_per_dof_by_kernel": DRAM_BYTES_PER_DOF["mixed"],
+            "traffic_source": "dram__bytes_read+write per DOF of one launch of each kernel (%s)" % CAPTURE,
             "fp32_achieved_tflops": tflops, "fp32_peak_tflops_measured": peak32.value * 1e-3,
             "fp32_frac": tflops / (peak32.value * 1e-3), "kernel_ms": kms}
 
@@ -626,7 +634,7 @@ def adjoint_tgv(stream, steps=200, fd_dirs=0):
     return res
 
 
-def profile_roofline(args, op, U, dt, stream, nDOF):
+def profile_roofline(args, op, U, dt, stream, nDOF, sm_mhz=None):
     import ctypes
     import torch
     from galaexi_gb300 import _native as nat
@@ -646,24 +654,30 @@ def profile_roofline(args, op, U, dt, stream, nDOF):
     mp = measured_peaks()
     hbm_peak = mp.get("hbm_gbs", 6800.0)
     stage_s = kms["stage"] * 1e-3
+    alg_b = ALG_BYTES_N7 if args.precision == "fp64" else ALG_BYTES_N7_MIXED
     roofline = {
-        "kernel": "k_volume (split-form volume + viscous volume + surface integral + Jacobian + RK stage)",
+        "kernel": ("k_volume" if args.precision == "fp64" else "k_volume_lines") +
+                  " (split-form volume + viscous volume + surface integral + Jacobian + RK stage)",
         "bound": "fp64" if args.precision == "fp64" else "fp32",
         "achieved": achieved, "peak": peak * 1e-3, "unit": "TFLOP/s", "frac": achieved / (peak * 1e-3),
         "peak_source": "FMA-chain microkernel measured in this run (no FP64/FP32 CUDA-core peak in MEASURED_PEAKS.json)",
         "alg_flops_per_dof": ALG_FLOPS_N7["volume"],
-        "traffic": KVOL_DRAM_BYTES_PER_DOF * nDOF if args.precision == "fp64" else None,
-        "traffic_source": "dram__bytes_read+write per DOF of one k_volume launch, scaled by nDOF (%s)" % KVOL_CAPTURE,
+        "traffic": DRAM_BYTES_PER_DOF[args.precision]["volume"] * nDOF,
+        "traffic_source": "dram__bytes_read+write per DOF of one launch, scaled by nDOF (%s)" % CAPTURE,
+        # executed FP64 instructions (captured per DOF) over the FP64 issue capacity at the SM clock
+        # sampled during the timed region
         "exec_fp64_issue_frac": (KVOL_FP64_INSTR_PER_DOF * nDOF / (kms["volume"] * 1e-3))
-                                / (FP64_ISSUE_PER_CYCLE * 2.07e9) if args.precision == "fp64" else None,
+                                / (FP64_ISSUE_PER_CYCLE * (sm_mhz or 2070.0) * 1e6) if args.precision == "fp64" else None,
         "kernel_ms": kms,
         "stage": {"alg_flops_per_dof_stage": sum(ALG_FLOPS_N7.values()),
                   "achieved_tflops": sum(ALG_FLOPS_N7.values()) * nDOF / stage_s * 1e-12,
-                  "alg_bytes_per_dof_stage": ALG_BYTES_N7,
-                  "hbm_gbs_alg": ALG_BYTES_N7 * nDOF / stage_s * 1e-9,
+                  "alg_bytes_per_dof_stage": alg_b,
+                  "traffic_per_dof_stage": sum(DRAM_BYTES_PER_DOF[args.precision].values()),
+                  "traffic_per_dof_by_kernel": DRAM_BYTES_PER_DOF[args.precision],
+                  "hbm_gbs_alg": alg_b * nDOF / stage_s * 1e-9,
                   "hbm_peak_gbs": hbm_peak,
                   "hbm_peak_source": "MEASURED_PEAKS.json" if "hbm_gbs" in mp else "fallback 6.8 TB/s",
-                  "hbm_frac_of_measured": ALG_BYTES_N7 * nDOF / stage_s * 1e-9 / hbm_peak},
+                  "hbm_frac_of_measured": alg_b * nDOF / stage_s * 1e-9 / hbm_peak},
         "fp64_peak_tflops_measured": peak64.value * 1e-3,
         "fp32_peak_tflops_measured": peak32.value * 1e-3,
     }

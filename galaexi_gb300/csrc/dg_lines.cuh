@@ -368,7 +368,8 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
       }
     }
     __syncthreads();
-    // output / LSERK-W2 stage in FP64 (vector.f90:163-183), one value per thread in turn: the element's
+    // output / LSERK-W2 stage in FP64 (vector.f90:163-183; the widening of Ut on the integer pipes, which
+    // leaves the FP64 pipe to the two FMAs of the stage), one value per thread in turn: the element's
     // (5, n^3) record is contiguous, so the loads and stores coalesce; the loads of a thread's values
     // are issued together (the state and RK register were pulled into L2 one element ahead)
     {
@@ -378,7 +379,7 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
 #pragma unroll
         for (int it = 0; it < NIT; ++it) {
           const int t = tid + it * T3;
-          if (t < NV) Ut[g0 + t] = (double)Xs[t];
+          if (t < NV) Ut[g0 + t] = f32_to_f64(Xs[t]);
         }
       } else {
         constexpr int BATCH = 7;
@@ -394,7 +395,7 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
           for (int q = 0; q < BATCH; ++q) {
             const int t = tid + (i0 + q) * T3;
             if (i0 + q < NIT && t < NV) {
-              const double utmp = tr[q] * mRKA + (double)Xs[t];
+              const double utmp = tr[q] * mRKA + f32_to_f64(Xs[t]);
               Ut_tmp[g0 + t] = utmp;
               Uio[g0 + t] = ur[q] + utmp * b_dt;
             }
@@ -418,9 +419,28 @@ k_lift_lines(const float* __restrict__ Pvol, const float* __restrict__ Met, cons
   constexpr int P0 = line_pad<NP>(0), P1 = line_pad<NP>(1), P2 = line_pad<NP>(2);
   constexpr int OFF1 = 4 * n * P0, OFF2 = OFF1 + 4 * n * P1;
   __shared__ float red[line_red_words<NP>(4)];
+  __shared__ int es[12];  // E2S row: side, flip of the six local sides
   const int e = blockIdx.x;
   if (e >= nElems) return;
   const int tid = threadIdx.x;
+  // the node-by-node part reads the element's metric terms and, on its faces, both face traces and the
+  // face geometry: they are pulled into L2 while the lines differentiate
+  if (tid < 12) es[tid] = E2S[(size_t)e * 12 + tid];
+  if (tid == 32) {
+    const float* m = Met + (size_t)e * 10 * n3;
+    if (bulk_ok(m, m, 10 * n3 * 4)) bulk_prefetch_l2(m, 10 * n3 * 4);
+  }
+  if (tid >= 64 && tid < 70) {
+    const size_t side = (size_t)E2S[(size_t)e * 12 + (tid - 64) * 2];
+    const float* pm = Pf + side * 6 * n2;
+    const float* ps = Pf + ((size_t)nSides + side) * 6 * n2;
+    const float* fg = Fgeo + side * 10 * n2;
+    if (bulk_ok(pm, ps, 6 * n2 * 4) && bulk_ok(fg, fg, 10 * n2 * 4)) {
+      bulk_prefetch_l2(pm, 6 * n2 * 4);
+      bulk_prefetch_l2(ps, 6 * n2 * 4);
+      bulk_prefetch_l2(fg, 10 * n2 * 4);
+    }
+  }
   {
     const int dir = tid / n2, li = tid - dir * n2;
     int base, stride;
@@ -447,7 +467,7 @@ k_lift_lines(const float* __restrict__ Pvol, const float* __restrict__ Met, cons
       }
   }
   __syncthreads();
-  const int* e2s = E2S + (size_t)e * 12;
+  const int* e2s = es;
   const int liftc[4] = {1, 2, 3, 5};
   for (int node = tid; node < n3; node += blockDim.x) {
     const int i = node % n, j = (node / n) % n, k = node / n2;
