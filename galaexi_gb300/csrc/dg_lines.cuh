@@ -410,6 +410,88 @@ k_volume_lines(const float* __restrict__ Pvol, const float* __restrict__ Gvol, c
   }
 }
 
+// k_prolong_gl: ConsToPrim of the volume and the face traces (ProlongToFace on Gauss-Lobatto nodes:
+// the node's own values; prolongtoface.t90:116-344, GetPrimitiveStateSurface) of the mixed form, as
+// k_prolong computes them (cons_to_prim_mixed; the same bits).  Persistent: a block walks the elements
+// b, b + gridDim.x, ...; each element's FP64 state (one contiguous (5, n^3) record) and its row of E2S
+// are copied into one of two shared-memory buffers by a bulk copy while the block converts the
+// previous element, so that the block does not wait for its loads.  n^3 threads, one per node; even
+// n (the record is then a multiple of 16 bytes).
+template <int NP, typename R, typename S> struct UseProlongGL {
+  static constexpr bool v = sizeof(R) == 4 && std::is_same<S, double>::value && NP % 2 == 0 && NP >= 6 && NP <= 8;
+};
+template <int NP> struct ProlongGLSmem {
+  static constexpr size_t ubytes = (size_t)5 * NP * NP * NP * 8;
+  static constexpr size_t buffer = round16(ubytes) + 64;  // the state, then the E2S row
+  static constexpr size_t bytes = 2 * buffer;
+};
+
+template <int NP>
+__global__ void __launch_bounds__(NP * NP * NP, 3)
+k_prolong_gl(const double* __restrict__ U, const int* __restrict__ E2S, Gas<float> gas, int nElems, int nSides,
+             float* __restrict__ Pvol, float* __restrict__ Uf, float* __restrict__ Pf, int* __restrict__ err) {
+  constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, N = NP - 1;
+  using L = ProlongGLSmem<NP>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ uint64_t bar[2];
+  const int tid = threadIdx.x;
+  if ((int)blockIdx.x >= nElems) return;
+  const bool bulk = bulk_ok(U, E2S, 16);
+  if (tid == 0) { mbar_init(&bar[0]); mbar_init(&bar[1]); }
+  __syncthreads();
+  auto issue = [&](int e, int b) {
+    unsigned char* B = smem_raw + (size_t)b * L::buffer;
+    if (tid == 0) mbar_arrive_expect(&bar[b], bulk ? (unsigned)(L::ubytes + 48) : 0u);
+    stage_bytes(B, U + (size_t)e * 5 * n3, (unsigned)L::ubytes, bulk, &bar[b]);
+    stage_bytes(B + round16(L::ubytes), E2S + (size_t)e * 12, 48, bulk, &bar[b]);
+  };
+  issue(blockIdx.x, 0);
+  int k = 0;
+  for (int e = blockIdx.x; e < nElems; e += gridDim.x, ++k) {
+    const int cb = k & 1;
+    const int en = e + gridDim.x;
+    if (en < nElems) issue(en, cb ^ 1);  // the other buffer was released at the end of the last element
+    __syncthreads();                     // the threads' own copies
+    if (__syncthreads_or(!mbar_wait(&bar[cb], (k >> 1) & 1, err))) {
+      if (en < nElems) mbar_wait(&bar[cb ^ 1], ((k + 1) >> 1) & 1, nullptr);
+      return;
+    }
+    const double* Us = reinterpret_cast<const double*>(smem_raw + (size_t)cb * L::buffer);  // [n3][5]
+    const int* es = reinterpret_cast<const int*>(smem_raw + (size_t)cb * L::buffer + round16(L::ubytes));
+    const int node = tid;
+    const float c[4] = {f64_to_f32_rn(Us[node * 5]), f64_to_f32_rn(Us[node * 5 + 1]), f64_to_f32_rn(Us[node * 5 + 2]),
+                        f64_to_f32_rn(Us[node * 5 + 3])};
+    const double E = Us[node * 5 + 4];
+    float prim[6], srho;
+    cons_to_prim_mixed(c, E, gas, prim, srho);
+    const float uo[5] = {c[0], c[1], c[2], c[3], f64_to_f32_rn(E)};
+    float* P = Pvol + (size_t)e * 7 * n3 + node;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) P[q * n3] = prim[q];
+    P[6 * n3] = srho;
+    // the traces of the faces the node lies on
+    const int i = node % n, j = (node / n) % n, kk = node / n2;
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+      int ls, a, b;
+      if (!node_face<NP>(f, i, j, kk, ls, a, b)) continue;
+      const int side = es[(ls - 1) * 2 + 0], flip = es[(ls - 1) * 2 + 1];
+      int p, q;
+      s2v2_inv(N, a, b, flip, ls, p, q);
+      const int slot = (flip == 0) ? 0 : 1;
+      float* uf = Uf + ((size_t)slot * nSides + side) * 5 * n2 + p + n * q;
+      float* pf = Pf + ((size_t)slot * nSides + side) * 6 * n2 + p + n * q;
+#pragma unroll
+      for (int v = 0; v < 5; ++v) uf[v * n2] = uo[v];
+#pragma unroll
+      for (int v = 0; v < 6; ++v) pf[v * n2] = prim[v];
+    }
+    // this buffer is refilled by the bulk copy of the element after next
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+  }
+}
+
 template <int NP>
 __global__ void __launch_bounds__(3 * NP * NP, 4)
 k_lift_lines(const float* __restrict__ Pvol, const float* __restrict__ Met, const float* __restrict__ Pf,

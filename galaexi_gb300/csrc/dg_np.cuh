@@ -163,7 +163,29 @@ void rhs_front(dg_ctx* ctx, PrecData<R>& P, const S* U, const gx::Gas<R>& gas, c
   if constexpr (std::is_same<R, gx::Dual<1>>::value) L.bcref = ctx->bcref_t.p;  // boundary states, zero tangents
   const gx::DevBasis<R> b = gxc::dev_basis(P, NP);
   const gx::DevBasis<double> bd = gxc::dev_basis(ctx->d, NP);  // FP64 face interpolation in every form
-  gx::k_prolong<NP, R, S><<<grid, NT, 0, st>>>(U, ctx->E2S.p, bd.Lm, bd.Lp, gas, L, P.Pvol.p, P.Uf.p, P.Pf.p);
+  bool persistent = false;
+  if constexpr (gx::UseProlongGL<NP, R, S>::v) {
+    if (!L.gauss) {
+      // mixed form on Gauss-Lobatto nodes: persistent, with the next element's state in flight
+      constexpr size_t sm = gx::ProlongGLSmem<NP>::bytes;
+      if (ctx->prolong_grid == 0) {
+        int dev = 0, nsm = 0, occ = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gx::k_prolong_gl<NP>, NP * NP * NP, sm) == cudaSuccess &&
+            occ > 0)
+          ctx->prolong_grid = nsm * occ;
+        else
+          ctx->prolong_grid = ctx->nElems;  // one element per block
+      }
+      const int pg = ctx->nElems < ctx->prolong_grid ? ctx->nElems : ctx->prolong_grid;
+      gx::k_prolong_gl<NP><<<pg, NP * NP * NP, sm, st>>>(U, ctx->E2S.p, gas, ctx->nElems, ctx->nSides, P.Pvol.p,
+                                                          P.Uf.p, P.Pf.p, ctx->kerr.p);
+      persistent = true;
+    }
+  }
+  if (!persistent)
+    gx::k_prolong<NP, R, S><<<grid, NT, 0, st>>>(U, ctx->E2S.p, bd.Lm, bd.Lp, gas, L, P.Pvol.p, P.Uf.p, P.Pf.p);
   ctx->launches++;
   const long long nbc = (long long)ctx->nBCSides * NP * NP;
   if (ctx->cfg.parabolic && nbc > 0) {
