@@ -1,4 +1,5 @@
-// Kernels of the mixed (FP32) form with one thread per 1D line of an element.
+// Kernels of the mixed (FP32) form on Gauss-Lobatto nodes: two with one thread per 1D line of an
+// element, and a prolongation with one thread per node.
 //
 // k_volume_lines: the volume kernel of the split form.  VolInt_splitForm (src/dg/volint.f90:211-353,
 // SplitVolumeFlux* of splitflux.f90:145-730) sums, for every node i of a line, DVolSurf(l,i) *
@@ -15,8 +16,17 @@
 // (constant-bank operands of the FMAs).  The three directions' sums of a node meet in shared memory
 // (padded so that neither the line-ordered writes nor the node-ordered reads conflict at N = 7), and
 // the block's threads then finish node by node: the Gauss-Lobatto surface integral of the face fluxes
-// (SurfIntCons, surfint.t90:352-586), -1, the Jacobian and the output or LSERK-W2 stage update
-// (vector.f90:163-183) in FP64.
+// (SurfIntCons, surfint.t90:352-586), -1 and the Jacobian; last, one value per thread in turn, the
+// output or the LSERK-W2 stage update (vector.f90:163-183) in FP64.
+// The kernel is persistent (a block walks the elements b, b + gridDim.x, ...) and double-buffered: the
+// slabs of the block's next element (primitives, metric terms, lifted gradients, each contiguous in
+// memory, and the element's row of E2S) are copied into shared memory by the tensor memory
+// accelerator (cp.async.bulk, dg_tma.cuh) while the block computes the current one, and its FP64 state
+// and RK register are pulled into L2 (cp.async.bulk.prefetch), so that the few warps of a block (two
+// blocks of 168 registers per SM at n = 8) seldom wait for memory.  Where a slab is not 16-byte aligned
+// (odd n) the threads copy it.
+//
+// k_prolong_gl: ConsToPrim and the face traces, persistent and double-buffered the same way.
 //
 // k_lift_lines: the BR1 lifting (Lifting_BR1, lifting_br1.t90:47-167, strong non-conservative form,
 // Gauss-Lobatto nodes).  The line threads differentiate u, v, w and T along their line (D(i,l) as
@@ -25,13 +35,10 @@
 // node lies on (0.5 SurfElem (P_slave - P_master) n L_hat sJ, lifting_fillflux.t90:39-103, 212-256,
 // surfint.t90:591-725) and writes the gradients and their face traces (ProlongToFaceLifting: on
 // Gauss-Lobatto nodes the node's own value).  The density gradient, which no flux reads, is not formed.
+// A block is one element; the metric terms and face data of its finish are pulled into L2 while its
+// lines differentiate.
 //
-// A block is one element's 3 n^2 lines.  Its input slabs (the element's primitives, metric terms,
-// lifted gradients and FP64 state / RK register: each one contiguous in memory) are copied into shared
-// memory by the tensor memory accelerator (cp.async.bulk, dg_tma.cuh) at the start of the block, all
-// at once, so that the few warps of a block wait once for their data instead of once per dependent
-// load; where a slab is not 16-byte aligned (N = 4, 6) the threads copy it.
-// Registers: ~9 n + 5 n values per thread, so the kernels are instantiated for n <= 8, the volume
+// Registers: ~9 n + 5 n values per thread, so the line kernels are instantiated for n <= 8, the volume
 // kernel for the forms whose pair flux needs no momenta (SD, KG, PI).
 #pragma once
 #include "dg_physics.cuh"
