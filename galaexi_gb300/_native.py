@@ -103,6 +103,7 @@ _SIGS = {
     "dg_fill_ini": (_I, [_I, _P, _I, ctypes.c_longlong, _P, _D, _D, _D, _P]),
     "dg_profile_stage": (_I, [_P, _P, _P, _D, _I, _DP, _P]),
     "dg_measure_fma_peak": (_I, [_I, _DP]),
+    "dg_selftest_bulk_wait": (_I, [ctypes.c_longlong, _DP]),
     "dg_set_pressure_offset": (_I, [_P, _D]),
     "dg_calc_timestep_noalloc": (_I, [_I, _I, _I, _I, _D, _D, _D, _P, _P, _P, _P, _P, _D, _D, _DP, _P]),
 }

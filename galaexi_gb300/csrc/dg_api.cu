@@ -10,6 +10,7 @@
 #include "../../include/galaexi_gb300.h"
 #include "dg_host.h"
 #include "dg_ctx.h"
+#include "dg_tma.cuh"
 
 using gxh::set_error;
 
@@ -145,6 +146,21 @@ __global__ void __launch_bounds__(256) k_fma_peak(T* out, int iters, T a, T b) {
 #pragma unroll
   for (int c = 0; c < 8; ++c) s += x[c];
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+// A bulk-copy wait that runs out: the barrier is armed for 16 bytes that no copy delivers (none is
+// issued) and every thread of the block waits with `limit` polls, then the block returns.  Records
+// the wait's duration (%globaltimer, ns) of thread 0.
+__global__ void k_selftest_bulk_wait(long long limit, int* err, long long* ns) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) gx::mbar_init(&bar);
+  __syncthreads();
+  if (threadIdx.x == 0) gx::mbar_arrive_expect(&bar, 16);
+  long long t0, t1;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0)::"memory");
+  gx::mbar_wait(&bar, 0, err, limit);
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1)::"memory");
+  if (threadIdx.x == 0) *ns = t1 - t0;
 }
 
 template <typename T>
@@ -358,6 +374,25 @@ int rev_stage(dg_ctx* ctx, int stage, double dt, const double* X, double* Ubar, 
 }  // namespace
 
 extern "C" {
+
+int dg_selftest_bulk_wait(long long polls, double* seconds) {
+  if (polls < 1 || !seconds) { set_error("dg_selftest_bulk_wait: bad argument"); return DG_ERR_ARG; }
+  gxc::DBuf<int> err;
+  gxc::DBuf<long long> ns;
+  if (!err.alloc(1) || !ns.alloc(1)) { set_error("dg_selftest_bulk_wait: device allocation failed"); return DG_ERR_CUDA; }
+  CUDA_TRY(cudaMemset(err.p, 0, sizeof(int)), "cudaMemset");
+  k_selftest_bulk_wait<<<1, 64>>>(polls, err.p, ns.p);
+  CUDA_TRY(cudaGetLastError(), "k_selftest_bulk_wait launch");
+  CUDA_TRY(cudaDeviceSynchronize(), "k_selftest_bulk_wait");
+  int f = 0;
+  long long t = 0;
+  CUDA_TRY(cudaMemcpy(&f, err.p, sizeof(int), cudaMemcpyDeviceToHost), "read error flag");
+  CUDA_TRY(cudaMemcpy(&t, ns.p, sizeof(long long), cudaMemcpyDeviceToHost), "read duration");
+  *seconds = t * 1e-9;
+  if (!f) return DG_OK;
+  set_error("a kernel's wait for its bulk copies into shared memory ran out (self-test)");
+  return DG_ERR_TIMEOUT;
+}
 
 int dg_measure_fma_peak(int precision, double* gflops) {
   if (!gflops) { set_error("null output"); return DG_ERR_ARG; }

@@ -57,13 +57,14 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, unsigned phase) {
   return done != 0;
 }
 
-// wait for the barrier's phase; false (and *err set) if the copies did not complete in time
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned phase, int* err) {
-  constexpr long long kLimit = 1ll << 24;  // try_wait suspends between polls: ~a second in total
-  for (long long it = 0; it < kLimit; ++it)
+// wait for the barrier's phase; false (and *err set) if the copies did not complete within `limit`
+// polls (try_wait suspends between polls)
+constexpr long long kTmaWaitLimit = 1ll << 24;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned phase, int* err, long long limit = kTmaWaitLimit) {
+  for (long long it = 0; it < limit; ++it)
     if (mbar_test(bar, phase)) return true;
   if (err) atomicExch(err, kTmaTimeout);
-  for (long long it = 0; it < kLimit; ++it)
+  for (long long it = 0; it < limit; ++it)
     if (mbar_test(bar, phase)) break;
   return false;
 }

@@ -275,6 +275,12 @@ INTERFACE
     REAL(C_DOUBLE), INTENT(OUT) :: gflops
   END FUNCTION dg_measure_fma_peak
 
+  INTEGER(C_INT) FUNCTION dg_selftest_bulk_wait(polls, seconds) BIND(C,NAME='dg_selftest_bulk_wait')
+    IMPORT :: C_INT, C_LONG_LONG, C_DOUBLE
+    INTEGER(C_LONG_LONG), VALUE :: polls
+    REAL(C_DOUBLE), INTENT(OUT) :: seconds
+  END FUNCTION dg_selftest_bulk_wait
+
   INTEGER(C_LONG_LONG) FUNCTION dg_kernel_launch_count(ctx) BIND(C,NAME='dg_kernel_launch_count')
     IMPORT :: C_LONG_LONG, C_PTR
     TYPE(C_PTR), VALUE :: ctx

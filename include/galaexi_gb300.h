@@ -282,6 +282,14 @@ int dg_set_pressure_offset(dg_ctx* ctx, double p_ref);
 int dg_profile_stage(dg_ctx* ctx, double* d_U, double* d_Ut_tmp, double dt, int reps, double* ms_out, void* stream);
 int dg_measure_fma_peak(int precision, double* gflops);
 
+/* Self-test of the bounded waits of the kernels that stage data by bulk copies (no counterpart in
+ * the reference).  Launches one block that arms a shared-memory barrier for 16 bytes that no copy
+ * delivers and waits for it with `polls` polls, as those kernels wait for their copies; the wait runs
+ * out, the block records the timeout and returns.  Returns DG_ERR_TIMEOUT (the status those kernels'
+ * callers report) with *seconds = the duration of the wait, DG_OK if the wait completed (which
+ * would be a defect), or an error code. */
+int dg_selftest_bulk_wait(long long polls, double* seconds);
+
 /* Number of kernels this context launched since creation (for accounting). */
 long long dg_kernel_launch_count(const dg_ctx* ctx);
 
