@@ -924,15 +924,15 @@ int dg_adjoint_forward(dg_ctx* ctx, double t0, double dt, int nSteps, const doub
   if (!ctx->W.p && !(ctx->W.alloc(S) && ctx->K.alloc(S))) { set_error("cudaMalloc adjoint work states"); return DG_ERR_ALLOC; }
   const size_t slots_max = budget_bytes / bytes;
   // plan 1: every stage input; plan 2: segment starts + the stage inputs of one segment (one extra
-  // forward sweep); plan 3: segment starts + step starts of one segment + the stage inputs of one step
-  // (two extra forward sweeps)
+  // forward sweep; the first stage input of a segment is its start, stored once); plan 3: segment
+  // starts + step starts of one segment + the stage inputs of one step (two extra forward sweeps)
   int plan = 0, k = 0, nSeg = 0;
   size_t slots = 0;
   if ((size_t)5 * nSteps <= slots_max) { plan = 1; k = nSteps; nSeg = 1; slots = (size_t)5 * nSteps; }
   else {
     size_t best = (size_t)-1; int bk = 0;
     for (int kk = 1; kk <= nSteps; ++kk) {
-      const size_t need = (size_t)((nSteps + kk - 1) / kk) + (size_t)5 * kk;
+      const size_t need = (size_t)((nSteps + kk - 1) / kk) + (size_t)5 * kk - 1;
       if (need < best) { best = need; bk = kk; }
     }
     if (best <= slots_max) { plan = 2; k = bk; nSeg = (nSteps + bk - 1) / bk; slots = best; }
@@ -966,7 +966,7 @@ int dg_adjoint_forward(dg_ctx* ctx, double t0, double dt, int nSteps, const doub
     for (int stage = 1; stage <= 5; ++stage) {
       double* slot = nullptr;
       if (plan == 1) slot = T.store.p + ((size_t)nstep * 5 + stage - 1) * S;
-      else if (plan == 2 && nstep >= nL) slot = buf + ((size_t)(nstep - nL) * 5 + stage - 1) * S;
+      else if (plan == 2 && nstep >= nL && (nstep > nL || stage > 1)) slot = T.p2_input(nSeg - 1, nstep, stage, buf);
       else if (plan == 3 && nstep == nSteps - 1) slot = buf + ((size_t)k + stage - 1) * S;
       if (slot) CUDA_TRY(cudaMemcpyAsync(slot, W, bytes, cudaMemcpyDeviceToDevice, st), "stage checkpoint");
       if (int rc = fwd_stage(ctx, stage, dt, W, K, st)) return rc;
@@ -1000,7 +1000,7 @@ int dg_adjoint_reverse(dg_ctx* ctx, double* d_Ubar, double* mu_bar, void* stream
         rc = rev_stage(ctx, stage, dt, T.store.p + ((size_t)nstep * 5 + stage - 1) * S, d_Ubar, Kbar, st);
   } else {
     double* seg = T.store.p;
-    double* buf = T.store.p + (size_t)T.nSeg * S;  // plan 2: 5k stage inputs; plan 3: k step starts + 5 stage inputs
+    double* buf = T.store.p + (size_t)T.nSeg * S;  // plan 2: 5k - 1 stage inputs; plan 3: k step starts + 5 stage inputs
     for (int sg = T.nSeg - 1; sg >= 0 && rc == DG_OK; --sg) {
       const int n0 = T.seg_start(sg), n1 = T.seg_end(sg);
       const bool last = sg == T.nSeg - 1;  // recorded by the forward sweep
@@ -1012,9 +1012,9 @@ int dg_adjoint_reverse(dg_ctx* ctx, double* d_Ubar, double* mu_bar, void* stream
         if (T.plan == 3)
           CUDA_TRY(cudaMemcpyAsync(buf + (size_t)(nstep - n0) * S, W, bytes, cudaMemcpyDeviceToDevice, st), "step start");
         for (int stage = 1; stage <= 5 && rc == DG_OK; ++stage) {
-          if (T.plan == 2)
-            CUDA_TRY(cudaMemcpyAsync(buf + ((size_t)(nstep - n0) * 5 + stage - 1) * S, W, bytes, cudaMemcpyDeviceToDevice,
-                                     st), "stage input");
+          if (T.plan == 2 && (nstep > n0 || stage > 1))  // the segment's first input is its start
+            CUDA_TRY(cudaMemcpyAsync(T.p2_input(sg, nstep, stage, buf), W, bytes, cudaMemcpyDeviceToDevice, st),
+                     "stage input");
           rc = fwd_stage(ctx, stage, dt, W, K2.p, st);
         }
       }
@@ -1038,7 +1038,7 @@ int dg_adjoint_reverse(dg_ctx* ctx, double* d_Ubar, double* mu_bar, void* stream
           continue;
         }
         for (int stage = 5; stage >= 1 && rc == DG_OK; --stage) {
-          X = buf + ((size_t)(nstep - n0) * 5 + stage - 1) * S;
+          X = T.p2_input(sg, nstep, stage, buf);
           rc = rev_stage(ctx, stage, dt, X, d_Ubar, Kbar, st);
         }
       }

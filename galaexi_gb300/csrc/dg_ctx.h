@@ -88,6 +88,12 @@ struct AdjTape {
   int seg_of(int nstep) const { return nstep < r ? 0 : 1 + (nstep - r) / k; }
   int seg_start(int sg) const { return sg == 0 ? 0 : r + (sg - 1) * k; }
   int seg_end(int sg) const { return sg == nSeg - 1 ? nSteps : seg_start(sg + 1); }
+  // plan 2: the slot of the input of `stage` of step `nstep` in segment sg; the segment's first input
+  // is its start checkpoint, the others fill the segment buffer `buf` (5 k - 1 slots)
+  double* p2_input(int sg, int nstep, int stage, double* buf) const {
+    const size_t j = (size_t)(nstep - seg_start(sg)) * 5 + stage - 1;
+    return j == 0 ? store.p + (size_t)sg * state : buf + (j - 1) * state;
+  }
 };
 
 struct dg_ctx {

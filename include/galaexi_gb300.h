@@ -248,8 +248,8 @@ int dg_rhs_vjp(dg_ctx* ctx, double t, const double* d_U, const double* d_Utbar, 
 /* Discrete adjoint of nSteps LSERK-W2 steps with fixed dt from d_U0.
  * dg_adjoint_forward runs the window and records checkpoints in device memory of at most
  * budget_bytes: every stage input if that fits (plan 1), else segment starts every k steps plus the
- * stage inputs of one segment, recomputed during the reverse sweep (plan 2, one extra forward sweep
- * over all segments but the last), else segment starts plus the step starts of one segment plus one
+ * stage inputs of one segment but its first (which is the segment start), recomputed during the
+ * reverse sweep (plan 2, one extra forward sweep over all segments but the last), else segment starts plus the step starts of one segment plus one
  * step's stage inputs (plan 3, two extra sweeps); the last segment's checkpoints are recorded by the
  * forward run itself.  *plan_out (if not null) receives the plan.  d_U_final (if not null) receives
  * the end state.
