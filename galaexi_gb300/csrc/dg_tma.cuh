@@ -4,8 +4,8 @@
 //
 // A copy needs a 16-byte aligned source and destination and a size that is a multiple of 16 bytes;
 // bulk_ok() checks that.  One thread arms the barrier with the total byte count of its copies and
-// issues them; every thread then waits for the barrier's phase with an iteration limit.  A wait that
-// runs out of iterations records kTmaTimeout in *err (read back by the host, which reports
+// issues them; every thread then waits for the barrier's phase with a limit on its polls.  A wait that
+// runs out of polls records kTmaTimeout in *err (read back by the host, which reports
 // DG_ERR_TIMEOUT), waits once more with a limit for the copies still in flight (so that they do not
 // land in shared memory the block no longer owns) and reports failure; the caller returns.
 #pragma once
@@ -58,8 +58,10 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, unsigned phase) {
 }
 
 // wait for the barrier's phase; false (and *err set) if the copies did not complete within `limit`
-// polls (try_wait suspends between polls)
-constexpr long long kTmaWaitLimit = 1ll << 24;
+// polls.  try_wait suspends the thread between polls until the phase completes or a time limit of
+// the hardware passes (7.5 us per poll measured on GB300 for a phase that never completes), so the
+// default limit gives up after about a second, far beyond the microseconds the copies take
+constexpr long long kTmaWaitLimit = 1ll << 17;
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned phase, int* err, long long limit = kTmaWaitLimit) {
   for (long long it = 0; it < limit; ++it)
     if (mbar_test(bar, phase)) return true;
