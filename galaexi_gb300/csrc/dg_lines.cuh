@@ -520,14 +520,19 @@ k_lift_lines(const float* __restrict__ Pvol, const float* __restrict__ Met, cons
     if (bulk_ok(m, m, 10 * n3 * 4)) bulk_prefetch_l2(m, 10 * n3 * 4);
   }
   if (tid >= 64 && tid < 70) {
+    // the rows the finish reads: u, v, w (rows 1-3) and T (row 5) of both traces, the normal (rows
+    // 0-2) and SurfElem (row 9) of the geometry
     const size_t side = (size_t)E2S[(size_t)e * 12 + (tid - 64) * 2];
     const float* pm = Pf + side * 6 * n2;
     const float* ps = Pf + ((size_t)nSides + side) * 6 * n2;
     const float* fg = Fgeo + side * 10 * n2;
-    if (bulk_ok(pm, ps, 6 * n2 * 4) && bulk_ok(fg, fg, 10 * n2 * 4)) {
-      bulk_prefetch_l2(pm, 6 * n2 * 4);
-      bulk_prefetch_l2(ps, 6 * n2 * 4);
-      bulk_prefetch_l2(fg, 10 * n2 * 4);
+    if (bulk_ok(pm, ps, n2 * 4) && bulk_ok(fg, fg, n2 * 4)) {
+      bulk_prefetch_l2(pm + n2, 3 * n2 * 4);
+      bulk_prefetch_l2(pm + 5 * n2, n2 * 4);
+      bulk_prefetch_l2(ps + n2, 3 * n2 * 4);
+      bulk_prefetch_l2(ps + 5 * n2, n2 * 4);
+      bulk_prefetch_l2(fg, 3 * n2 * 4);
+      bulk_prefetch_l2(fg + 9 * n2, n2 * 4);
     }
   }
   {
