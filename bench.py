@@ -44,13 +44,14 @@ ALG_BYTES_N7 = 510.0  # compulsory HBM bytes per DOF-stage of a fully fused impl
 #       --steps 2 --warmup 1 --no-e2e --no-cpu-baseline --no-profile --no-extras
 #   and for k_volume (FP64) the executed DFMA + DADD + DMUL thread-instructions
 #   (sm__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum).
-CAPTURE = "ncu, one kernel and one launch per capture, tgv_n7_16cube, 2026-12-04 19:11 UTC, commit 05fa055"
+CAPTURE = {"fp64": "ncu, one kernel and one launch per capture, tgv_n7_16cube, 2026-12-04 19:11 UTC, commit 05fa055",
+           "mixed": "ncu, one kernel and one launch per capture, tgv_n7_16cube, 2026-12-04 20:25 UTC, commit c00486e"}
 _DOF16 = 2097152
 DRAM_BYTES_PER_DOF = {  # read + write per launch
     "fp64": {"prolong": (84145920 + 196942336) / _DOF16, "lift": (329342464 + 302912256) / _DOF16,
              "face": (289529856 + 24906496) / _DOF16, "volume": (671186432 + 143390720) / _DOF16},
-    "mixed": {"prolong": (84113664 + 73380608) / _DOF16, "lift": (156297472 + 126710272) / _DOF16,
-              "face": (144754432 + 9628416) / _DOF16, "volume": (426945536 + 124306432) / _DOF16},
+    "mixed": {"prolong": (84130048 + 69619200) / _DOF16, "lift": (157313792 + 127674624) / _DOF16,
+              "face": (144744960 + 9332992) / _DOF16, "volume": (427753216 + 123999744) / _DOF16},
 }
 KVOL_FP64_INSTR_PER_DOF = (642252800 + 248512512 + 195297280) / _DOF16
 FP64_ISSUE_PER_CYCLE = 304  # sm__sass_thread_inst_executed_op_dfma_pred_on.sum.peak_sustained (152 SMs x 2)
@@ -420,7 +421,7 @@ def mixed_roofline(op, U0, dt, stream, nDOF):
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)",
             "traffic_per_dof_stage": sum(DRAM_BYTES_PER_DOF["mixed"].values()),
             "traffic_per_dof_by_kernel": DRAM_BYTES_PER_DOF["mixed"],
-            "traffic_source": "dram__bytes_read+write per DOF of one launch of each kernel (%s)" % CAPTURE,
+            "traffic_source": "dram__bytes_read+write per DOF of one launch of each kernel (%s)" % CAPTURE["mixed"],
             "fp32_achieved_tflops": tflops, "fp32_peak_tflops_measured": peak32.value * 1e-3,
             "fp32_frac": tflops / (peak32.value * 1e-3), "kernel_ms": kms}
 
@@ -663,7 +664,7 @@ def profile_roofline(args, op, U, dt, stream, nDOF, sm_mhz=None):
         "peak_source": "FMA-chain microkernel measured in this run (no FP64/FP32 CUDA-core peak in MEASURED_PEAKS.json)",
         "alg_flops_per_dof": ALG_FLOPS_N7["volume"],
         "traffic": DRAM_BYTES_PER_DOF[args.precision]["volume"] * nDOF,
-        "traffic_source": "dram__bytes_read+write per DOF of one launch, scaled by nDOF (%s)" % CAPTURE,
+        "traffic_source": "dram__bytes_read+write per DOF of one launch, scaled by nDOF (%s)" % CAPTURE[args.precision],
         # executed FP64 instructions (captured per DOF) over the FP64 issue capacity at the SM clock
         # sampled during the timed region
         "exec_fp64_issue_frac": (KVOL_FP64_INSTR_PER_DOF * nDOF / (kms["volume"] * 1e-3))
