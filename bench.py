@@ -80,7 +80,7 @@ def parse():
                     help="steps of the adjoint window (default 200 for the N=5 case, 50 for --only scale64)")
     ap.add_argument("--curved-ne", type=int, default=32,
                     help="elements per direction of the curved-box case (32; smaller for profiling)")
-    ap.add_argument("--only", default=None, choices=["adjoint", "mixed_tgv", "mixed_curved", "scale64"],
+    ap.add_argument("--only", default=None, choices=["adjoint", "mixed_tgv", "mixed_curved", "scale64", "vortex"],
                     help="run one of the extra measurements alone and print its JSON (profiling runs)")
     args = ap.parse_args()
     args.steps_given = any(a == "--steps" or a.startswith("--steps=") for a in sys.argv[1:])
@@ -323,6 +323,8 @@ def run_ours(args, world, rank, local):
         # the mixed form over the workload's 200 steps, with its own roofline
         extras["mixed_vs_fp64"] = mixed_vs_fp64_tgv(args.workload, 200, stream, roofline=not args.no_profile)
         extras["mixed_vs_fp64_curved_br2"] = mixed_vs_fp64_curved_br2(stream)
+        # the Euler vortex case (N=3 Gauss, weak, LF, 8^3): 100 steps against the exact solution
+        extras["vortex_c1"] = vortex_c1(stream)
         # the discrete adjoint of 200 steps on the N=5 16^3 TGV, checked along 16 seeded directions
         extras["adjoint"] = adjoint_tgv(stream, steps=args.adjoint_steps or 200, fd_dirs=args.adjoint_fd)
         if not args.no_scale64:
@@ -478,6 +480,32 @@ def mixed_vs_fp64_curved_br2(stream, steps=500, ne=32):
            "reference": "FP64 path of this library (matches the oracle to <=1e-12 per evaluation)"}
     for op in ops.values():
         op.close()
+    return res
+
+
+def vortex_c1(stream, steps=100):
+    """Euler, Gauss N=3, weak form, Lax-Friedrichs, 8^3 elements on [0,10]^3, Shu vortex (beta 5,
+    half-width 1, advected with (1,1,0); exactfunc.f90:482-502), `steps` LSERK steps at CFL 0.9 from
+    the exact state: DOF-stage/s and the relative L2 distance of the end state from the exact
+    advected vortex (the discretisation error of 4 nodes per element and direction)."""
+    import torch
+    import galaexi_gb300 as gx
+    from galaexi_gb300 import _native as nat
+    m = gx.Mesh(3, 1, 8, 8, 8, (0.0,) * 3, (10.0,) * 3)
+    prm = [1, 1, 1, 0, 1, 5, 5, 0, 0, 0, 1, 5, 1]  # RefState, IniCenter, IniAxis, beta, half-width
+    U0 = gx.fill_ini(m, nat.DG_EXACTFUNC_SHU_VORTEX, prm)
+    op = gx.DG(gx.config(N=3, NodeType="gauss", Riemann="lf"), m)
+    U = torch.from_numpy(U0).cuda()
+    dt, _ = op.CalcTimeStep(U, 0.9)
+    W, K = U.clone(), torch.zeros_like(U)
+    op.TimeStepByLSERKW2(0.0, dt, W, K)  # warm-up
+    K.zero_()
+    ms, _ = timed(lambda: op.TimeStepByLSERKW2(0.0, dt, U, K, nSteps=steps), stream)
+    exact = torch.from_numpy(gx.fill_ini(m, nat.DG_EXACTFUNC_SHU_VORTEX, prm, t=steps * dt)).cuda()
+    res = {"workload": "vortex_n3_gauss_8cube_weak_lf", "nDOF": m.nDOF, "steps": steps, "dt": dt,
+           "dof_stage_per_s": m.nDOF * 5 * steps / (ms * 1e-3), "ms_per_step": ms / steps,
+           "l2_rel_vs_exact": float((U - exact).norm() / exact.norm())}
+    op.close()
     return res
 
 
@@ -699,6 +727,8 @@ def main():
             res = scale_c5(stream, steps=args.steps if args.steps_given else 100, adj_steps=args.adjoint_steps or 50)
         elif args.only == "mixed_tgv":
             res = mixed_vs_fp64_tgv(args.workload, args.steps, stream)
+        elif args.only == "vortex":
+            res = vortex_c1(stream)
         else:
             res = mixed_vs_fp64_curved_br2(stream, steps=args.steps, ne=args.curved_ne)
         if rank == 0:
