@@ -120,7 +120,6 @@ struct dg_ctx {
   long long launches = 0;
   int lines_grid = 0;      // blocks of the persistent line volume kernel (SMs x resident blocks), on first use
   int prolong_grid = 0;    // blocks of the persistent prolongation kernel of the mixed form, on first use
-  int lift_grid = 0;       // blocks of the persistent lifting line kernel, on first use
   gxc::DBuf<int> S2E;      // [side][5]: master elem, master local side, slave elem, slave local side, flip (0-based)
   gxc::DBuf<double> wq;    // 1D quadrature weights (n)
   // tangent-linear operator (R = S = Dual<1>), set up on first use

@@ -499,160 +499,126 @@ k_prolong_gl(const double* __restrict__ U, const int* __restrict__ E2S, Gas<floa
   }
 }
 
-// shared memory of k_lift_lines, one buffer (bytes): the element's u, v, w, T (4 slots of n^3
-// floats) and its row of E2S; the kernel holds two
-template <int NP> struct LiftLinesSmem {
-  static constexpr size_t slots = (size_t)4 * NP * NP * NP * 4;
-  static constexpr size_t buffer = round16(slots) + 64;
-  static constexpr size_t bytes = 2 * buffer;
-};
-
 template <int NP>
 __global__ void __launch_bounds__(3 * NP * NP, 4)
 k_lift_lines(const float* __restrict__ Pvol, const float* __restrict__ Met, const float* __restrict__ Pf,
              const float* __restrict__ Fgeo, const int* __restrict__ E2S, LiftBasis<NP> lb, int nElems, int nSides,
-             float* __restrict__ Gvol, float* __restrict__ Gf, int* __restrict__ err) {
+             float* __restrict__ Gvol, float* __restrict__ Gf) {
   constexpr int n = NP, n2 = NP * NP, n3 = NP * NP * NP, N = NP - 1;
   constexpr int P0 = line_pad<NP>(0), P1 = line_pad<NP>(1), P2 = line_pad<NP>(2);
   constexpr int OFF1 = 4 * n * P0, OFF2 = OFF1 + 4 * n * P1;
-  using L = LiftLinesSmem<NP>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ float red[line_red_words<NP>(4)];
-  __shared__ uint64_t bar[2];
+  __shared__ int es[12];  // E2S row: side, flip of the six local sides
+  const int e = blockIdx.x;
+  if (e >= nElems) return;
   const int tid = threadIdx.x;
-  if ((int)blockIdx.x >= nElems) return;
-  // bulk copies where an element's slots start 16-byte aligned (n^3 a multiple of 4); else the
-  // threads copy
-  const bool bulk = (n3 % 4 == 0) && bulk_ok(Pvol, E2S, 16);
-  const unsigned txb = bulk ? (unsigned)(4 * n3 * 4 + 48) : 0u;
-  if (tid == 0) { mbar_init(&bar[0]); mbar_init(&bar[1]); }
-  __syncthreads();
-  // queue element e's u, v, w, T and E2S row into buffer b, and pull its metric terms into L2
-  auto issue = [&](int e, int b) {
-    unsigned char* B = smem_raw + (size_t)b * L::buffer;
-    if (tid == 0) mbar_arrive_expect(&bar[b], txb);
+  // the node-by-node part reads the element's metric terms and, on its faces, both face traces and the
+  // face geometry: they are pulled into L2 while the lines differentiate
+  if (tid < 12) es[tid] = E2S[(size_t)e * 12 + tid];
+  if (tid == 32) {
+    const float* m = Met + (size_t)e * 10 * n3;
+    if (bulk_ok(m, m, 10 * n3 * 4)) bulk_prefetch_l2(m, 10 * n3 * 4);
+  }
+  if (tid >= 64 && tid < 70) {
+    // the rows the finish reads: u, v, w (rows 1-3) and T (row 5) of both traces, the normal (rows
+    // 0-2) and SurfElem (row 9) of the geometry
+    const size_t side = (size_t)E2S[(size_t)e * 12 + (tid - 64) * 2];
+    const float* pm = Pf + side * 6 * n2;
+    const float* ps = Pf + ((size_t)nSides + side) * 6 * n2;
+    const float* fg = Fgeo + side * 10 * n2;
+    if (bulk_ok(pm, ps, n2 * 4) && bulk_ok(fg, fg, n2 * 4)) {
+      bulk_prefetch_l2(pm + n2, 3 * n2 * 4);
+      bulk_prefetch_l2(pm + 5 * n2, n2 * 4);
+      bulk_prefetch_l2(ps + n2, 3 * n2 * 4);
+      bulk_prefetch_l2(ps + 5 * n2, n2 * 4);
+      bulk_prefetch_l2(fg, 3 * n2 * 4);
+      bulk_prefetch_l2(fg + 9 * n2, n2 * 4);
+    }
+  }
+  {
+    const int dir = tid / n2, li = tid - dir * n2;
+    int base, stride;
+    if (dir == 0) { base = n * li; stride = 1; }
+    else if (dir == 1) { base = (li % n) + n2 * (li / n); stride = n; }
+    else { base = li; stride = n2; }
     const float* P = Pvol + (size_t)e * 7 * n3;
-    stage_bytes(B, P + n3, 3 * n3 * 4, bulk, &bar[b]);                 // u, v, w
-    stage_bytes(B + 3 * n3 * 4, P + 5 * n3, n3 * 4, bulk, &bar[b]);    // T
-    stage_bytes(B + round16(L::slots), E2S + (size_t)e * 12, 48, bulk, &bar[b]);
-    if (tid == 32) {
-      const float* m = Met + (size_t)e * 10 * n3;
-      if (bulk_ok(m, m, 10 * n3 * 4)) bulk_prefetch_l2(m, 10 * n3 * 4);
-    }
-  };
-  issue(blockIdx.x, 0);
-  int k = 0;
-  for (int e = blockIdx.x; e < nElems; e += gridDim.x, ++k) {
-    const int cb = k & 1;
-    const int en = e + gridDim.x;
-    if (en < nElems) issue(en, cb ^ 1);  // the other buffer was released at the end of the last element
-    __syncthreads();                     // the threads' own copies
-    if (__syncthreads_or(!mbar_wait(&bar[cb], (k >> 1) & 1, err))) {
-      if (en < nElems) mbar_wait(&bar[cb ^ 1], ((k + 1) >> 1) & 1, nullptr);
-      return;
-    }
-    const float* const Ps = reinterpret_cast<const float*>(smem_raw + (size_t)cb * L::buffer);  // u, v, w, T
-    const int* const es = reinterpret_cast<const int*>(smem_raw + (size_t)cb * L::buffer + round16(L::slots));
-    if (tid >= 64 && tid < 70) {
-      // the face rows the finish reads: u, v, w (rows 1-3) and T (row 5) of both traces, the normal
-      // (rows 0-2) and SurfElem (row 9) of the geometry; pulled into L2 while the lines differentiate
-      const size_t side = (size_t)es[(tid - 64) * 2];
-      const float* pm = Pf + side * 6 * n2;
-      const float* ps = Pf + ((size_t)nSides + side) * 6 * n2;
-      const float* fg = Fgeo + side * 10 * n2;
-      if (bulk_ok(pm, ps, n2 * 4) && bulk_ok(fg, fg, n2 * 4)) {
-        bulk_prefetch_l2(pm + n2, 3 * n2 * 4);
-        bulk_prefetch_l2(pm + 5 * n2, n2 * 4);
-        bulk_prefetch_l2(ps + n2, 3 * n2 * 4);
-        bulk_prefetch_l2(ps + 5 * n2, n2 * 4);
-        bulk_prefetch_l2(fg, 3 * n2 * 4);
-        bulk_prefetch_l2(fg + 9 * n2, n2 * 4);
-      }
-    }
-    {
-      const int dir = tid / n2, li = tid - dir * n2;
-      int base, stride;
-      if (dir == 0) { base = n * li; stride = 1; }
-      else if (dir == 1) { base = (li % n) + n2 * (li / n); stride = n; }
-      else { base = li; stride = n2; }
-      float x[4][n];
+    const int slot[4] = {1, 2, 3, 5};  // u, v, w, T
+    float x[4][n];
 #pragma unroll
-      for (int c = 0; c < 4; ++c) line_load<NP>(Ps + c * n3, dir, base, stride, x[c]);
-      float* R0 = red + (dir == 0 ? 0 : (dir == 1 ? OFF1 : OFF2));
-      const int Pd = dir == 0 ? P0 : (dir == 1 ? P1 : P2);
+    for (int l = 0; l < n; ++l)
 #pragma unroll
-      for (int i = 0; i < n; ++i)
+      for (int c = 0; c < 4; ++c) x[c][l] = P[slot[c] * n3 + base + l * stride];
+    float* R0 = red + (dir == 0 ? 0 : (dir == 1 ? OFF1 : OFF2));
+    const int Pd = dir == 0 ? P0 : (dir == 1 ? P1 : P2);
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          float sacc = 0.f;
-#pragma unroll
-          for (int l = 0; l < n; ++l) sacc = sacc + lb.D[i + n * l] * x[c][l];
-          R0[(c * n + i) * Pd + li] = sacc;
-        }
-    }
-    __syncthreads();
-    const int* e2s = es;
-    const int liftc[4] = {1, 2, 3, 5};
-    for (int node = tid; node < n3; node += blockDim.x) {
-      const int i = node % n, j = (node / n) % n, kk = node / n2;
-      const float* M = Met + (size_t)e * 10 * n3 + node;
-      const float sj = M[9 * n3];
-      const float mf[3] = {sj * M[0], sj * M[n3], sj * M[2 * n3]}, mg[3] = {sj * M[3 * n3], sj * M[4 * n3], sj * M[5 * n3]},
-                  mh[3] = {sj * M[6 * n3], sj * M[7 * n3], sj * M[8 * n3]};
-      float g[3][4];
+    for (int i = 0; i < n; ++i)
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
-        const float gxi = red[(c * n + i) * P0 + j + n * kk];
-        const float geta = red[OFF1 + (c * n + j) * P1 + i + n * kk];
-        const float gzeta = red[OFF2 + (c * n + k) * P2 + i + n * j];
+        float s = 0.f;
 #pragma unroll
-        for (int d = 0; d < 3; ++d) g[d][c] = mf[d] * gxi + mg[d] * geta + mh[d] * gzeta;
+        for (int l = 0; l < n; ++l) s = s + lb.D[i + n * l] * x[c][l];
+        R0[(c * n + i) * Pd + li] = s;
       }
-      // surface part of the faces the node lies on, one normal direction after the other
+  }
+  __syncthreads();
+  const int* e2s = es;
+  const int liftc[4] = {1, 2, 3, 5};
+  for (int node = tid; node < n3; node += blockDim.x) {
+    const int i = node % n, j = (node / n) % n, k = node / n2;
+    const float* M = Met + (size_t)e * 10 * n3 + node;
+    const float sj = M[9 * n3];
+    const float mf[3] = {sj * M[0], sj * M[n3], sj * M[2 * n3]}, mg[3] = {sj * M[3 * n3], sj * M[4 * n3], sj * M[5 * n3]},
+                mh[3] = {sj * M[6 * n3], sj * M[7 * n3], sj * M[8 * n3]};
+    float g[3][4];
 #pragma unroll
-      for (int f = 0; f < 6; ++f) {
-        int ls, a, b;
-        if (!node_face<NP>(f, i, j, kk, ls, a, b)) continue;
-        const int side = e2s[(ls - 1) * 2 + 0], flip = e2s[(ls - 1) * 2 + 1];
-        int p, q;
-        s2v2_inv(N, a, b, flip, ls, p, q);
-        const int pq = p + n * q;
-        const float* pm = Pf + (size_t)side * 6 * n2 + pq;
-        const float* ps = Pf + ((size_t)nSides + side) * 6 * n2 + pq;
-        const float* fg = Fgeo + (size_t)side * 10 * n2 + pq;
-        const float Lhat = is_minus(ls) ? lb.lhm0 : lb.lhpN;
-        const float wgt = Lhat * 0.5f * fg[9 * n2] * sj;
-        const float nvv[3] = {wgt * fg[0], wgt * fg[n2], wgt * fg[2 * n2]};
+    for (int c = 0; c < 4; ++c) {
+      const float gxi = red[(c * n + i) * P0 + j + n * k];
+      const float geta = red[OFF1 + (c * n + j) * P1 + i + n * k];
+      const float gzeta = red[OFF2 + (c * n + k) * P2 + i + n * j];
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          const float fl = -pm[liftc[c] * n2] + ps[liftc[c] * n2];
+      for (int d = 0; d < 3; ++d) g[d][c] = mf[d] * gxi + mg[d] * geta + mh[d] * gzeta;
+    }
+    // surface part of the faces the node lies on, one normal direction after the other
 #pragma unroll
-          for (int d = 0; d < 3; ++d) g[d][c] = g[d][c] + fl * nvv[d];
-        }
+    for (int f = 0; f < 6; ++f) {
+      int ls, a, b;
+      if (!node_face<NP>(f, i, j, k, ls, a, b)) continue;
+      const int side = e2s[(ls - 1) * 2 + 0], flip = e2s[(ls - 1) * 2 + 1];
+      int p, q;
+      s2v2_inv(N, a, b, flip, ls, p, q);
+      const int pq = p + n * q;
+      const float* pm = Pf + (size_t)side * 6 * n2 + pq;
+      const float* ps = Pf + ((size_t)nSides + side) * 6 * n2 + pq;
+      const float* fg = Fgeo + (size_t)side * 10 * n2 + pq;
+      const float Lhat = is_minus(ls) ? lb.lhm0 : lb.lhpN;
+      const float wgt = Lhat * 0.5f * fg[9 * n2] * sj;
+      const float nvv[3] = {wgt * fg[0], wgt * fg[n2], wgt * fg[2 * n2]};
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const float fl = -pm[liftc[c] * n2] + ps[liftc[c] * n2];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) g[d][c] = g[d][c] + fl * nvv[d];
       }
-      float* G = Gvol + (size_t)e * 15 * n3 + node;
+    }
+    float* G = Gvol + (size_t)e * 15 * n3 + node;
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) G[(d * 5 + 1 + c) * n3] = g[d][c];
+    // face traces: on Gauss-Lobatto nodes the node's own gradient
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+      int ls, a, b;
+      if (!node_face<NP>(f, i, j, k, ls, a, b)) continue;
+      const int side = e2s[(ls - 1) * 2 + 0], flip = e2s[(ls - 1) * 2 + 1];
+      int p, q;
+      s2v2_inv(N, a, b, flip, ls, p, q);
+      float* gf = Gf + (((size_t)(flip == 0 ? 0 : 1) * nSides + side) * 15) * n2 + p + n * q;
 #pragma unroll
       for (int d = 0; d < 3; ++d)
 #pragma unroll
-        for (int c = 0; c < 4; ++c) G[(d * 5 + 1 + c) * n3] = g[d][c];
-      // face traces: on Gauss-Lobatto nodes the node's own gradient
-#pragma unroll
-      for (int f = 0; f < 6; ++f) {
-        int ls, a, b;
-        if (!node_face<NP>(f, i, j, kk, ls, a, b)) continue;
-        const int side = e2s[(ls - 1) * 2 + 0], flip = e2s[(ls - 1) * 2 + 1];
-        int p, q;
-        s2v2_inv(N, a, b, flip, ls, p, q);
-        float* gf = Gf + (((size_t)(flip == 0 ? 0 : 1) * nSides + side) * 15) * n2 + p + n * q;
-#pragma unroll
-        for (int d = 0; d < 3; ++d)
-#pragma unroll
-          for (int c = 0; c < 4; ++c) gf[(d * 5 + 1 + c) * n2] = g[d][c];
-      }
+        for (int c = 0; c < 4; ++c) gf[(d * 5 + 1 + c) * n2] = g[d][c];
     }
-    // this buffer is refilled by the bulk copies of the element after next, the sums by the next element
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
   }
 }
 

@@ -202,21 +202,8 @@ void rhs_front(dg_ctx* ctx, PrecData<R>& P, const S* U, const gx::Gas<R>& gas, c
         for (int t = 0; t < NP * NP; ++t) lb.D[t] = (float)ctx->B.D[t];
         lb.lhm0 = (float)ctx->B.Lhm[0];
         lb.lhpN = (float)ctx->B.Lhp[NP - 1];
-        if (ctx->lift_grid == 0) {
-          // persistent: every SM holds as many blocks as fit, each walks its share of the elements
-          int dev = 0, nsm = 0, occ = 0;
-          if (cudaGetDevice(&dev) == cudaSuccess &&
-              cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
-              cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gx::k_lift_lines<NP>, 3 * NP * NP,
-                                                            gx::LiftLinesSmem<NP>::bytes) == cudaSuccess &&
-              occ > 0)
-            ctx->lift_grid = nsm * occ;
-          else
-            ctx->lift_grid = ctx->nElems;  // one element per block
-        }
-        const int lg = ctx->nElems < ctx->lift_grid ? ctx->nElems : ctx->lift_grid;
-        gx::k_lift_lines<NP><<<lg, 3 * NP * NP, gx::LiftLinesSmem<NP>::bytes, st>>>(
-            P.Pvol.p, P.Met.p, P.Pf.p, P.Fgeo.p, ctx->E2S.p, lb, ctx->nElems, ctx->nSides, P.Gvol.p, P.Gf.p, ctx->kerr.p);
+        gx::k_lift_lines<NP><<<ctx->nElems, 3 * NP * NP, 0, st>>>(P.Pvol.p, P.Met.p, P.Pf.p, P.Fgeo.p, ctx->E2S.p, lb,
+                                                                  ctx->nElems, ctx->nSides, P.Gvol.p, P.Gf.p);
         lines = true;
       }
     }
