@@ -143,3 +143,29 @@ def test_mixed_split_forms(N, split):
         err = rel(Ut.cpu().numpy(), ref)
         op.close()
         assert err <= 1e-5, (N, split, parabolic, err)
+
+
+@pytest.mark.parametrize("N", [3, 4, 5, 6, 7])
+def test_mixed_persistent_kernels_walk_several_elements(N):
+    """The mixed form's persistent kernels on Gauss-Lobatto nodes (k_volume_lines at n = 4..8,
+    k_prolong_gl at n = 6, 8) run one block per SM slot and let each block walk several elements,
+    swapping its two shared-memory buffers; on a 12^3 mesh every block takes more than one element
+    (n = 4, 6, 8 copy by bulk copies, n = 5, 7 by the threads).  The RHS and two LSERK steps against
+    the oracle."""
+    R = 71.42857
+    kw = dict(Riemann="roe", parabolic=True, mu0=2e-3, SplitDG="pi")
+    m = gx.Mesh(N, 2, 12, 12, 12, (-math.pi,) * 3, (math.pi,) * 3)
+    U = state(m, 300 + N, R)
+    o = Oracle(gx.config(N=N, R=R, **kw), m)
+    ref = o.rhs(U)
+    op = gx.DG(gx.config(N=N, R=R, precision="mixed", **kw), m)
+    Ud = torch.from_numpy(U.copy()).cuda()
+    Ut = op.DGTimeDerivative_weakForm(0.0, Ud)
+    torch.cuda.synchronize()
+    assert rel(Ut.cpu().numpy(), ref) <= 1e-5, N
+    dt, _ = o.calc_timestep(U, 0.8, 0.8)
+    ref2, _ = o.lserk_steps(U, dt, 2)
+    op.TimeStepByLSERKW2(0.0, dt, Ud, torch.zeros_like(Ud), nSteps=2)
+    torch.cuda.synchronize()
+    assert rel(Ud.cpu().numpy(), ref2) <= 1e-6, N
+    op.close()
