@@ -500,7 +500,7 @@ k_prolong_gl(const double* __restrict__ U, const int* __restrict__ E2S, Gas<floa
 }
 
 template <int NP>
-__global__ void __launch_bounds__(3 * NP * NP, 4)
+__global__ void __launch_bounds__(3 * NP * NP, 6)
 k_lift_lines(const float* __restrict__ Pvol, const float* __restrict__ Met, const float* __restrict__ Pf,
              const float* __restrict__ Fgeo, const int* __restrict__ E2S, LiftBasis<NP> lb, int nElems, int nSides,
              float* __restrict__ Gvol, float* __restrict__ Gf) {
