@@ -658,9 +658,9 @@ k_bc_face(const R* __restrict__ Pf, const R* __restrict__ Gf, const R* __restric
 // =====================================================================================
 // k_face: FillFlux (fillflux.f90:45-172): Riemann + ViscousFlux + SurfElem, thread per face node
 // (128-thread blocks, at most 128 registers: four blocks per SM instead of one 256-thread block; the
-// FP32 form, which streams its face data, six)
+// FP32 form, which streams its face data, eight at 64 registers)
 // =====================================================================================
-template <typename R> struct FaceMinBlocks { static constexpr int v = sizeof(R) == 4 ? 6 : 4; };
+template <typename R> struct FaceMinBlocks { static constexpr int v = sizeof(R) == 4 ? 8 : 4; };
 template <typename R>
 __global__ void __launch_bounds__(128, FaceMinBlocks<R>::v)
 k_face(const R* __restrict__ Uf, const R* __restrict__ Pf, const R* __restrict__ Gf, const R* __restrict__ Fgeo,
