@@ -22,6 +22,7 @@
 #pragma once
 #include "dg_physics.cuh"
 #include "dg_bc.cuh"
+#include "dg_tma.cuh"
 
 namespace gx {
 
@@ -333,6 +334,25 @@ k_lift(const R* __restrict__ Pvol, const R* __restrict__ Met, const R* __restric
   const int nloc = min(EPB, L.nElems - e0);
   const int liftc[5] = {0, 1, 2, 3, 5};
   const bool facepass = !L.gauss && !L.br2;
+  if constexpr (sizeof(R) == 4 && EPB == 1) {
+    // FP32 form: the metric terms and the six faces' traces and geometry, read after the volume part,
+    // are pulled into L2 while the block loads and differentiates its primitives
+    if (threadIdx.x == 32 && nloc > 0) {
+      const R* m = Met + (size_t)e0 * 10 * n3;
+      if (bulk_ok(m, m, 10 * n3 * sizeof(R))) bulk_prefetch_l2(m, 10 * n3 * sizeof(R));
+    }
+    if (threadIdx.x >= 64 && threadIdx.x < 70 && nloc > 0) {
+      const size_t side = (size_t)E2S[((size_t)e0 * 6 + threadIdx.x - 64) * 2];
+      const R* pm = Pf + side * 6 * n2;
+      const R* ps = Pf + ((size_t)L.nSides + side) * 6 * n2;
+      const R* fg = Fgeo + side * 10 * n2;
+      if (bulk_ok(pm, ps, 6 * n2 * sizeof(R)) && bulk_ok(fg, fg, 10 * n2 * sizeof(R))) {
+        bulk_prefetch_l2(pm, 6 * n2 * sizeof(R));
+        bulk_prefetch_l2(ps, 6 * n2 * sizeof(R));
+        bulk_prefetch_l2(fg, 10 * n2 * sizeof(R));
+      }
+    }
+  }
   const R sigflux = (L.lift_mode == 2) ? R(1) : R(-1);
   for (int t = threadIdx.x; t < nloc * 5 * n3; t += blockDim.x) {
     int el = t / (5 * n3), r = t - el * 5 * n3;
