@@ -808,6 +808,22 @@ k_volume(const S* __restrict__ U, const R* __restrict__ Pvol, const R* __restric
   const int nloc = min(EPB, L.nElems - e0);
   const int tid = threadIdx.x;
   const bool active = tid < nloc * n3;
+  if constexpr (sizeof(R) == 4 && EPB == 1 && std::is_same<S, double>::value) {
+    // FP32 form: the six faces' fluxes and the FP64 state and RK register, read by the surface
+    // integral and the stage update at the end, are pulled into L2 while the volume part runs
+    if (tid == 32 && nloc > 0 && rkmode) {
+      const double* u = rk.U + (size_t)e0 * 5 * n3;
+      const double* r = rk.Ut_tmp + (size_t)e0 * 5 * n3;
+      if (bulk_ok(u, r, 5 * n3 * 8)) {
+        bulk_prefetch_l2(u, 5 * n3 * 8);
+        bulk_prefetch_l2(r, 5 * n3 * 8);
+      }
+    }
+    if (tid >= 64 && tid < 70 && nloc > 0) {
+      const R* fx = Flux + (size_t)E2S[((size_t)e0 * 6 + tid - 64) * 2] * 5 * n2;
+      if (bulk_ok(fx, fx, 5 * n2 * sizeof(R))) bulk_prefetch_l2(fx, 5 * n2 * sizeof(R));
+    }
+  }
   const int el = tid / n3, node = tid - (tid / n3) * n3;
   const int e = e0 + el;
   const int i = node % n, j = (node / n) % n, k = node / n2;
