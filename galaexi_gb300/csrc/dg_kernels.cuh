@@ -317,7 +317,9 @@ k_bc_lift_ghost(R* __restrict__ Pf, const R* __restrict__ Fgeo, Gas<R> gas, Laun
 // FP32 (mixed form) blocks of at most 256 threads: four blocks per SM (at most 72 registers); the
 // FP32 kernel is latency bound, and at two blocks per SM (107 registers at N=5) only 14 warps hid it
 template <int NP, typename R> struct LiftMinBlocks {
-  static constexpr int v = (sizeof(R) == 4 && EPBof<NP>::v * NP * NP * NP <= 256) ? 4 : 2;
+  // FP32: four blocks per SM for blocks of at most 256 threads, five for one element of 216 (N = 5)
+  static constexpr int v =
+      (sizeof(R) == 4 && EPBof<NP>::v * NP * NP * NP <= 256) ? (EPBof<NP>::v == 1 ? 5 : 4) : 2;
 };
 
 template <int NP, typename R, int V0 = 0>
