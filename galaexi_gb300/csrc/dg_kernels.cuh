@@ -135,8 +135,10 @@ __host__ __device__ constexpr int lift_ps_slots(int NP) { return 5 * NP * NP * N
 // work is only E - ke and p - p_ref once its conversions run on the integer pipes (latency bound).
 // =====================================================================================
 template <int NP, typename R> struct ProlongMinBlocks {
-  // three blocks per SM where they fit the SM's 2048 threads (the mixed form up to N = 7), else two
-  static constexpr int v = (OffsetOf<R>::v && 3 * EPBof<NP>::v * NP * NP * NP <= 2048) ? 3 : 2;
+  // three blocks per SM where they fit the SM's 2048 threads (the mixed form up to N = 7), else two;
+  // the mixed form's element of 216 threads (N = 5) five
+  static constexpr int v =
+      (OffsetOf<R>::v && NP == 6) ? 5 : ((OffsetOf<R>::v && 3 * EPBof<NP>::v * NP * NP * NP <= 2048) ? 3 : 2);
 };
 template <int NP, typename R, typename S = double>
 __global__ void __launch_bounds__(EPBof<NP>::v * NP * NP * NP, ProlongMinBlocks<NP, R>::v)
